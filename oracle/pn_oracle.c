@@ -1,0 +1,72 @@
+/*
+ * pn_oracle.c -- CPU restatement of PointNeighbors.jl's GridNeighborhoodSearch +
+ * FullGridCellList (ParallelUpdate), TrivialNeighborhoodSearch and the benchmark pair
+ * functions.  TEST INFRASTRUCTURE ONLY: the checker for the CUDA library, never part of
+ * the product path.  Build: oracle/build_oracle.py (gcc -O2 -fopenmp -ffp-contract=off).
+ *
+ * Reference files followed (paths inside PointNeighbors.jl v0.6.7):
+ *   src/util.jl:2-34                      extract_svector, floor_to_int
+ *   src/cell_lists/full_grid.jl:48-212    FullGridCellList ctor, cell coords, bounds check
+ *   src/vector_of_vectors.jl:93-121       pushat_atomic!, "cell list is full"
+ *   src/nhs_grid.jl:77-129,255-281        Grid NHS ctor, initialize_grid! (ParallelUpdate)
+ *   src/nhs_grid.jl:519-638               traversal, neighboring_cells, periodic_cell_index
+ *   src/neighborhood_search.jl:183-453    foreach_point_neighbor, periodic distance/coords
+ *   src/nhs_trivial.jl:21-55              brute-force TrivialNeighborhoodSearch
+ *   benchmarks/n_body.jl:16-55            n-body pair function
+ * The WCSPH pair functions (Wendland C2, Tait EOS, Monaghan viscosity) are the workload's
+ * own definitions; the reference delegates them to TrixiParticles, which is not vendored.
+ */
+#include "pn_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PNO_CAT_(a, b) a##b
+#define PNO_CAT(a, b) PNO_CAT_(a, b)
+
+#ifndef M_PI
+#define M_PI 3.14159265358979323846
+#endif
+
+/* Julia Int64 arithmetic wraps around. */
+static inline int64_t pno_wadd(int64_t a, int64_t b) { return (int64_t)((uint64_t)a + (uint64_t)b); }
+static inline int64_t pno_wsub(int64_t a, int64_t b) { return (int64_t)((uint64_t)a - (uint64_t)b); }
+/* Julia `mod(x, n)` for n > 0: result in [0, n). */
+static inline int64_t pno_mod(int64_t x, int64_t n) {
+  int64_t r = x % n;
+  if (r != 0 && ((r < 0) != (n < 0))) r += n;
+  return r;
+}
+
+/* Wendland C2 kernel with support 2h: W = sigma_d (1 - q/2)^4 (2q + 1), q = r/h. */
+static inline double pno_wendland_sigma(int d, double h) {
+  if (d == 3) return 21.0 / (16.0 * M_PI * h * h * h);
+  if (d == 2) return 7.0 / (4.0 * M_PI * h * h);
+  return 5.0 / (8.0 * h);
+}
+static inline double pno_wendland_w(int d, double h, double r) {
+  const double q = r / h;
+  if (q >= 2.0) return 0.0;
+  const double t = 1.0 - 0.5 * q;
+  return pno_wendland_sigma(d, h) * t * t * t * t * (2.0 * q + 1.0);
+}
+/* dW/dr = sigma_d / h * (-5 q) (1 - q/2)^3 */
+static inline double pno_wendland_dw(int d, double h, double r) {
+  const double q = r / h;
+  if (q >= 2.0) return 0.0;
+  const double t = 1.0 - 0.5 * q;
+  return pno_wendland_sigma(d, h) / h * (-5.0 * q) * t * t * t;
+}
+
+#define T float
+#define S f32
+#include "pn_oracle_body.h"
+#undef T
+#undef S
+
+#define T double
+#define S f64
+#include "pn_oracle_body.h"
+#undef T
+#undef S

@@ -1,0 +1,212 @@
+"""Pin the CPU oracle against the known answers of the reference's own test suite.
+
+The reference (Julia) cannot run here, so these vectors -- transcribed from its tests in
+tests/golden/make_golden.py -- are what makes the oracle trustworthy as the checker for
+the CUDA path.  CPU only.
+"""
+import numpy as np
+import pytest
+
+from conftest import jfloat
+
+
+def test_floor_to_int_saturates(O):
+    # src/util.jl:19-34
+    t63 = 2**63 - 1
+    for dt in (np.float32, np.float64):
+        assert O.floor_to_int(float("inf"), dt) == t63
+        assert O.floor_to_int(float("nan"), dt) == t63
+        assert O.floor_to_int(-float("inf"), dt) == -t63 - 1
+        assert O.floor_to_int(2.0**63, dt) == t63
+        assert O.floor_to_int(-(2.0**63), dt) == -t63 - 1
+        assert O.floor_to_int(-1.5, dt) == -2
+        assert O.floor_to_int(2.9999, dt) == 2
+
+
+def test_cell_coords_limits(O, golden):
+    c = golden["cell_coords_limits"]
+    gd = O.grid_create(2, c["radius"], [0.0, 0.0], [1.0, 1.0])  # geometry only
+    gf = O.grid_create(2, c["radius"], c["full_grid"]["min_corner"], c["full_grid"]["max_corner"])
+    for x, ed, ef in zip(c["coords"], c["dict_expected"], c["full_expected"]):
+        xv = np.array([jfloat(v) for v in x])
+        assert O.cell_coords_dict(gd, xv) == tuple(ed)
+        assert O.cell_coords(gf, xv) == tuple(ef)
+
+
+def _dict_grid(O, ndims, r, box=None):
+    mn = [0.0] * ndims
+    mx = [1.0] * ndims
+    return O.grid_create(ndims, r, mn, mx, periodic_box=box)
+
+
+@pytest.mark.parametrize("case", ["rect_2d", "rect_3d"])
+def test_rectangular_candidates_dictionary(O, golden, case):
+    c = golden[case]
+    base = np.array(c["coords"])
+    d = base.shape[1]
+    for chk in c["checks"]:
+        y = base + np.array(chk["shift"])
+        q = np.array(chk["query"])
+        if chk.get("query_shifted"):
+            q = q + np.array(chk["shift"])
+        g = _dict_grid(O, d, chk["radius"])
+        got = sorted((O.eachneighbor_dict(g, y, q) + 1).tolist())
+        assert got == chk["expected"]
+
+
+def test_eachindex_y_full_grid(O, golden):
+    c = golden["eachindex_y_3d"]
+    c1 = np.array(c["coords"])
+    shift = np.array(c["shift"])
+    c2 = c1 + shift
+    mn = np.minimum(c1.min(axis=0), c2.min(axis=0))
+    mx = np.maximum(c1.max(axis=0), c2.max(axis=0))
+    g = O.grid_create(3, c["radius"], mn, mx)
+    O.build(g, c1)  # initialize! with all points
+    lo, hi = c["eachindex_y"]
+    cl = O.build(g, c2, idx=np.arange(lo - 1, hi))  # update! (full rebuild) with a subset
+    q1 = np.array(c["query1"])
+    assert sorted((O.eachneighbor(g, cl, q1) + 1).tolist()) == c["expected1"]
+    q2 = q1 + shift
+    assert sorted((O.eachneighbor(g, cl, q2) + 1).tolist()) == c["expected2"]
+
+
+def _periodic_setup(s):
+    y = np.array(s["coords"], dtype=np.float64)
+    bmin = np.array(s["box_min"])
+    bmax = np.array(s["box_max"])
+    if "offset" in s:
+        off = np.array(s["offset"])
+        y = y - off
+        bmin = bmin - off
+        bmax = bmax - off
+    return y, bmin, bmax
+
+
+def test_periodic_candidates(O, golden):
+    c = golden["periodic_candidates"]
+    for s in c["setups"]:
+        y, bmin, bmax = _periodic_setup(s)
+        d = y.shape[1]
+        # FullGridCellList over the periodic box
+        g = O.grid_create(d, c["radius"], bmin, bmax, periodic_box=(bmin, bmax))
+        cl = O.build(g, y)
+        # DictionaryCellList
+        gd = O.grid_create(d, c["radius"], bmin, bmax, periodic_box=(bmin, bmax))
+        for i, exp in enumerate(c["expected"]):
+            assert sorted((O.eachneighbor(g, cl, y[i]) + 1).tolist()) == exp, s["name"]
+            assert sorted((O.eachneighbor_dict(gd, y, y[i]) + 1).tolist()) == exp, s["name"]
+
+
+def test_periodic_neighbors_grid_and_trivial(O, golden):
+    c = golden["periodic_neighbors"]
+    for s in c["setups"]:
+        y, bmin, bmax = _periodic_setup(s)
+        d = y.shape[1]
+        g = O.grid_create(d, c["radius"], bmin, bmax, periodic_box=(bmin, bmax))
+        cl = O.build(g, y)
+        off, nb = O.neighbor_lists(g, cl, y, y)
+        toff, tnb = O.trivial_lists(g, y, y)
+        for i, exp in enumerate(c["expected"]):
+            assert sorted((nb[off[i]:off[i + 1]] + 1).tolist()) == exp, s["name"]
+            assert sorted((tnb[toff[i]:toff[i + 1]] + 1).tolist()) == exp, s["name"]
+
+
+def test_split_cells(O, golden):
+    c = golden["split_cells"]
+    y = np.array(c["coords"])
+    bmin, bmax = np.array(c["box_min"]), np.array(c["box_max"])
+    g = O.grid_create(2, c["radius"], bmin, bmax, periodic_box=(bmin, bmax))
+    for i, exp in enumerate(c["expected"]):
+        got = sorted(set((O.eachneighbor_dict(g, y, y[i]) + 1).tolist()))
+        assert got == exp
+
+
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_periodic_rounding(O, golden, dt):
+    c = golden["periodic_rounding"]
+    bmin = np.array(c["box_min"], dtype=dt)
+    bmax = np.array(c["box_max"], dtype=dt)
+    g = O.grid_create(2, dt(c["radius"]), bmin, bmax, periodic_box=(bmin, bmax), dtype=dt)
+    size = bmax - bmin
+    for x in c["coords"]:
+        xv = np.array([jfloat(v, dt) for v in x], dtype=dt)
+        xp = O.periodic_coords(g, xv)
+        assert np.all(bmin <= xp) and np.all(xp <= bmax)
+        for k in range(2):
+            assert xp[k] in (xv[k], dt(xv[k] - size[k]), dt(xv[k] + size[k]))
+        cell = O.cell_coords(g, xv)
+        assert cell == O.cell_coords(g, xp)
+        assert all(2 <= cell[k] <= g.n_cells[k] + 1 for k in range(2))
+
+
+@pytest.mark.parametrize("ndims", [1, 2, 3])
+def test_full_grid_bounds(O, golden, ndims):
+    c = golden["full_grid_bounds"]
+    mn = [c["min_corner"]] * ndims
+    mx = [c["max_corner"]] * ndims
+    g = O.grid_create(ndims, c["radius"], mn, mx)
+    assert list(g.min_pad)[:ndims] == [c["expected_min_pad"]] * ndims
+    assert list(g.max_pad)[:ndims] == [c["expected_max_pad"]] * ndims
+    rng = np.random.default_rng(0)
+    y = rng.random((10, ndims))
+    for phase in ("initialize", "update"):
+        for val, fails in c[phase]:
+            y[6, 0] = jfloat(val)  # y[1, 7] in the reference's 1-based (d, N) indexing
+            if fails:
+                with pytest.raises(O.OracleError) as e:
+                    O.build(g, y)
+                assert e.value.status == O.PNO_ERR_OUT_OF_DOMAIN
+            else:
+                O.build(g, y)
+
+
+def test_gpu_tutorial_extrema(O, golden):
+    c = golden["gpu_tutorial"]
+    from __graft_entry__ import package
+    W = package().workloads
+    y = W.lattice(c["n_per_dim"], dtype=np.float32)
+    g = O.grid_create(2, np.float32(c["radius"]), y.min(axis=0), y.max(axis=0),
+                      dtype=np.float32)
+    cl = O.build(g, y)
+    cnt = O.foreach(g, cl, y, y, O.F_COUNT)
+    assert (int(cnt.min()), int(cnt.max())) == tuple(c["expected_extrema"])
+
+
+def test_cell_full(O):
+    y = np.array([[0.5, 0.5]] * 5)
+    g = O.grid_create(2, 1.0, [0.0, 0.0], [1.0, 1.0], max_ppc=4)
+    with pytest.raises(O.OracleError) as e:
+        O.build(g, y)
+    assert e.value.status == O.PNO_ERR_CELL_FULL
+
+
+CLOUDS = [(10, 11), (100, 90), (9, 10, 7), (39, 40, 41)]
+
+
+@pytest.mark.parametrize("shape", CLOUDS)
+@pytest.mark.parametrize("seed", [1, 2])
+def test_grid_equals_trivial(O, pkg, shape, seed):
+    """test/neighborhood_search.jl:186-469: Grid + FullGrid neighbour lists equal brute
+    force, initialize! with seed 1 then (seed 2) update! with other coordinates."""
+    W = pkg.workloads
+    r = 2.5
+    coords = W.reference_test_cloud(shape, r, seed=seed)
+    coords_init = W.reference_test_cloud(shape, r, seed=1)
+    d = len(shape)
+    mn = coords.min(axis=0) - r
+    mx = coords.max(axis=0) + r
+    g = O.grid_create(d, r, mn, mx)
+    cl = O.build(g, coords_init)
+    if seed != 1:
+        # update! after an initialize! with other coordinates (full rebuild semantics)
+        cl = O.build(g, coords)
+    toff, tnb = O.trivial_lists(g, coords, coords)
+    off, nb = O.neighbor_lists(g, cl, coords, coords)
+    assert np.array_equal(off, toff)
+    for i in range(coords.shape[0]):
+        assert np.array_equal(np.sort(nb[off[i]:off[i + 1]]), tnb[toff[i]:toff[i + 1]])
+    # mapreduce_neighbor(+, ...) of the neighbour index (1-based)
+    isum = O.foreach(g, cl, coords, coords, O.F_INDEX_SUM)
+    expect = np.array([int((tnb[toff[i]:toff[i + 1]] + 1).sum()) for i in range(coords.shape[0])])
+    assert np.array_equal(isum, expect)
