@@ -1,0 +1,226 @@
+/*
+ * pn_gb300.h -- C ABI of libpn_gb300.so: PointNeighbors.jl's GridNeighborhoodSearch over a
+ * FullGridCellList, implemented as CUDA kernels for GB300 (sm_103a).
+ *
+ * The entry points are what a Julia `ccall` binding of the reference's API for this path
+ * needs.  Each declaration cites the reference function it replaces (paths inside
+ * PointNeighbors.jl v0.6.7).
+ *
+ * Conventions
+ *  - Coordinates use the reference's memory layout: a Julia `T[d, N]` column-major matrix,
+ *    i.e. point-major (x1 y1 z1 x2 y2 z2 ...).  T is Float32 or Float64 and equals the
+ *    eltype of the search radius and of the corners (pn_config.dtype).
+ *  - All array arguments are DEVICE pointers owned by the caller.  Point indices are
+ *    0-based at this interface (the Julia binding subtracts 1).
+ *  - Calls are asynchronous on the given stream (a cudaStream_t; NULL = default stream).
+ *    Kernel-side errors (a point outside the grid, a full cell, ...) are recorded in a
+ *    sticky per-search error word: pn_sync() waits for the stream and returns it.
+ *  - A search is not thread-safe: one host thread at a time per handle.
+ *  - Scratch memory (cell arrays, the cell-sorted copy of the points) is owned by the
+ *    handle and allocated by pn_create / grown on demand.
+ *  - The pair function is a compile-time functor picked by `functor` (pn_functor); an
+ *    arbitrary Julia closure cannot be compiled into the library, and there is no CPU
+ *    fallback: unknown functors return PN_ERR_UNSUPPORTED_FUNCTOR.
+ */
+#ifndef PN_GB300_H
+#define PN_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PN_ABI_VERSION 1
+
+typedef struct pn_search pn_search; /* one GridNeighborhoodSearch{NDIMS} */
+typedef void* pn_stream_t;          /* cudaStream_t */
+
+typedef enum {
+  PN_OK = 0,
+  PN_ERR_OUT_OF_DOMAIN = 1,  /* "particle coordinates are NaN or outside the domain bounds
+                                of the cell list" (full_grid.jl:205-212)                   */
+  PN_ERR_INVALID_ARG = 2,    /* ArgumentError / bad sizes / eachindex_y out of bounds       */
+  PN_ERR_CUDA = 3,           /* a CUDA runtime error                                        */
+  PN_ERR_TIMEOUT = 4,        /* a bounded device-side wait gave up                          */
+  PN_ERR_UNSUPPORTED_FUNCTOR = 5,
+  PN_ERR_CELL_FULL = 6,      /* "cell list is full. Use a larger `max_points_per_cell`."
+                                (vector_of_vectors.jl:114-121), only when the limit is set  */
+  PN_ERR_NOT_INITIALIZED = 7,/* traversal before initialize, or on an empty template        */
+  PN_ERR_OUT_OF_MEMORY = 8,
+  PN_ERR_BOUNDS = 9,         /* a query point whose neighbouring cells are outside the grid
+                                (the reference's BoundsError in points_in_cell)             */
+  PN_ERR_CAPACITY = 10       /* neighbour-list output buffer too small                      */
+} pn_status;
+
+typedef enum { PN_FLOAT32 = 0, PN_FLOAT64 = 1 } pn_dtype;
+
+/* nhs_grid.jl:135-192 update strategies available for a FullGridCellList. */
+typedef enum {
+  PN_PARALLEL_UPDATE = 0,             /* full rebuild (the FullGridCellList default)       */
+  PN_PARALLEL_INCREMENTAL_UPDATE = 1  /* re-bin only points whose cell changed            */
+} pn_update_strategy;
+
+/* Pair functions (the `f` of foreach_point_neighbor), with their parameter structs. */
+typedef enum {
+  PN_F_COUNT = 0,          /* pn_count_params                                             */
+  PN_F_NEIGHBOR_LIST = 1,  /* pn_neighbor_list_params                                     */
+  PN_F_NBODY_ACCEL = 2,    /* pn_nbody_params    (benchmarks/n_body.jl:16-55)             */
+  PN_F_POTENTIAL = 3,      /* pn_potential_params                                         */
+  PN_F_WCSPH_DENSITY = 4,  /* pn_wcsph_params                                             */
+  PN_F_WCSPH_FORCE = 5,    /* pn_wcsph_params                                             */
+  PN_F_WCSPH_STEP = 6,     /* pn_wcsph_params: density + EOS, then force, one call        */
+  PN_F_INDEX_SUM = 7       /* pn_index_sum_params: mapreduce_neighbor(+) of j (1-based)   */
+} pn_functor;
+
+/* GridNeighborhoodSearch{NDIMS}(; search_radius, n_points, periodic_box,
+ *   cell_list = FullGridCellList(; min_corner, max_corner, search_radius,
+ *                                  max_points_per_cell), update_strategy)
+ * (nhs_grid.jl:77-129, full_grid.jl:48-82, neighborhood_search.jl:129-141). */
+typedef struct {
+  int32_t ndims;               /* 1, 2 or 3                                                 */
+  int32_t dtype;               /* pn_dtype                                                  */
+  double search_radius;        /* value in T (exactly representable)                        */
+  double min_corner[3];        /* FullGridCellList corners, unpadded, values in T           */
+  double max_corner[3];
+  int32_t periodic;            /* 1 if a PeriodicBox is given                               */
+  int32_t update_strategy;     /* pn_update_strategy                                        */
+  double periodic_min[3];      /* PeriodicBox corners, values in T                          */
+  double periodic_max[3];
+  int64_t n_points;            /* expected number of points in y (pre-sizes scratch)       */
+  int32_t max_points_per_cell; /* > 0: error like the reference when a cell exceeds it;
+                                  0: no limit (the CSR cell list has no fixed capacity)     */
+  int32_t flags;               /* reserved, must be 0                                       */
+} pn_config;
+
+/* Geometry as computed by the constructors (for tests and for the Julia binding's
+ * `cell_list.min_corner`, `nhs.n_cells`, `nhs.cell_size`). */
+typedef struct {
+  int32_t ndims, dtype, periodic, is_template;
+  int64_t grid_size[3];        /* padded FullGridCellList size per dimension               */
+  int64_t n_cells[3];          /* periodic cells per dimension, -1 when not periodic       */
+  double min_corner[3];        /* padded corners (min_corner - 1.001 r)                     */
+  double max_corner[3];
+  double cell_size[3];
+  double search_radius;
+  int64_t n_binned;            /* points in the cell list after the last initialize/update */
+  int64_t n_overflow;          /* points held in the incremental-update overflow lists     */
+} pn_grid_info;
+
+typedef struct { int32_t* counts; } pn_count_params;       /* out int32[n_queries]         */
+typedef struct { int64_t* sums; } pn_index_sum_params;     /* out int64[n_queries]         */
+
+/* Neighbour lists in CSR form: row q holds the neighbour indices j of query q.
+ * The call counts, writes offsets (exclusive scan, offsets[n_queries] = total), and if
+ * total <= capacity writes the rows (else sets PN_ERR_CAPACITY); sort_rows sorts each row
+ * ascending (the reference's test compares sorted lists). */
+typedef struct {
+  int32_t* counts;      /* out int32[n_queries] (may be NULL)                               */
+  int64_t* offsets;     /* out int64[n_queries + 1]                                         */
+  int32_t* neighbors;   /* out int32[capacity]                                              */
+  int64_t capacity;
+  int32_t sort_rows;
+  int32_t pad_;
+} pn_neighbor_list_params;
+
+/* benchmarks/n_body.jl:41-56: dv_i += -G m_j pos_diff / d^3 for d >= sqrt(eps(T)). */
+typedef struct {
+  const void* masses;   /* T[n_y]                                                           */
+  double G;
+  void* accel;          /* out T[n_queries * d]                                             */
+} pn_nbody_params;
+
+/* Truncated pair potential e_i = sum_j m_i m_j (1/d - 1/R) for 0 < d < R. */
+typedef struct {
+  const void* masses;   /* T[n]  (x == y)                                                   */
+  double cutoff;        /* R                                                                */
+  void* energy;         /* out T[n_queries]                                                 */
+} pn_potential_params;
+
+/* Weakly compressible SPH: Wendland C2 kernel (support 2h), Tait equation of state
+ * p = c0^2 rho0 / gamma ((rho/rho0)^gamma - 1), momentum equation with Monaghan artificial
+ * viscosity (alpha, beta = 0, mu = h v.x / (d^2 + eps_visc h^2)).
+ * DENSITY: density[i] = sum_j m W(d_ij) (self included), pressure[i] = EOS(density[i]).
+ * FORCE:   accel[i] = -sum_{j, d>r_min} m (p_i/rho_i^2 + p_j/rho_j^2 + Pi_ij) grad W_ij,
+ *          reading density, pressure, velocity (x == y required).
+ * STEP:    DENSITY then FORCE in one call. */
+typedef struct {
+  double mass, h, c0, rho0, gamma_exp, alpha, eps_visc;
+  double r_min;          /* pairs closer than this are skipped by FORCE (self pair)        */
+  void* density;         /* T[n]: out for DENSITY/STEP, in for FORCE                       */
+  void* pressure;        /* T[n]: out for DENSITY/STEP, in for FORCE                       */
+  const void* velocity;  /* T[n * d]: in for FORCE/STEP                                    */
+  void* accel;           /* T[n * d]: out for FORCE/STEP                                   */
+} pn_wcsph_params;
+
+/* ----------------------------------------------------------------- lifetime */
+
+/* GridNeighborhoodSearch{NDIMS}(...) with a FullGridCellList (nhs_grid.jl:77-129,
+ * full_grid.jl:48-82).  ArgumentError cases of the reference return PN_ERR_INVALID_ARG:
+ * integer-like radius is not representable here; periodic boxes with < 3 cells. */
+int pn_create(const pn_config* cfg, pn_search** out);
+
+/* copy_neighborhood_search(nhs, search_radius, n_points) (nhs_grid.jl:640-649,
+ * full_grid.jl:179-185): same corners, periodic box, strategy and cell capacity. */
+int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
+                   pn_search** out);
+
+int pn_destroy(pn_search* s);
+
+/* ----------------------------------------------------------------- cell list */
+
+/* initialize!(nhs, x, y; eachindex_y) -> initialize_grid! (nhs_grid.jl:220-281):
+ * bins the points y[:, eachindex_y] (all points when eachindex_y == NULL). */
+int pn_initialize(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
+                  int64_t n_eachindex_y, pn_stream_t stream);
+
+/* update!(nhs, x, y; points_moving, eachindex_y) (nhs_grid.jl:283-292, 408-477):
+ * a no-op when points_moving_y == 0; PN_PARALLEL_UPDATE rebuilds, the incremental
+ * strategy re-bins only points whose cell changed (it rejects eachindex_y subsets, like
+ * nhs_grid.jl:414-417). */
+int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
+              int64_t n_eachindex_y, int32_t points_moving_y, pn_stream_t stream);
+
+/* ----------------------------------------------------------------- traversal */
+
+/* foreach_point_neighbor(f, x, y, nhs; points) (neighborhood_search.jl:183-234,
+ * nhs_grid.jl:519-575).  Loops over the query points x[:, points] (all of x when
+ * points == NULL) and, for every neighbour j in y with d^2 <= r^2 (periodic images
+ * included, the point itself included), applies the functor.  The search must have been
+ * initialized/updated with this y.  Outputs are indexed like `points` (query order). */
+int pn_foreach_point_neighbor(pn_search* s, int32_t functor, const void* x, int64_t n_x,
+                              const void* y, int64_t n_y, const int32_t* points,
+                              int64_t n_points, const void* params, pn_stream_t stream);
+
+/* ----------------------------------------------------------------- status / tests */
+
+/* Wait for the stream of the last call and return (and clear) the sticky error. */
+int pn_sync(pn_search* s);
+/* Return the sticky error without waiting for queued kernels; clear it if `clear`. */
+int pn_get_error(pn_search* s, int32_t clear);
+const char* pn_status_string(int32_t status);
+
+/* requires_update(nhs) == (false, true) (nhs_grid.jl:133). */
+int pn_requires_update(const pn_search* s, int32_t out[2]);
+
+int pn_get_grid_info(const pn_search* s, pn_grid_info* out);
+
+/* The geometry pn_create would compute for `cfg` (FullGridCellList padding and cell
+ * counts, periodic n_cells and cell_size), on the host only: no device is touched. */
+int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out);
+
+/* cell_coords(x, nhs) (nhs_grid.jl:622-638, util.jl:19-34) for n points:
+ * out int64[n * ndims], the reference's 1-based (periodic) cell coordinates. */
+int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stream_t stream);
+
+/* The contents of the cell list (`cell_list[cell]` for every cell, full_grid.jl:165-169):
+ * counts int32[prod(grid_size)] per linear cell index, points int32[n_binned] with each
+ * cell's points ascending. */
+int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream);
+
+int pn_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,373 @@
+// pn_api.cu -- the C ABI of libpn_gb300 (include/pn_gb300.h): construction of a
+// GridNeighborhoodSearch over a FullGridCellList, its device scratch, and dispatch by dtype.
+//
+// Geometry follows the reference constructors exactly, in the element type T:
+//   FullGridCellList (full_grid.jl:48-82): corners padded by T(1001)/T(1000) * r,
+//     n = ceil(Int, (max - min) / r) cells per dimension, column-major linear indices;
+//   GridNeighborhoodSearch (nhs_grid.jl:77-129): with a PeriodicBox,
+//     n_cells = floor(Int, (size + 10 eps()) / r) in Float64, cell_size = size / n_cells in T,
+//     at least 3 cells per dimension.
+// This file is compiled with -ffp-contract=off for the host compiler as well, so these T
+// expressions are rounded exactly like Julia's.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "pn_internal.cuh"
+
+namespace pn {
+
+int cuda_status(cudaError_t e) { return e == cudaSuccess ? PN_OK : PN_ERR_CUDA; }
+
+static void free_points(pn_search* s) {
+  void* ptrs[] = {s->d_cell_of, s->d_slot_of, s->d_tmp_perm, s->d_perm, s->d_cell_of_slot,
+                  s->d_pos,     s->d_pa,      s->d_pb,       s->d_main_perm, s->d_ovf_list,
+                  s->d_ovf_cell, s->d_ovf_slot};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  s->d_cell_of = s->d_slot_of = s->d_tmp_perm = s->d_perm = s->d_cell_of_slot = nullptr;
+  s->d_main_perm = s->d_ovf_list = s->d_ovf_cell = s->d_ovf_slot = nullptr;
+  s->d_pos = s->d_pa = s->d_pb = nullptr;
+  s->cap = 0;
+}
+
+// Grow the point arrays to hold n points (2n slots).  Growing discards the cell list, so
+// it only happens at the start of a build.
+int ensure_capacity(pn_search* s, int64_t n) {
+  if (n <= s->cap) return PN_OK;
+  if (n > (int64_t)INT32_MAX / 2) return PN_ERR_INVALID_ARG;  // Int32 point indices
+  free_points(s);
+  const int64_t cap = n + n / 8 + 1024;
+  const size_t tb = s->dtype == PN_FLOAT64 ? 8 : 4;
+  const size_t i4 = sizeof(int32_t);
+  bool ok = true;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (ok && cudaMalloc(p, bytes) != cudaSuccess) ok = false;
+  };
+  alloc((void**)&s->d_cell_of, i4 * cap);
+  alloc((void**)&s->d_slot_of, i4 * cap);
+  alloc((void**)&s->d_tmp_perm, i4 * 2 * cap);
+  alloc((void**)&s->d_perm, i4 * 2 * cap);
+  alloc((void**)&s->d_cell_of_slot, i4 * 2 * cap);
+  alloc(&s->d_pos, tb * 4 * 2 * cap);
+  alloc(&s->d_pa, tb * 4 * 2 * cap);
+  alloc(&s->d_pb, tb * 4 * 2 * cap);
+  alloc((void**)&s->d_main_perm, i4 * cap);
+  alloc((void**)&s->d_ovf_list, i4 * cap);
+  alloc((void**)&s->d_ovf_cell, i4 * cap);
+  alloc((void**)&s->d_ovf_slot, i4 * cap);
+  if (!ok) {
+    free_points(s);
+    cudaGetLastError();
+    return PN_ERR_OUT_OF_MEMORY;
+  }
+  s->cap = cap;
+  s->initialized = false;
+  s->ovf_active = false;
+  s->main_perm_valid = false;
+  return PN_OK;
+}
+
+int ensure_qcount(pn_search* s, int64_t n) {
+  if (n <= s->qcount_cap) return PN_OK;
+  if (s->d_qcount) cudaFree(s->d_qcount);
+  s->d_qcount = nullptr;
+  s->qcount_cap = 0;
+  if (cudaMalloc(&s->d_qcount, sizeof(int32_t) * (n + 1)) != cudaSuccess) {
+    cudaGetLastError();
+    return PN_ERR_OUT_OF_MEMORY;
+  }
+  s->qcount_cap = n;
+  return PN_OK;
+}
+
+template <typename T>
+static int geometry(pn_search* s) {
+  const pn_config& c = s->cfg;
+  const int d = c.ndims;
+  const T r = (T)c.search_radius;
+  const T pad = (T)((T)1001 / (T)1000) * r;  // `1001 // 1000 * search_radius`
+  s->radius = (double)r;
+  s->is_template = (double)r < 2.220446049250313e-16 ? 1 : 0;  // search_radius < eps()
+  int64_t total = 1;
+  for (int k = 0; k < 3; ++k) {
+    s->grid_size[k] = 1;
+    s->n_cells[k] = -1;
+    s->min_pad[k] = s->max_pad[k] = 0.0;
+    s->cell_size[k] = 1.0;
+    s->box_size[k] = 0.0;
+  }
+  for (int k = 0; k < d; ++k) {
+    const T mn = (T)c.min_corner[k], mx = (T)c.max_corner[k];
+    const T mnp = (T)(mn - pad), mxp = (T)(mx + pad);
+    s->min_pad[k] = (double)mnp;
+    s->max_pad[k] = (double)mxp;
+    s->cell_size[k] = (double)r;
+    if (!s->is_template) {
+      const T q = (T)((T)(mxp - mnp) / r);
+      if (!(q >= (T)1) || !(q < (T)2147483647.0)) return PN_ERR_INVALID_ARG;
+      s->grid_size[k] = (int64_t)std::ceil((double)q);
+      total *= s->grid_size[k];
+      if (total > (int64_t)INT32_MAX - 1) return PN_ERR_INVALID_ARG;
+    }
+  }
+  s->n_total = s->is_template ? 0 : (int32_t)total;
+  s->periodic = 0;
+  if (c.periodic && !s->is_template) {
+    s->periodic = 1;
+    for (int k = 0; k < d; ++k) {
+      const T size = (T)((T)c.periodic_max[k] - (T)c.periodic_min[k]);
+      s->box_size[k] = (double)size;
+      const double nc = std::floor(((double)size + 10.0 * 2.220446049250313e-16) / (double)r);
+      if (!(nc >= 3.0)) return PN_ERR_INVALID_ARG;  // "needs at least 3 cells"
+      if (nc > 1e9) return PN_ERR_INVALID_ARG;
+      s->n_cells[k] = (int64_t)nc;
+      s->cell_size[k] = (double)(T)(size / (T)s->n_cells[k]);
+    }
+  }
+  return PN_OK;
+}
+
+static int create(const pn_config* cfg, pn_search** out) {
+  if (!cfg || !out) return PN_ERR_INVALID_ARG;
+  *out = nullptr;
+  if (cfg->ndims < 1 || cfg->ndims > 3) return PN_ERR_INVALID_ARG;
+  if (cfg->dtype != PN_FLOAT32 && cfg->dtype != PN_FLOAT64) return PN_ERR_INVALID_ARG;
+  if (cfg->update_strategy != PN_PARALLEL_UPDATE &&
+      cfg->update_strategy != PN_PARALLEL_INCREMENTAL_UPDATE)
+    return PN_ERR_INVALID_ARG;
+  if (!(cfg->search_radius >= 0.0) || cfg->max_points_per_cell < 0 || cfg->n_points < 0)
+    return PN_ERR_INVALID_ARG;
+  pn_search* s = new (std::nothrow) pn_search();
+  if (!s) return PN_ERR_OUT_OF_MEMORY;
+  s->cfg = *cfg;
+  s->ndims = cfg->ndims;
+  s->dtype = cfg->dtype;
+  int rc = cfg->dtype == PN_FLOAT64 ? geometry<double>(s) : geometry<float>(s);
+  if (rc != PN_OK) {
+    delete s;
+    return rc;
+  }
+  bool ok = cudaMalloc(&s->d_err, sizeof(int32_t) * 4) == cudaSuccess;
+  ok = ok && cudaMemset(s->d_err, 0, sizeof(int32_t) * 4) == cudaSuccess;
+  ok = ok && cudaMallocHost(&s->h_ovf_n, sizeof(int32_t)) == cudaSuccess;
+  ok = ok && cudaEventCreateWithFlags(&s->ev_ovf, cudaEventDisableTiming) == cudaSuccess;
+  if (ok && !s->is_template) {
+    const int64_t nt = s->n_total;
+    s->scan_tiles = div_up(nt, 2048);
+    ok = cudaMalloc(&s->d_counts, sizeof(int32_t) * nt) == cudaSuccess &&
+         cudaMalloc(&s->d_start, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
+         cudaMalloc(&s->d_ovf_counts, sizeof(int32_t) * nt) == cudaSuccess &&
+         cudaMalloc(&s->d_ovf_start, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
+         cudaMalloc(&s->d_ovf_n, sizeof(int32_t) * 4) == cudaSuccess &&
+         cudaMalloc(&s->d_scan_state, sizeof(unsigned long long) * (s->scan_tiles + 1)) == cudaSuccess;
+    if (ok && cfg->n_points > 0) ok = ensure_capacity(s, cfg->n_points) == PN_OK;
+  }
+  if (!ok) {
+    cudaGetLastError();
+    pn_destroy(s);
+    return PN_ERR_OUT_OF_MEMORY;
+  }
+  *out = s;
+  return PN_OK;
+}
+
+static int record(pn_search* s, int rc, cudaStream_t st) {
+  s->last_stream = st;
+  if (rc != PN_OK && s->host_error == 0) s->host_error = rc;
+  return rc;
+}
+
+}  // namespace pn
+
+using namespace pn;
+
+extern "C" {
+
+int pn_abi_version(void) { return PN_ABI_VERSION; }
+
+int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, out); }
+
+int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
+                   pn_search** out) {
+  if (!tmpl) return PN_ERR_INVALID_ARG;
+  pn_config c = tmpl->cfg;
+  c.search_radius = search_radius;
+  c.n_points = n_points;
+  return create(&c, out);
+}
+
+int pn_destroy(pn_search* s) {
+  if (!s) return PN_OK;
+  free_points(s);
+  void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start, s->d_scan_state,
+                  s->d_ovf_counts, s->d_ovf_start, s->d_ovf_n, s->d_qcount,
+                  s->d_part,       s->d_sort_tmp};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->h_ovf_n) cudaFreeHost(s->h_ovf_n);
+  if (s->ev_ovf) cudaEventDestroy(s->ev_ovf);
+  delete s;
+  return PN_OK;
+}
+
+int pn_initialize(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
+                  int64_t n_eachindex_y, pn_stream_t stream) {
+  if (!s || n_y < 0 || (n_y > 0 && !y) || (eachindex_y && n_eachindex_y < 0))
+    return PN_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->is_template) {
+    // initialize_grid! returns early for search_radius < eps() (nhs_grid.jl:263-267).
+    s->initialized = false;
+    return record(s, PN_OK, st);
+  }
+  int rc = s->dtype == PN_FLOAT64
+               ? build<double>(s, (const double*)y, n_y, eachindex_y, n_eachindex_y, st)
+               : build<float>(s, (const float*)y, n_y, eachindex_y, n_eachindex_y, st);
+  if (rc == PN_OK) {
+    s->initialized = true;
+    s->full_binned = eachindex_y == nullptr;
+    s->n_y = n_y;
+    s->y_ptr = y;
+  }
+  return record(s, rc, st);
+}
+
+int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
+              int64_t n_eachindex_y, int32_t points_moving_y, pn_stream_t stream) {
+  if (!s) return PN_ERR_INVALID_ARG;
+  // update! is a no-op when the neighbour points do not move (nhs_grid.jl:289).
+  if (!points_moving_y) return PN_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (s->cfg.update_strategy == PN_PARALLEL_UPDATE || s->is_template)
+    return pn_initialize(s, y, n_y, eachindex_y, n_eachindex_y, stream);
+  // ParallelIncrementalUpdate: no inactive points (nhs_grid.jl:414-417).
+  if (eachindex_y != nullptr) return record(s, PN_ERR_INVALID_ARG, st);
+  if (!s->initialized) return record(s, PN_ERR_NOT_INITIALIZED, st);
+  if (n_y != s->n_y || !s->full_binned) return record(s, PN_ERR_INVALID_ARG, st);
+  // Rebuild policy: once the previous update's movers (read back asynchronously) exceed
+  // rebuild_fraction of the points, a full build resets the main structure.
+  bool rebuild = false;
+  if (s->ovf_pending && cudaEventQuery(s->ev_ovf) == cudaSuccess) {
+    s->n_ovf = *s->h_ovf_n;
+    s->ovf_pending = false;
+  }
+  if (s->ovf_active && (double)s->n_ovf > s->rebuild_fraction * (double)s->n_binned) rebuild = true;
+  if (rebuild) {
+    s->n_ovf = 0;
+    return pn_initialize(s, y, n_y, nullptr, 0, stream);
+  }
+  int rc = s->dtype == PN_FLOAT64 ? update_incremental<double>(s, (const double*)y, n_y, st)
+                                  : update_incremental<float>(s, (const float*)y, n_y, st);
+  if (rc == PN_OK) s->y_ptr = y;
+  return record(s, rc, st);
+}
+
+int pn_foreach_point_neighbor(pn_search* s, int32_t functor, const void* x, int64_t n_x,
+                              const void* y, int64_t n_y, const int32_t* points,
+                              int64_t n_points, const void* params, pn_stream_t stream) {
+  if (!s) return PN_ERR_INVALID_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = s->dtype == PN_FLOAT64
+               ? pn::foreach<double>(s, functor, (const double*)x, n_x, (const double*)y, n_y,
+                                     points, n_points, params, st)
+               : pn::foreach<float>(s, functor, (const float*)x, n_x, (const float*)y, n_y,
+                                    points, n_points, params, st);
+  return record(s, rc, st);
+}
+
+int pn_get_error(pn_search* s, int32_t clear) {
+  if (!s) return PN_ERR_INVALID_ARG;
+  int32_t e = 0;
+  if (cudaMemcpy(&e, s->d_err, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return PN_ERR_CUDA;
+  int rc = s->host_error ? s->host_error : e;
+  if (clear) {
+    s->host_error = 0;
+    if (e) cudaMemset(s->d_err, 0, sizeof(int32_t));
+  }
+  return rc;
+}
+
+int pn_sync(pn_search* s) {
+  if (!s) return PN_ERR_INVALID_ARG;
+  cudaError_t ce = cudaStreamSynchronize(s->last_stream);
+  if (ce != cudaSuccess) return PN_ERR_CUDA;
+  return pn_get_error(s, 1);
+}
+
+const char* pn_status_string(int32_t status) {
+  switch (status) {
+    case PN_OK: return "ok";
+    case PN_ERR_OUT_OF_DOMAIN:
+      return "particle coordinates are NaN or outside the domain bounds of the cell list";
+    case PN_ERR_INVALID_ARG: return "invalid argument";
+    case PN_ERR_CUDA: return "CUDA error";
+    case PN_ERR_TIMEOUT: return "a device-side wait timed out";
+    case PN_ERR_UNSUPPORTED_FUNCTOR: return "unsupported pair function";
+    case PN_ERR_CELL_FULL: return "cell list is full. Use a larger `max_points_per_cell`.";
+    case PN_ERR_NOT_INITIALIZED: return "`search_radius` is not defined or the search is not initialized";
+    case PN_ERR_OUT_OF_MEMORY: return "out of device memory";
+    case PN_ERR_BOUNDS: return "BoundsError: a query point's neighbouring cells are outside the grid";
+    case PN_ERR_CAPACITY: return "neighbour-list buffer too small";
+    default: return "unknown status";
+  }
+}
+
+int pn_requires_update(const pn_search* s, int32_t out[2]) {
+  if (!s || !out) return PN_ERR_INVALID_ARG;
+  out[0] = 0;
+  out[1] = 1;
+  return PN_OK;
+}
+
+int pn_get_grid_info(const pn_search* s, pn_grid_info* out) {
+  if (!s || !out) return PN_ERR_INVALID_ARG;
+  std::memset(out, 0, sizeof(*out));
+  out->ndims = s->ndims;
+  out->dtype = s->dtype;
+  out->periodic = s->periodic;
+  out->is_template = s->is_template;
+  for (int k = 0; k < 3; ++k) {
+    out->grid_size[k] = k < s->ndims ? s->grid_size[k] : 0;
+    out->n_cells[k] = k < s->ndims ? s->n_cells[k] : 0;
+    out->min_corner[k] = s->min_pad[k];
+    out->max_corner[k] = s->max_pad[k];
+    out->cell_size[k] = s->cell_size[k];
+  }
+  out->search_radius = s->radius;
+  out->n_binned = s->n_binned;
+  out->n_overflow = s->n_ovf;
+  return PN_OK;
+}
+
+int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out) {
+  if (!cfg || !out || cfg->ndims < 1 || cfg->ndims > 3) return PN_ERR_INVALID_ARG;
+  if (cfg->dtype != PN_FLOAT32 && cfg->dtype != PN_FLOAT64) return PN_ERR_INVALID_ARG;
+  pn_search tmp;
+  tmp.cfg = *cfg;
+  tmp.ndims = cfg->ndims;
+  tmp.dtype = cfg->dtype;
+  int rc = cfg->dtype == PN_FLOAT64 ? geometry<double>(&tmp) : geometry<float>(&tmp);
+  if (rc != PN_OK) return rc;
+  return pn_get_grid_info(&tmp, out);
+}
+
+int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stream_t stream) {
+  if (!s || n < 0 || (n > 0 && (!x || !out))) return PN_ERR_INVALID_ARG;
+  if (s->is_template) return PN_ERR_NOT_INITIALIZED;
+  cudaStream_t st = (cudaStream_t)stream;
+  int rc = s->dtype == PN_FLOAT64 ? cell_coords<double>(s, (const double*)x, n, out, st)
+                                  : cell_coords<float>(s, (const float*)x, n, out, st);
+  return record(s, rc, st);
+}
+
+int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream) {
+  if (!s || !counts) return PN_ERR_INVALID_ARG;
+  if (!s->initialized) return PN_ERR_NOT_INITIALIZED;
+  cudaStream_t st = (cudaStream_t)stream;
+  return record(s, export_cells(s, counts, points, st), st);
+}
+
+}  // extern "C"

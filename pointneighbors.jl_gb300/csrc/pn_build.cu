@@ -1,0 +1,687 @@
+// pn_build.cu -- cell-list build (initialize! / update! with ParallelUpdate), cell
+// coordinates, cell export and the small scans/sorts used by the neighbour lists.
+//
+// The reference (nhs_grid.jl:255-281, vector_of_vectors.jl:93-112) pushes every point into
+// a fixed-capacity column with one atomic per point.  Here the cell list is a counting
+// sort into a CSR layout:
+//   1. k_bin      per point: cell index (exact reference semantics, bounds check), then a
+//                 warp-aggregated atomic increment of the cell histogram (lanes that share
+//                 a cell issue one atomic) that also hands each point its rank.
+//   2. k_scan     exclusive scan of the histogram -> cell starts, single pass with
+//                 decoupled look-back (bounded waits), plus the max_points_per_cell check.
+//   3. k_scatter  point -> slot start[cell] + rank.
+//   4. k_finalize rank-sort each cell's points by point index (a deterministic order,
+//                 independent of atomic timing) and write the cell-sorted coordinates.
+#include <algorithm>
+
+#include "pn_internal.cuh"
+
+namespace pn {
+
+constexpr int BIN_THREADS = 256;
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 8;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+constexpr unsigned long long FLAG_AGG = 1ull << 32;
+constexpr unsigned long long FLAG_INCL = 2ull << 32;
+constexpr long long SCAN_SPIN_LIMIT = 1ll << 22;
+
+// ---------------------------------------------------------------- 1. histogram
+template <typename T, int D, bool PER>
+__global__ void __launch_bounds__(BIN_THREADS)
+k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* __restrict__ idx,
+      int32_t m, int32_t* __restrict__ cell_of, int32_t* __restrict__ slot_of,
+      int32_t* __restrict__ counts, int32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = base + threadIdx.x;
+    int32_t cell = -1;
+    if (t < m) {
+      const int64_t i = idx ? (int64_t)idx[t] : t;
+      if (i < 0 || i >= n_y) {
+        set_error(err, PN_ERR_INVALID_ARG);
+      } else {
+        bool ok = true;
+        int32_t lin = 0, stride = 1;
+#pragma unroll
+        for (int k = 0; k < D; ++k) {
+          int32_t c;
+          ok &= cell_coord_1d(g, PER, k, y[i * D + k], c);
+          lin += (c - 1) * stride;
+          stride *= g.n[k];
+        }
+        if (ok) cell = lin;
+        else set_error(err, PN_ERR_OUT_OF_DOMAIN);
+      }
+    }
+    // `base` is uniform over the block, so every lane of the warp reaches this point.
+    const unsigned valid = __ballot_sync(0xffffffffu, cell >= 0);
+    if (cell >= 0) {
+      const unsigned peers = __match_any_sync(valid, cell);
+      const int leader = __ffs(peers) - 1;
+      int32_t b = 0;
+      if (lane == leader) b = atomicAdd(&counts[cell], __popc(peers));
+      b = __shfl_sync(peers, b, leader);
+      slot_of[t] = b + __popc(peers & lanemask_lt());
+    }
+    if (t < m) cell_of[t] = cell;
+  }
+}
+
+// ---------------------------------------------------------------- 2. scan
+// Exclusive scan of counts[0..n) into start[0..n], start[n] = total.  Tiles are taken in
+// launch order from a counter, so a tile only ever waits for tiles that are already
+// running; every wait is bounded and reports PN_ERR_TIMEOUT if it gives up.
+__global__ void __launch_bounds__(SCAN_THREADS)
+k_scan_cells(const int32_t* __restrict__ counts, int32_t n, int32_t* __restrict__ start,
+             unsigned long long* __restrict__ state, int32_t n_tiles, int32_t max_ppc,
+             const int32_t* __restrict__ base_ptr, int32_t* __restrict__ err) {
+  __shared__ int s_tile, s_prefix;
+  __shared__ int s_warp[SCAN_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (threadIdx.x == 0) s_tile = (int)atomicAdd(&state[n_tiles], 1ull);
+  __syncthreads();
+  const int tile = s_tile;
+  const int64_t base = (int64_t)tile * SCAN_TILE + (int64_t)threadIdx.x * SCAN_ITEMS;
+  int v[SCAN_ITEMS];
+  if (base + SCAN_ITEMS <= n) {
+    const int4 a = *reinterpret_cast<const int4*>(counts + base);
+    const int4 b = *reinterpret_cast<const int4*>(counts + base + 4);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  } else {
+#pragma unroll
+    for (int i = 0; i < SCAN_ITEMS; ++i) v[i] = (base + i < n) ? counts[base + i] : 0;
+  }
+  int sum = 0, mx = 0;
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    sum += v[i];
+    mx = max(mx, v[i]);
+  }
+  if (max_ppc > 0 && mx > max_ppc) set_error(err, PN_ERR_CELL_FULL);
+  int incl = sum;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < SCAN_THREADS / 32 ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < SCAN_THREADS / 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < SCAN_THREADS / 32) s_warp[lane] = w;
+  }
+  __syncthreads();
+  const int aggregate = s_warp[SCAN_THREADS / 32 - 1];
+  const int thread_excl = (warp > 0 ? s_warp[warp - 1] : 0) + incl - sum;
+  if (threadIdx.x == 0) {
+    int prefix = 0;
+    if (tile == 0) {
+      atomicExch(&state[0], FLAG_INCL | (unsigned)aggregate);
+    } else {
+      atomicExch(&state[tile], FLAG_AGG | (unsigned)aggregate);
+      int j = tile - 1;
+      long long spins = 0;
+      while (j >= 0) {
+        const unsigned long long st = *(volatile unsigned long long*)&state[j];
+        const unsigned long long flag = st & (3ull << 32);
+        if (flag == 0) {
+          if (++spins > SCAN_SPIN_LIMIT) {
+            set_error(err, PN_ERR_TIMEOUT);
+            break;
+          }
+          __nanosleep(32);
+          continue;
+        }
+        prefix += (int)(unsigned)(st & 0xffffffffull);
+        if (flag == FLAG_INCL) break;
+        --j;
+      }
+      atomicExch(&state[tile], FLAG_INCL | (unsigned)(prefix + aggregate));
+    }
+    s_prefix = prefix;
+  }
+  __syncthreads();
+  int run = s_prefix + thread_excl + (base_ptr ? *base_ptr : 0);
+#pragma unroll
+  for (int i = 0; i < SCAN_ITEMS; ++i) {
+    if (base + i < n) {
+      start[base + i] = run;
+      run += v[i];
+      if (base + i == n - 1) start[n] = run;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- 3. scatter
+__global__ void __launch_bounds__(256)
+k_scatter(const int32_t* __restrict__ cell_of, const int32_t* __restrict__ slot_of,
+          const int32_t* __restrict__ idx, int32_t m, const int32_t* __restrict__ start,
+          int32_t* __restrict__ tmp_perm, int32_t* __restrict__ cell_of_slot) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const int32_t c = cell_of[t];
+  if (c < 0) return;
+  const int32_t p = start[c] + slot_of[t];
+  tmp_perm[p] = idx ? idx[t] : (int32_t)t;
+  cell_of_slot[p] = c;
+}
+
+// ---------------------------------------------------------------- 4. in-cell sort
+template <typename T, int D>
+__device__ __forceinline__ void store_pos(T* pos, int64_t k, const T* v) {
+  constexpr int S = PS<D>::value;
+#pragma unroll
+  for (int c = 0; c < S; ++c) pos[k * S + c] = c < D ? v[c] : (T)0;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void finalize_slot(const int32_t* __restrict__ tmp_perm,
+                                              const int32_t* __restrict__ cell_of_slot,
+                                              const int32_t* __restrict__ start, int64_t k,
+                                              const T* __restrict__ y, int32_t* __restrict__ perm,
+                                              T* __restrict__ pos) {
+  const int32_t c = cell_of_slot[k];
+  const int32_t s = start[c], e = start[c + 1];
+  const int32_t v = tmp_perm[k];
+  int32_t rank = 0;
+  for (int32_t q = s; q < e; ++q) rank += (__ldg(&tmp_perm[q]) < v);
+  const int32_t dst = s + rank;
+  perm[dst] = v;
+  T p[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) p[d] = y[(int64_t)v * D + d];
+  store_pos<T, D>(pos, dst, p);
+}
+
+template <typename T, int D>
+__global__ void __launch_bounds__(256)
+k_finalize(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
+           const int32_t* __restrict__ start, int32_t n_total, const T* __restrict__ y,
+           int32_t* __restrict__ perm, T* __restrict__ pos) {
+  // Only start[n_total] slots were filled: points that failed the bounds check were not
+  // binned, so the slot count is read on the device.
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= start[n_total]) return;
+  finalize_slot<T, D>(tmp_perm, cell_of_slot, start, k, y, perm, pos);
+}
+
+// ---------------------------------------------------------------- incremental update
+// ParallelIncrementalUpdate (nhs_grid.jl:408-467) moves only the points whose cell
+// changed.  Here the main structure of the last full build stays in place; every update
+// re-checks all points against their main cell and
+//   - refreshes the coordinates of points still in their main cell (in place),
+//   - vacates the main slot of every other point (perm = -1, NaN coordinates, which no
+//     distance test accepts) and re-bins it into the overflow lists: a second CSR over the
+//     same cells, stored in the slots after the main ones.
+// The traversal visits both lists for every stencil row.  Because the overflow is rebuilt
+// relative to the main structure on every update, it never accumulates; a full rebuild
+// (which empties it) is taken when the movers exceed a threshold.
+template <typename T, int D, bool PER>
+__global__ void __launch_bounds__(256)
+k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
+              const int32_t* __restrict__ cell_of_slot, const int32_t* __restrict__ n_main,
+              const T* __restrict__ y, int32_t* __restrict__ perm, T* __restrict__ pos,
+              int32_t* __restrict__ ovf_counts, int32_t* __restrict__ ovf_n,
+              int32_t* __restrict__ ovf_list, int32_t* __restrict__ ovf_cell,
+              int32_t* __restrict__ ovf_slot, int32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  const int32_t nm = *n_main;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nm;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = base + threadIdx.x;
+    int32_t cell = -1;
+    bool moved = false;
+    int32_t i = -1;
+    if (k < nm) {
+      i = main_perm[k];
+      T p[D];
+      bool ok = true;
+      int32_t lin = 0, stride = 1;
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        p[d] = y[(int64_t)i * D + d];
+        int32_t c;
+        ok &= cell_coord_1d(g, PER, d, p[d], c);
+        lin += (c - 1) * stride;
+        stride *= g.n[d];
+      }
+      if (!ok) {
+        set_error(err, PN_ERR_OUT_OF_DOMAIN);
+      } else if (lin == cell_of_slot[k]) {
+        perm[k] = i;
+        store_pos<T, D>(pos, k, p);
+      } else {
+        moved = true;
+        cell = lin;
+      }
+      if (!ok || moved) {
+        perm[k] = -1;
+        T nan_p[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d) nan_p[d] = (T)NAN;
+        store_pos<T, D>(pos, k, nan_p);
+      }
+    }
+    // Movers: one list entry each (warp-aggregated), plus their rank in the new cell.
+    const unsigned mv = __ballot_sync(0xffffffffu, moved);
+    if (mv) {
+      int32_t b = 0;
+      if (lane == __ffs(mv) - 1) b = atomicAdd(ovf_n, __popc(mv));
+      b = __shfl_sync(0xffffffffu, b, __ffs(mv) - 1);
+      if (moved) {
+        const int32_t m = b + __popc(mv & lanemask_lt());
+        const unsigned peers = __match_any_sync(mv, cell);
+        const int leader = __ffs(peers) - 1;
+        int32_t cb = 0;
+        if (lane == leader) cb = atomicAdd(&ovf_counts[cell], __popc(peers));
+        cb = __shfl_sync(peers, cb, leader);
+        ovf_list[m] = i;
+        ovf_cell[m] = cell;
+        ovf_slot[m] = cb + __popc(peers & lanemask_lt());
+      }
+    }
+  }
+}
+
+// Movers -> their overflow slots (ovf_start is absolute: it starts after the main slots).
+__global__ void __launch_bounds__(256)
+k_scatter_movers(const int32_t* __restrict__ ovf_n, const int32_t* __restrict__ ovf_list,
+                 const int32_t* __restrict__ ovf_cell, const int32_t* __restrict__ ovf_slot,
+                 const int32_t* __restrict__ ovf_start, int32_t* __restrict__ tmp_perm,
+                 int32_t* __restrict__ cell_of_slot) {
+  const int32_t n = *ovf_n;
+  for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < n;
+       m += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t c = ovf_cell[m];
+    const int32_t p = ovf_start[c] + ovf_slot[m];
+    tmp_perm[p] = ovf_list[m];
+    cell_of_slot[p] = c;
+  }
+}
+
+// In-cell sort + coordinates of the overflow slots [start_main[n_total], ovf_start[n_total]).
+template <typename T, int D>
+__global__ void __launch_bounds__(256)
+k_finalize_movers(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
+                  const int32_t* __restrict__ ovf_start, const int32_t* __restrict__ n_main,
+                  int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
+                  T* __restrict__ pos) {
+  const int32_t k0 = *n_main, k1 = ovf_start[n_total];
+  for (int64_t k = k0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < k1;
+       k += (int64_t)gridDim.x * blockDim.x)
+    finalize_slot<T, D>(tmp_perm, cell_of_slot, ovf_start, k, y, perm, pos);
+}
+
+// ---------------------------------------------------------------- host side
+template <typename T, int D, bool PER>
+static void launch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int32_t m,
+                       cudaStream_t st) {
+  const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
+  k_bin<T, D, PER><<<blocks, BIN_THREADS, 0, st>>>(make_grid<T>(s), y, n_y, idx, m,
+                                                   s->d_cell_of, s->d_slot_of, s->d_counts,
+                                                   s->d_err);
+}
+
+template <typename T>
+static void dispatch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* idx,
+                         int32_t m, cudaStream_t st) {
+  const bool per = s->periodic != 0;
+  switch (s->ndims * 2 + (per ? 1 : 0)) {
+    case 2: launch_bin<T, 1, false>(s, y, n_y, idx, m, st); break;
+    case 3: launch_bin<T, 1, true>(s, y, n_y, idx, m, st); break;
+    case 4: launch_bin<T, 2, false>(s, y, n_y, idx, m, st); break;
+    case 5: launch_bin<T, 2, true>(s, y, n_y, idx, m, st); break;
+    case 6: launch_bin<T, 3, false>(s, y, n_y, idx, m, st); break;
+    default: launch_bin<T, 3, true>(s, y, n_y, idx, m, st); break;
+  }
+}
+
+template <typename T>
+static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st) {
+  const int blocks = div_up(m, 256);
+  if (blocks == 0) return;
+  T* pos = static_cast<T*>(s->d_pos);
+  const int32_t nt = s->n_total;
+  switch (s->ndims) {
+    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); break;
+    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); break;
+    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); break;
+  }
+}
+
+// Exclusive scan of the cell histogram into s->d_start (one launch).
+// start[c] = *base_ptr + sum(counts[0..c)) when base_ptr is given.
+static void scan_cells(pn_search* s, const int32_t* counts, int32_t* start, cudaStream_t st,
+                       const int32_t* base_ptr = nullptr, int32_t max_ppc = 0) {
+  cudaMemsetAsync(s->d_scan_state, 0, sizeof(unsigned long long) * (s->scan_tiles + 1), st);
+  k_scan_cells<<<s->scan_tiles, SCAN_THREADS, 0, st>>>(counts, s->n_total, start,
+                                                       s->d_scan_state, s->scan_tiles,
+                                                       max_ppc, base_ptr, s->d_err);
+}
+
+template <typename T>
+int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_idx,
+          cudaStream_t st) {
+  const int64_t m = idx ? n_idx : n_y;
+  int rc = ensure_capacity(s, std::max(m, n_y));
+  if (rc != PN_OK) return rc;
+  cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * s->n_total, st);
+  if (m > 0) dispatch_bin<T>(s, y, n_y, idx, (int32_t)m, st);
+  scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
+  if (m > 0) {
+    k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
+                                              s->d_start, s->d_tmp_perm, s->d_cell_of_slot);
+    // Points rejected by the bounds check are not binned; every kernel that walks the
+    // slots bounds itself by start[n_total], read on the device.
+    launch_finalize<T>(s, y, (int32_t)m, st);
+  }
+  s->n_binned = m;
+  s->ovf_active = false;
+  s->main_perm_valid = false;
+  s->n_ovf = 0;
+  s->updates_since_build = 0;
+  return cuda_status(cudaGetLastError());
+}
+
+template <typename T, int D, bool PER>
+static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {
+  const int blocks = std::max(1, std::min(div_up(s->n_binned, 256), 152 * 8));
+  k_mark_movers<T, D, PER><<<blocks, 256, 0, st>>>(
+      make_grid<T>(s), s->d_main_perm, s->d_cell_of_slot, s->d_start + s->n_total, y,
+      s->d_perm, static_cast<T*>(s->d_pos), s->d_ovf_counts, s->d_ovf_n, s->d_ovf_list,
+      s->d_ovf_cell, s->d_ovf_slot, s->d_err);
+}
+
+template <typename T, int D>
+static void launch_movers(pn_search* s, const T* y, cudaStream_t st) {
+  k_scatter_movers<<<152 * 4, 256, 0, st>>>(s->d_ovf_n, s->d_ovf_list, s->d_ovf_cell,
+                                             s->d_ovf_slot, s->d_ovf_start, s->d_tmp_perm,
+                                             s->d_cell_of_slot);
+  k_finalize_movers<T, D><<<152 * 4, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot,
+                                                   s->d_ovf_start, s->d_start + s->n_total,
+                                                   s->n_total, y, s->d_perm,
+                                                   static_cast<T*>(s->d_pos));
+}
+
+template <typename T>
+int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
+  (void)n_y;
+  if (!s->main_perm_valid) {
+    cudaMemcpyAsync(s->d_main_perm, s->d_perm, sizeof(int32_t) * s->n_binned,
+                    cudaMemcpyDeviceToDevice, st);
+    s->main_perm_valid = true;
+  }
+  cudaMemsetAsync(s->d_ovf_counts, 0, sizeof(int32_t) * s->n_total, st);
+  cudaMemsetAsync(s->d_ovf_n, 0, sizeof(int32_t), st);
+  const bool per = s->periodic != 0;
+  switch (s->ndims * 2 + (per ? 1 : 0)) {
+    case 2: launch_mark<T, 1, false>(s, y, st); break;
+    case 3: launch_mark<T, 1, true>(s, y, st); break;
+    case 4: launch_mark<T, 2, false>(s, y, st); break;
+    case 5: launch_mark<T, 2, true>(s, y, st); break;
+    case 6: launch_mark<T, 3, false>(s, y, st); break;
+    default: launch_mark<T, 3, true>(s, y, st); break;
+  }
+  scan_cells(s, s->d_ovf_counts, s->d_ovf_start, st, s->d_start + s->n_total);
+  switch (s->ndims) {
+    case 1: launch_movers<T, 1>(s, y, st); break;
+    case 2: launch_movers<T, 2>(s, y, st); break;
+    default: launch_movers<T, 3>(s, y, st); break;
+  }
+  s->ovf_active = true;
+  // The mover count feeds the rebuild policy of the next update; it is read back lazily.
+  cudaMemcpyAsync(s->h_ovf_n, s->d_ovf_n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
+  cudaEventRecord(s->ev_ovf, st);
+  s->ovf_pending = true;
+  ++s->updates_since_build;
+  return cuda_status(cudaGetLastError());
+}
+
+template int update_incremental<float>(pn_search*, const float*, int64_t, cudaStream_t);
+template int update_incremental<double>(pn_search*, const double*, int64_t, cudaStream_t);
+
+template int build<float>(pn_search*, const float*, int64_t, const int32_t*, int64_t, cudaStream_t);
+template int build<double>(pn_search*, const double*, int64_t, const int32_t*, int64_t, cudaStream_t);
+
+// ---------------------------------------------------------------- cell_coords
+template <typename T, int D>
+__global__ void k_cell_coords(const GridDev<T> g, bool per, const T* __restrict__ x, int64_t n,
+                              int64_t* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  T xi[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) xi[k] = x[i * D + k];
+  int64_t c[D];
+  cell_coords_exact<T, D>(g, per, xi, c);
+#pragma unroll
+  for (int k = 0; k < D; ++k) out[i * D + k] = c[k];
+}
+
+template <typename T>
+int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t st) {
+  if (n <= 0) return PN_OK;
+  const GridDev<T> g = make_grid<T>(s);
+  const bool per = s->periodic != 0;
+  const int b = div_up(n, 256);
+  switch (s->ndims) {
+    case 1: k_cell_coords<T, 1><<<b, 256, 0, st>>>(g, per, x, n, out); break;
+    case 2: k_cell_coords<T, 2><<<b, 256, 0, st>>>(g, per, x, n, out); break;
+    default: k_cell_coords<T, 3><<<b, 256, 0, st>>>(g, per, x, n, out); break;
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+template int cell_coords<float>(pn_search*, const float*, int64_t, int64_t*, cudaStream_t);
+template int cell_coords<double>(pn_search*, const double*, int64_t, int64_t*, cudaStream_t);
+
+// ---------------------------------------------------------------- 64-bit scan
+// Three-phase exclusive scan (tile sums, scan of the tile sums, apply) of int32 values
+// into int64 offsets; out[n] = total.  Used for neighbour-list offsets.
+constexpr int S64_THREADS = 256, S64_ITEMS = 8, S64_TILE = S64_THREADS * S64_ITEMS;
+
+__device__ __forceinline__ long long block_excl_scan64(long long v, long long* s_warp,
+                                                       long long& total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  long long incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const long long t = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += t;
+  }
+  if (lane == 31) s_warp[warp] = incl;
+  __syncthreads();
+  if (warp == 0) {
+    long long w = lane < S64_THREADS / 32 ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < S64_THREADS / 32; o <<= 1) {
+      const long long t = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += t;
+    }
+    if (lane < S64_THREADS / 32) s_warp[lane] = w;
+  }
+  __syncthreads();
+  total = s_warp[S64_THREADS / 32 - 1];
+  const long long r = (warp > 0 ? s_warp[warp - 1] : 0) + incl - v;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(S64_THREADS)
+k_s64_reduce(const int32_t* __restrict__ in, int64_t n, int64_t* __restrict__ part) {
+  __shared__ long long s_warp[S64_THREADS / 32];
+  const int64_t base = (int64_t)blockIdx.x * S64_TILE + (int64_t)threadIdx.x * S64_ITEMS;
+  long long sum = 0;
+  for (int i = 0; i < S64_ITEMS; ++i)
+    if (base + i < n) sum += in[base + i];
+  long long total;
+  block_excl_scan64(sum, s_warp, total);
+  if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(S64_THREADS)
+k_s64_parts(int64_t* __restrict__ part, int64_t n_parts) {
+  __shared__ long long s_warp[S64_THREADS / 32];
+  long long carry = 0;
+  for (int64_t b0 = 0; b0 < n_parts; b0 += S64_THREADS) {
+    const int64_t i = b0 + threadIdx.x;
+    const long long v = i < n_parts ? part[i] : 0;
+    long long total;
+    const long long ex = block_excl_scan64(v, s_warp, total);
+    if (i < n_parts) part[i] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(S64_THREADS)
+k_s64_apply(const int32_t* __restrict__ in, int64_t n, const int64_t* __restrict__ part,
+            int64_t* __restrict__ out) {
+  __shared__ long long s_warp[S64_THREADS / 32];
+  const int64_t base = (int64_t)blockIdx.x * S64_TILE + (int64_t)threadIdx.x * S64_ITEMS;
+  int v[S64_ITEMS];
+  long long sum = 0;
+  for (int i = 0; i < S64_ITEMS; ++i) {
+    v[i] = base + i < n ? in[base + i] : 0;
+    sum += v[i];
+  }
+  long long total;
+  long long run = part[blockIdx.x] + block_excl_scan64(sum, s_warp, total);
+  for (int i = 0; i < S64_ITEMS; ++i) {
+    if (base + i < n) {
+      out[base + i] = run;
+      run += v[i];
+      if (base + i == n - 1) out[n] = run;
+    }
+  }
+}
+
+int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st) {
+  if (n == 0) {
+    cudaMemsetAsync(out, 0, sizeof(int64_t), st);
+    return cuda_status(cudaGetLastError());
+  }
+  const int64_t parts = div_up(n, S64_TILE);
+  if (parts > s->part_cap) {
+    if (s->d_part) cudaFree(s->d_part);
+    s->d_part = nullptr;
+    if (cudaMalloc(&s->d_part, sizeof(int64_t) * parts) != cudaSuccess) return PN_ERR_OUT_OF_MEMORY;
+    s->part_cap = parts;
+  }
+  k_s64_reduce<<<(unsigned)parts, S64_THREADS, 0, st>>>(in, n, s->d_part);
+  k_s64_parts<<<1, S64_THREADS, 0, st>>>(s->d_part, parts);
+  k_s64_apply<<<(unsigned)parts, S64_THREADS, 0, st>>>(in, n, s->d_part, out);
+  return cuda_status(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- row sort
+// One warp per row: rank every entry (entries of a row are distinct point indices) into
+// the scratch, then copy the sorted row back.
+__global__ void __launch_bounds__(256)
+k_sort_rows(const int64_t* __restrict__ offsets, int64_t n_rows, int32_t* __restrict__ vals,
+            int32_t* __restrict__ tmp) {
+  const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n_rows) return;
+  const int64_t s = offsets[row], e = offsets[row + 1];
+  for (int64_t a = s + lane; a < e; a += 32) {
+    const int32_t v = vals[a];
+    int64_t rank = 0;
+    for (int64_t b = s; b < e; ++b) rank += (vals[b] < v);
+    tmp[s + rank] = v;
+  }
+  __syncwarp();
+  for (int64_t a = s + lane; a < e; a += 32) vals[a] = tmp[a];
+}
+
+int sort_rows(pn_search* s, const int64_t* offsets, int64_t n_rows, int32_t* vals,
+              int64_t total, cudaStream_t st) {
+  if (n_rows == 0 || total == 0) return PN_OK;
+  if (total > s->sort_tmp_cap) {
+    if (s->d_sort_tmp) cudaFree(s->d_sort_tmp);
+    s->d_sort_tmp = nullptr;
+    if (cudaMalloc(&s->d_sort_tmp, sizeof(int32_t) * total) != cudaSuccess) return PN_ERR_OUT_OF_MEMORY;
+    s->sort_tmp_cap = total;
+  }
+  k_sort_rows<<<div_up(n_rows * 32, 256), 256, 0, st>>>(offsets, n_rows, vals, s->d_sort_tmp);
+  return cuda_status(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------- export
+// counts[c] = points in cell c; points = every cell's points, ascending, cell by cell.
+// With overflow lists active, a cell holds its main points that are still there (slots not
+// vacated) followed by its overflow points, merged and sorted.
+template <typename T, int D>
+__global__ void k_export_counts(const int32_t* __restrict__ start, const int32_t* __restrict__ ovf_start,
+                                const int32_t* __restrict__ perm, int32_t n_total,
+                                int32_t* __restrict__ counts) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_total) return;
+  int32_t n = 0;
+  for (int32_t k = start[c]; k < start[c + 1]; ++k) n += perm[k] >= 0;
+  if (ovf_start) n += ovf_start[c + 1] - ovf_start[c];
+  counts[c] = n;
+}
+
+template <typename T, int D>
+__global__ void k_export_points(const int32_t* __restrict__ start, const int32_t* __restrict__ perm,
+                                const int32_t* __restrict__ ovf_start,
+                                const int32_t* __restrict__ ovf_perm, const int64_t* __restrict__ out_start,
+                                int32_t n_total, int32_t* __restrict__ points) {
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_total) return;
+  int64_t o = out_start[c];
+  const int64_t o0 = o;
+  for (int32_t k = start[c]; k < start[c + 1]; ++k)
+    if (perm[k] >= 0) points[o++] = perm[k];
+  if (ovf_start) {
+    for (int32_t k = ovf_start[c]; k < ovf_start[c + 1]; ++k) points[o++] = ovf_perm[k];
+    // insertion sort of the merged cell (short lists)
+    for (int64_t a = o0 + 1; a < o; ++a) {
+      const int32_t v = points[a];
+      int64_t b = a - 1;
+      while (b >= o0 && points[b] > v) {
+        points[b + 1] = points[b];
+        --b;
+      }
+      points[b + 1] = v;
+    }
+  }
+}
+
+template <typename T, int D>
+static int export_cells_t(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st) {
+  const int b = div_up(s->n_total, 256);
+  const int32_t* ovf = s->ovf_active ? s->d_ovf_start : nullptr;
+  k_export_counts<T, D><<<b, 256, 0, st>>>(s->d_start, ovf, s->d_perm, s->n_total, counts);
+  int64_t* out_start = nullptr;
+  if (cudaMallocAsync(&out_start, sizeof(int64_t) * (s->n_total + 1), st) != cudaSuccess)
+    return PN_ERR_OUT_OF_MEMORY;
+  int rc = scan64(s, counts, s->n_total, out_start, st);
+  if (rc == PN_OK && points)
+    k_export_points<T, D><<<b, 256, 0, st>>>(s->d_start, s->d_perm, ovf, s->d_perm,
+                                              out_start, s->n_total, points);
+  cudaFreeAsync(out_start, st);
+  return rc != PN_OK ? rc : cuda_status(cudaGetLastError());
+}
+
+int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st) {
+  const int key = s->ndims + (s->dtype == PN_FLOAT64 ? 3 : 0);
+  switch (key) {
+    case 1: return export_cells_t<float, 1>(s, counts, points, st);
+    case 2: return export_cells_t<float, 2>(s, counts, points, st);
+    case 3: return export_cells_t<float, 3>(s, counts, points, st);
+    case 4: return export_cells_t<double, 1>(s, counts, points, st);
+    case 5: return export_cells_t<double, 2>(s, counts, points, st);
+    default: return export_cells_t<double, 3>(s, counts, points, st);
+  }
+}
+
+}  // namespace pn

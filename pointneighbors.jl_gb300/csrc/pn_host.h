@@ -1,0 +1,106 @@
+// pn_host.h -- the search handle and the host-side launchers shared by the translation
+// units of libpn_gb300 (build/update kernels, traversal kernels, C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pn_gb300.h"
+
+// One GridNeighborhoodSearch over a FullGridCellList.
+//
+// Device layout of the cell list (a CSR counting-sort structure instead of the
+// reference's fixed-capacity DynamicVectorOfVectors columns):
+//   start[c] .. start[c+1]   slots of cell c (c = 0-based column-major linear index)
+//   perm[slot]               point index of the slot (ascending inside a cell)
+//   cell_of_slot[slot]       linear cell index of the slot
+//   pos[slot * PS]           the point's coordinates, cell-sorted (3D padded to 4 values)
+// Incremental update! keeps this "main" structure from the last full build and holds the
+// points that have left their main cell in a second CSR over the same cells (the overflow
+// lists): ovf_start[c] .. ovf_start[c+1] are slots after the main ones, in the same
+// perm / cell_of_slot / pos arrays (which therefore hold up to 2 * cap slots).  A main slot
+// whose point left is vacated: perm = -1 and NaN coordinates, which no distance test
+// accepts.
+struct pn_search {
+  pn_config cfg;
+  // geometry (values exact in T, stored as double)
+  int32_t ndims, dtype, periodic, is_template;
+  int64_t grid_size[3], n_cells[3];
+  double min_pad[3], max_pad[3], cell_size[3], box_size[3];
+  double radius;
+  int32_t n_total;      // number of cells, prod(grid_size)
+  int32_t scan_tiles;   // tiles of the cell-start scan
+
+  // device scratch owned by the handle
+  int32_t* d_err = nullptr;        // sticky error word
+  int32_t* d_counts = nullptr;     // [n_total] histogram
+  int32_t* d_start = nullptr;      // [n_total + 1]
+  unsigned long long* d_scan_state = nullptr;  // [scan_tiles + 1] look-back state + counter
+  int64_t cap = 0;                 // point capacity; slot arrays hold 2 * cap slots
+  int32_t* d_cell_of = nullptr;    // [cap] cell of the t-th binned input point
+  int32_t* d_slot_of = nullptr;    // [cap] its rank inside the cell (atomic order)
+  int32_t* d_tmp_perm = nullptr;   // [2 cap] scatter target before the in-cell sort
+  int32_t* d_perm = nullptr;       // [2 cap]
+  int32_t* d_cell_of_slot = nullptr;  // [2 cap]
+  void* d_pos = nullptr;           // [2 cap * 4] T
+  void* d_pa = nullptr;            // [2 cap * 4] T  WCSPH neighbour state (x, y, z, p/rho^2)
+  void* d_pb = nullptr;            // [2 cap * 4] T  WCSPH neighbour state (vx, vy, vz, rho)
+  int32_t* d_qcount = nullptr;     // [qcount_cap] per-query counts (neighbour lists)
+  int64_t qcount_cap = 0;
+  int64_t* d_part = nullptr;       // partial sums of the 64-bit scan
+  int64_t part_cap = 0;
+  int32_t* d_sort_tmp = nullptr;   // row-sort scratch of the neighbour lists
+  int64_t sort_tmp_cap = 0;
+
+  // incremental update (overflow lists relative to the main structure)
+  int32_t* d_main_perm = nullptr;      // [cap] perm of the last full build
+  int32_t* d_ovf_counts = nullptr;     // [n_total]
+  int32_t* d_ovf_start = nullptr;      // [n_total + 1] absolute slots
+  int32_t* d_ovf_n = nullptr;          // [1] number of movers
+  int32_t* d_ovf_list = nullptr;       // [cap] point index of each mover
+  int32_t* d_ovf_cell = nullptr;       // [cap] its new cell
+  int32_t* d_ovf_slot = nullptr;       // [cap] rank in the new cell (atomic order)
+  int32_t* h_ovf_n = nullptr;          // pinned copy of the mover count
+  cudaEvent_t ev_ovf = nullptr;        // recorded after the copy
+  bool ovf_pending = false;
+  int64_t n_ovf = 0;                   // movers after the last update (host view)
+  bool ovf_active = false;             // overflow lists in use
+  bool main_perm_valid = false;
+  double rebuild_fraction = 0.25;      // full rebuild when movers exceed this fraction
+  int32_t updates_since_build = 0;
+
+  // state
+  bool initialized = false;
+  bool full_binned = false;   // every point of y is binned (no eachindex_y subset)
+  int64_t n_binned = 0;
+  int64_t n_y = 0;            // size of y at the last build
+  const void* y_ptr = nullptr;
+  cudaStream_t last_stream = nullptr;
+  int32_t host_error = 0;     // errors detected on the host before launching
+};
+
+namespace pn {
+
+int ensure_capacity(pn_search* s, int64_t n);
+int ensure_qcount(pn_search* s, int64_t n);
+int cuda_status(cudaError_t e);
+
+// pn_build.cu
+template <typename T>
+int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_idx,
+          cudaStream_t st);
+template <typename T>
+int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st);
+template <typename T>
+int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t st);
+int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
+int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st);
+int sort_rows(pn_search* s, const int64_t* offsets, int64_t n_rows, int32_t* vals,
+              int64_t total, cudaStream_t st);
+
+// pn_traverse_f32.cu / pn_traverse_f64.cu
+template <typename T>
+int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
+            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st);
+
+}  // namespace pn

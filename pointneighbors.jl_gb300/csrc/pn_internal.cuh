@@ -1,0 +1,160 @@
+// pn_internal.cuh -- device-side building blocks shared by the build, update and
+// traversal kernels of libpn_gb300.
+//
+// Floating-point rules follow the reference (Julia, no fast-math): the arithmetic that
+// decides cell membership and neighbour sets uses explicitly rounded intrinsics
+// (__fsub_rn/__fmul_rn/__fadd_rn/__fdiv_rn and the double forms) so nvcc cannot contract
+// a*b+c into an FMA or substitute an approximate divide.  Pair functions (the physics)
+// are free to use fast math: only their sums are compared, within a tolerance.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/pn_gb300.h"
+
+namespace pn {
+
+// ------------------------------------------------------------------ exact arithmetic
+__device__ __forceinline__ float xsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float xadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float xmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float xdiv(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double xsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double xadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double xmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double xdiv(double a, double b) { return __ddiv_rn(a, b); }
+__device__ __forceinline__ float xfloor(float a) { return floorf(a); }
+__device__ __forceinline__ double xfloor(double a) { return floor(a); }
+__device__ __forceinline__ float xrint(float a) { return rintf(a); }
+__device__ __forceinline__ double xrint(double a) { return rint(a); }
+
+// Julia Int64 arithmetic wraps around.
+__host__ __device__ __forceinline__ int64_t wadd(int64_t a, int64_t b) {
+  return (int64_t)((uint64_t)a + (uint64_t)b);
+}
+__host__ __device__ __forceinline__ int64_t wsub(int64_t a, int64_t b) {
+  return (int64_t)((uint64_t)a - (uint64_t)b);
+}
+// Julia `mod(x, n)` for n > 0.
+__host__ __device__ __forceinline__ int64_t jl_mod(int64_t x, int64_t n) {
+  int64_t r = x % n;
+  if (r != 0 && ((r < 0) != (n < 0))) r += n;
+  return r;
+}
+
+// util.jl:19-34 floor_to_int: saturating floor (NaN and >= 2^63 -> typemax).
+template <typename T>
+__device__ __forceinline__ int64_t floor_to_int(T x) {
+  const T r = xfloor(x);
+  if (isnan(r) || r >= (T)9223372036854775808.0) return INT64_MAX;
+  if (r <= -(T)9223372036854775808.0) return INT64_MIN;
+  return (int64_t)r;
+}
+
+// ------------------------------------------------------------------ grid description
+// Storage stride (in T) of one point in the cell-sorted coordinate array: 3D points are
+// padded to 4 components so that a point is one 16-byte (float) / 32-byte (double) load.
+template <int D>
+struct PS {
+  static constexpr int value = (D == 3) ? 4 : D;
+};
+
+template <typename T>
+struct GridDev {
+  int32_t n[3];        // padded FullGridCellList size per dimension
+  int32_t ncell[3];    // periodic cells per dimension (0 when not periodic)
+  int32_t n_total;     // prod(n)
+  int32_t pad_;
+  T min_pad[3];        // padded min corner (cell (1,1,1) starts here)
+  T cell_size[3];
+  T box_size[3];       // periodic box size
+  T half_box[3];       // box_size / 2
+  T r, r2;             // search radius and r*r (both in T)
+};
+
+// nhs_grid.jl:622-638 + full_grid.jl:84-94: the reference's cell coordinates, exactly,
+// for arbitrary inputs (saturation and Int64 wrap-around included).
+template <typename T, int D>
+__device__ __forceinline__ void cell_coords_exact(const GridDev<T>& g, bool periodic,
+                                                  const T* x, int64_t* c) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) {
+    const T q = xdiv(xsub(x[k], g.min_pad[k]), g.cell_size[k]);
+    int64_t ck = wadd(floor_to_int(q), 1);
+    if (periodic) ck = wadd(jl_mod(wsub(ck, 2), (int64_t)g.ncell[k]), 2);
+    c[k] = ck;
+  }
+}
+
+// Fast form used by the kernels: the 1-based cell coordinate of one dimension as int32,
+// and whether it is a valid cell (2 <= c <= n-1, full_grid.jl:205-212).  Identical to
+// cell_coords_exact for every input: the saturated cases all fall outside the grid, or
+// take the int64 path in the periodic case.
+template <typename T>
+__device__ __forceinline__ bool cell_coord_1d(const GridDev<T>& g, bool periodic, int k,
+                                              T xk, int32_t& c) {
+  const T q = xdiv(xsub(xk, g.min_pad[k]), g.cell_size[k]);
+  const T fl = xfloor(q);
+  if (!periodic) {
+    // c = fl + 1 in 2..n-1  <=>  1 <= fl <= n-2 (false for NaN)
+    const bool ok = (fl >= (T)1) && (fl <= (T)(g.n[k] - 2));
+    c = ok ? (int32_t)fl + 1 : 0;
+    return ok;
+  }
+  const int64_t nc = g.ncell[k];
+  int64_t m;
+  if (fl >= (T)-4611686018427387904.0 && fl <= (T)4611686018427387904.0) {
+    m = (int64_t)fl - 1;  // (fl + 1) - 2, no overflow in this range
+    if (m < 0 && m >= -nc) m += nc;
+    else if (m >= nc && m < 2 * nc) m -= nc;
+    else if (m < 0 || m >= nc) m = jl_mod(m, nc);
+  } else {
+    m = jl_mod(wsub(wadd(floor_to_int(q), 1), 2), nc);
+  }
+  // periodic cells are 2..ncell+1; check_cell_bounds still applies (full_grid.jl:205-212)
+  c = (int32_t)(m + 2);
+  return c <= g.n[k] - 1;
+}
+
+// ------------------------------------------------------------------ errors
+// Sticky per-search error word: the first error code set by any kernel wins.
+__device__ __forceinline__ void set_error(int32_t* err, int32_t code) {
+  if (*(volatile int32_t*)err == 0) atomicCAS(err, 0, code);
+}
+
+__device__ __forceinline__ unsigned lanemask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ------------------------------------------------------------------ launch helpers
+inline int div_up(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
+
+}  // namespace pn
+
+// ------------------------------------------------------------------ host -> device grid
+#include "pn_host.h"
+
+namespace pn {
+
+template <typename T>
+inline GridDev<T> make_grid(const pn_search* s) {
+  GridDev<T> g{};
+  g.n_total = s->n_total;
+  for (int k = 0; k < 3; ++k) {
+    const bool used = k < s->ndims;
+    g.n[k] = used ? (int32_t)s->grid_size[k] : 1;
+    g.ncell[k] = (used && s->periodic) ? (int32_t)s->n_cells[k] : 0;
+    g.min_pad[k] = used ? (T)s->min_pad[k] : (T)0;
+    g.cell_size[k] = used ? (T)s->cell_size[k] : (T)1;
+    g.box_size[k] = used && s->periodic ? (T)s->box_size[k] : (T)0;
+    g.half_box[k] = g.box_size[k] / (T)2;
+  }
+  g.r = (T)s->radius;
+  g.r2 = g.r * g.r;
+  return g;
+}
+
+}  // namespace pn

@@ -1,0 +1,7 @@
+// pn_traverse_f64.cu -- foreach_point_neighbor kernels for Float64 searches.
+#include "pn_traverse_impl.cuh"
+
+namespace pn {
+template int foreach<double>(pn_search*, int32_t, const double*, int64_t, const double*, int64_t,
+                             const int32_t*, int64_t, const void*, cudaStream_t);
+}  // namespace pn

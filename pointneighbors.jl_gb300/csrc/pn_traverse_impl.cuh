@@ -1,0 +1,215 @@
+// pn_traverse_impl.cuh -- host dispatch of foreach_point_neighbor for one element type;
+// included by pn_traverse_f32.cu and pn_traverse_f64.cu.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+#include "pn_traverse.cuh"
+
+namespace pn {
+
+// Writes PN_ERR_CAPACITY when the neighbour lists do not fit (total read on the device).
+static __global__ void k_check_capacity(const int64_t* total, int64_t capacity, int32_t* err) {
+  if (*total > capacity) set_error(err, PN_ERR_CAPACITY);
+}
+
+// Sorted WCSPH state from user arrays (original order) for a standalone FORCE call.
+template <typename T, int D>
+__global__ void __launch_bounds__(256)
+k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int32_t n_slots_max,
+               const int32_t* __restrict__ n_slots, const T* __restrict__ density,
+               const T* __restrict__ pressure, const T* __restrict__ velocity,
+               T* __restrict__ pa, T* __restrict__ pb) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_slots_max || k >= *n_slots) return;
+  const int32_t i = perm[k];
+  if (i < 0) return;
+  T x[D];
+  load_pos<T, D>(pos, k, x);
+  const T rho = density[i];
+  V4<T> va{(T)0, (T)0, (T)0, pressure[i] / (rho * rho)};
+  V4<T> vb{(T)0, (T)0, (T)0, rho};
+  T* xa = &va.x;
+  T* xb = &vb.x;
+#pragma unroll
+  for (int d = 0; d < D; ++d) {
+    xa[d] = x[d];
+    xb[d] = velocity[(int64_t)i * D + d];
+  }
+  store4(pa, k, va);
+  store4(pb, k, vb);
+}
+
+template <typename T, template <typename, int> class F>
+static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename F<T, 1>::Params& p,
+                       bool sorted, int64_t n_launch, cudaStream_t st) {
+  const int blocks = div_up(n_launch, TRAV_THREADS);
+  if (blocks == 0) return PN_OK;
+  const int key = s->ndims * 2 + (s->periodic ? 1 : 0);
+#define PN_TRAV_CASE(KEY, DD, PP)                                                       \
+  case KEY:                                                                             \
+    if (sorted)                                                                         \
+      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
+    else                                                                                \
+      k_trav_list<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);          \
+    break;
+  switch (key) {
+    PN_TRAV_CASE(2, 1, false)
+    PN_TRAV_CASE(3, 1, true)
+    PN_TRAV_CASE(4, 2, false)
+    PN_TRAV_CASE(5, 2, true)
+    PN_TRAV_CASE(6, 3, false)
+    PN_TRAV_CASE(7, 3, true)
+    default: return PN_ERR_INVALID_ARG;
+  }
+#undef PN_TRAV_CASE
+  return cuda_status(cudaGetLastError());
+}
+
+template <typename T>
+static SphConst<T> sph_const(const pn_search* s, const pn_wcsph_params* w) {
+  SphConst<T> c{};
+  const double h = w->h;
+  const double pi = 3.14159265358979323846;
+  const double sigma = s->ndims == 3 ? 21.0 / (16.0 * pi * h * h * h)
+                     : s->ndims == 2 ? 7.0 / (4.0 * pi * h * h)
+                                     : 5.0 / (8.0 * h);
+  c.mass = (T)w->mass;
+  c.h = (T)h;
+  c.inv_h = (T)(1.0 / h);
+  c.sigma = (T)sigma;
+  c.dw_coef = (T)(-5.0 * sigma / (h * h));
+  c.c0 = (T)w->c0;
+  c.rho0 = (T)w->rho0;
+  c.inv_rho0 = (T)(1.0 / w->rho0);
+  c.gamma = (T)w->gamma_exp;
+  c.gamma_int = (w->gamma_exp == std::floor(w->gamma_exp) && w->gamma_exp >= 1.0 &&
+                 w->gamma_exp <= 64.0) ? (int32_t)w->gamma_exp : 0;
+  c.eos_b = (T)(w->c0 * w->c0 * w->rho0 / w->gamma_exp);
+  c.alpha = (T)w->alpha;
+  c.eps_h2 = (T)(w->eps_visc * h * h);
+  c.r_min2 = (T)(w->r_min * w->r_min);
+  return c;
+}
+
+template <typename T>
+int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
+            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st) {
+  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
+  if (n_y != s->n_y || n_x < 0 || (points == nullptr && n_points != 0 && n_points != n_x))
+    return PN_ERR_INVALID_ARG;
+  if (params == nullptr) return PN_ERR_INVALID_ARG;
+  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && points == nullptr &&
+                      s->full_binned;
+  const int64_t n_q = points ? n_points : n_x;
+
+  TravArgs<T> a{};
+  a.g = make_grid<T>(s);
+  a.start = s->d_start;
+  a.ovf_start = s->ovf_active ? s->d_ovf_start : nullptr;
+  a.perm = s->d_perm;
+  a.cell_of_slot = s->d_cell_of_slot;
+  a.pos = static_cast<const T*>(s->d_pos);
+  a.x = x;
+  a.qlist = points;
+  a.n_q = n_q;
+  a.n_x = n_x;
+  a.err = s->d_err;
+  // Sorted mode launches one thread per possible slot; the kernel reads the live count.
+  const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
+  const int64_t n_launch = sorted ? n_sorted : n_q;
+
+  switch (functor) {
+    case PN_F_COUNT: {
+      const auto* u = static_cast<const pn_count_params*>(params);
+      CountParams<T> p{u->counts, 0};
+      return launch_trav<T, FCount>(s, a, p, sorted, n_launch, st);
+    }
+    case PN_F_INDEX_SUM: {
+      const auto* u = static_cast<const pn_index_sum_params*>(params);
+      IndexSumParams<T> p{u->sums, s->d_perm};
+      return launch_trav<T, FIndexSum>(s, a, p, sorted, n_launch, st);
+    }
+    case PN_F_NEIGHBOR_LIST: {
+      const auto* u = static_cast<const pn_neighbor_list_params*>(params);
+      if (u->offsets == nullptr) return PN_ERR_INVALID_ARG;
+      int32_t* counts = u->counts;
+      if (counts == nullptr) {
+        int rc = ensure_qcount(s, n_q);
+        if (rc != PN_OK) return rc;
+        counts = s->d_qcount;
+      }
+      CountParams<T> pc{counts, 1};
+      int rc = launch_trav<T, FCount>(s, a, pc, sorted, n_launch, st);
+      if (rc != PN_OK) return rc;
+      rc = scan64(s, counts, n_q, u->offsets, st);
+      if (rc != PN_OK) return rc;
+      k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err);
+      if (u->neighbors == nullptr || u->capacity <= 0) return cuda_status(cudaGetLastError());
+      EmitParams<T> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
+      rc = launch_trav<T, FEmit>(s, a, pe, sorted, n_launch, st);
+      if (rc != PN_OK) return rc;
+      if (u->sort_rows) rc = sort_rows(s, u->offsets, n_q, u->neighbors, u->capacity, st);
+      return rc;
+    }
+    case PN_F_NBODY_ACCEL: {
+      const auto* u = static_cast<const pn_nbody_params*>(params);
+      const T eps_t = std::numeric_limits<T>::epsilon();
+      NBodyParams<T> p{static_cast<const T*>(u->masses), s->d_perm, (T)u->G, std::sqrt(eps_t),
+                       static_cast<T*>(u->accel)};
+      return launch_trav<T, FNBody>(s, a, p, sorted, n_launch, st);
+    }
+    case PN_F_POTENTIAL: {
+      const auto* u = static_cast<const pn_potential_params*>(params);
+      if ((const void*)x != (const void*)y) return PN_ERR_INVALID_ARG;
+      PotentialParams<T> p{static_cast<const T*>(u->masses), s->d_perm, (T)u->cutoff,
+                           (T)(1.0 / u->cutoff), static_cast<T*>(u->energy)};
+      return launch_trav<T, FPotential>(s, a, p, sorted, n_launch, st);
+    }
+    case PN_F_WCSPH_DENSITY:
+    case PN_F_WCSPH_STEP: {
+      const auto* u = static_cast<const pn_wcsph_params*>(params);
+      const bool step = functor == PN_F_WCSPH_STEP;
+      if (step && !sorted) return PN_ERR_INVALID_ARG;
+      DensityParams<T> p{sph_const<T>(s, u), static_cast<T*>(u->density),
+                         static_cast<T*>(u->pressure), static_cast<const T*>(u->velocity),
+                         nullptr, nullptr};
+      if (step) {
+        p.pa = static_cast<T*>(s->d_pa);
+        p.pb = static_cast<T*>(s->d_pb);
+      }
+      int rc = launch_trav<T, FDensity>(s, a, p, sorted, n_launch, st);
+      if (rc != PN_OK || !step) return rc;
+      ForceParams<T> pf{p.c, static_cast<const T*>(s->d_pa), static_cast<const T*>(s->d_pb),
+                        static_cast<T*>(u->accel)};
+      return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
+    }
+    case PN_F_WCSPH_FORCE: {
+      const auto* u = static_cast<const pn_wcsph_params*>(params);
+      if (!sorted) return PN_ERR_INVALID_ARG;
+      const int b = div_up(n_sorted, 256);
+      const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
+      const T* pos = static_cast<const T*>(s->d_pos);
+      T* pa = static_cast<T*>(s->d_pa);
+      T* pb = static_cast<T*>(s->d_pb);
+      const T* dn = static_cast<const T*>(u->density);
+      const T* pr = static_cast<const T*>(u->pressure);
+      const T* ve = static_cast<const T*>(u->velocity);
+      if (b > 0) {
+        switch (s->ndims) {
+          case 1: k_gather_state<T, 1><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); break;
+          case 2: k_gather_state<T, 2><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); break;
+          default: k_gather_state<T, 3><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); break;
+        }
+      }
+      ForceParams<T> pf{sph_const<T>(s, u), pa, pb, static_cast<T*>(u->accel)};
+      return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
+    }
+    default:
+      return PN_ERR_UNSUPPORTED_FUNCTOR;
+  }
+}
+
+}  // namespace pn

@@ -1,0 +1,157 @@
+"""C ABI checks that need no GPU: the library loads, exports every entry point that
+include/pn_gb300.h declares, its structs have the layout the ctypes binding assumes, and the
+host-side geometry (pn_compute_geometry) equals the oracle's restatement of the reference
+constructors.  The Python host API's argument checks that run before any device call are
+covered too."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "pn_gb300.h")
+
+
+@pytest.fixture(scope="module")
+def L(pkg):
+    pkg.build.build()
+    return pkg._lib
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(pn_\w+)\s*\(", src, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(L):
+    lib = L.load()
+    names = declared_functions()
+    assert len(names) >= 14
+    out = subprocess.run(["nm", "-D", "--defined-only", L.LIB_PATH], capture_output=True,
+                         text=True, check=True).stdout
+    exported = set(re.findall(r" T (pn_\w+)$", out, flags=re.M))
+    for n in names:
+        assert n in exported, n
+        getattr(lib, n)
+    assert lib.pn_abi_version() == 1
+
+
+def test_struct_layout_matches_header(L, tmp_path):
+    structs = {"pn_config": L.pn_config, "pn_grid_info": L.pn_grid_info,
+               "pn_count_params": L.pn_count_params,
+               "pn_index_sum_params": L.pn_index_sum_params,
+               "pn_neighbor_list_params": L.pn_neighbor_list_params,
+               "pn_nbody_params": L.pn_nbody_params,
+               "pn_potential_params": L.pn_potential_params,
+               "pn_wcsph_params": L.pn_wcsph_params}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(){"]
+    for name, cls in structs.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for f, _ in cls._fields_:
+            lines.append(f'printf("{name}.{f} %zu\\n", offsetof({name}, {f}));')
+    lines.append("return 0;}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", str(src), "-o", str(exe)], check=True)
+    got = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True,
+                                                         text=True, check=True).stdout.split("\n") if l)
+    for name, cls in structs.items():
+        assert int(got[name]) == C.sizeof(cls), name
+        for f, _ in cls._fields_:
+            assert int(got[f"{name}.{f}"]) == getattr(cls, f).offset, f"{name}.{f}"
+
+
+def _geometry(L, ndims, dtype, r, mn, mx, box=None):
+    cfg = L.pn_config()
+    cfg.ndims = ndims
+    cfg.dtype = L.PN_FLOAT32 if dtype == np.float32 else L.PN_FLOAT64
+    cfg.search_radius = float(dtype(r))
+    for k in range(ndims):
+        cfg.min_corner[k] = float(dtype(mn[k]))
+        cfg.max_corner[k] = float(dtype(mx[k]))
+    if box is not None:
+        cfg.periodic = 1
+        for k in range(ndims):
+            cfg.periodic_min[k] = float(dtype(box[0][k]))
+            cfg.periodic_max[k] = float(dtype(box[1][k]))
+    gi = L.pn_grid_info()
+    rc = L.load().pn_compute_geometry(C.byref(cfg), C.byref(gi))
+    return rc, gi
+
+
+GEOMS = [
+    (3, np.float64, 3.0, [-1.0] * 3, [51.0] * 3, None),           # 50^3 lattice, r = 3
+    (3, np.float32, 3.0, [-1.0] * 3, [201.0] * 3, None),          # 200^3 lattice, r = 3
+    (2, np.float32, 2.5, [0.0, 0.0], [4096.0, 4096.0], ([0.0, 0.0], [4096.0, 4096.0])),
+    (2, np.float64, 0.1, [-0.1, -0.2], [0.2, 0.4], ([-0.1, -0.2], [0.2, 0.4])),
+    (2, np.float64, 0.1, [-0.1, -0.2], [0.205, 0.43], ([-0.1, -0.2], [0.205, 0.43])),
+    (3, np.float64, 0.1, [-0.1, -0.2, 0.05], [0.2, 0.4, 0.35], ([-0.1, -0.2, 0.05], [0.2, 0.4, 0.35])),
+    (1, np.float64, 1.0, [0.0], [10.0], None),
+    (2, np.float32, 3.0, [1.0, 1.0], [100.0, 100.0], None),
+    (2, np.float32, 0.1, [0.0, 0.0], [1.0, 1.0], ([0.0, 0.0], [1.0, 1.0])),
+]
+
+
+@pytest.mark.parametrize("g", GEOMS)
+def test_geometry_equals_oracle(L, O, g):
+    ndims, dt, r, mn, mx, box = g
+    rc, gi = _geometry(L, ndims, dt, r, mn, mx, box)
+    assert rc == 0
+    og = O.grid_create(ndims, dt(r), np.array(mn, dt), np.array(mx, dt),
+                       periodic_box=None if box is None else (np.array(box[0], dt), np.array(box[1], dt)),
+                       dtype=dt)
+    for k in range(ndims):
+        assert gi.grid_size[k] == og.n[k]
+        assert gi.min_corner[k] == og.min_pad[k]
+        assert gi.max_corner[k] == og.max_pad[k]
+        assert gi.cell_size[k] == og.cell_size[k]
+        assert gi.n_cells[k] == og.n_cells[k]
+
+
+def test_geometry_known_values(L):
+    # test/cell_lists/full_grid.jl:28-29
+    rc, gi = _geometry(L, 3, np.float64, 1.0, [0.0] * 3, [10.0] * 3)
+    assert rc == 0 and list(gi.min_corner) == [-1.001] * 3 and list(gi.max_corner) == [11.001] * 3
+    # the 2D periodic n-body workload: 1638 periodic cells of 4096/1638, 1641 grid cells
+    rc, gi = _geometry(L, 2, np.float32, 2.5, [0.0, 0.0], [4096.0, 4096.0],
+                       ([0.0, 0.0], [4096.0, 4096.0]))
+    assert rc == 0 and gi.n_cells[0] == 1638 and gi.grid_size[0] == 1641
+    assert gi.cell_size[0] == float(np.float32(4096.0) / np.float32(1638))
+    # fewer than 3 periodic cells is an ArgumentError (nhs_grid.jl:120-124)
+    rc, _ = _geometry(L, 2, np.float64, 1.0, [0.0, 0.0], [2.5, 2.5], ([0.0, 0.0], [2.5, 2.5]))
+    assert rc == L.PN_ERR_INVALID_ARG
+
+
+def test_status_strings_are_the_references(L):
+    assert L.status_string(L.PN_ERR_OUT_OF_DOMAIN) == \
+        "particle coordinates are NaN or outside the domain bounds of the cell list"
+    assert L.status_string(L.PN_ERR_CELL_FULL) == \
+        "cell list is full. Use a larger `max_points_per_cell`."
+
+
+def test_host_api_argument_errors(pkg):
+    P = pkg
+    with pytest.raises(P.ArgumentError, match="same length"):
+        P.FullGridCellList(min_corner=[0.0, 0.0, 0.0], max_corner=[1.0, 1.0])
+    with pytest.raises(P.ArgumentError, match="up to 100 dimensions"):
+        P.FullGridCellList(min_corner=np.zeros(101), max_corner=np.ones(101))
+    cl3 = P.FullGridCellList(min_corner=[0.0] * 3, max_corner=[1.0] * 3, search_radius=1.0)
+    assert list(cl3.min_corner) == [-1.001] * 3 and list(cl3.max_corner) == [2.001] * 3
+    with pytest.raises(P.ArgumentError, match="a 2D cell list is required for a GridNeighborhoodSearch"):
+        P.GridNeighborhoodSearch(2, search_radius=1.0, cell_list=cl3)
+    with pytest.raises(P.ArgumentError, match="is not a valid update strategy"):
+        P.GridNeighborhoodSearch(3, search_radius=1.0, cell_list=cl3, update_strategy="test")
+    with pytest.raises(P.ArgumentError, match="cannot be an integer type"):
+        P.GridNeighborhoodSearch(3, search_radius=1, cell_list=cl3)
+    box32 = P.PeriodicBox(min_corner=np.zeros(3, np.float32), max_corner=np.ones(3, np.float32))
+    with pytest.raises(P.ArgumentError, match="same element type"):
+        P.GridNeighborhoodSearch(3, search_radius=1.0, cell_list=cl3, periodic_box=box32)
+    assert P.requires_update(None) == (False, True)
+    with pytest.raises(P.UnsupportedFunctorError):
+        P.foreach_point_neighbor(lambda i, j, pd, d: None, None, None, None)
