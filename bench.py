@@ -1,0 +1,419 @@
+#!/usr/bin/env python
+"""Benchmark: WCSPH pair-evaluations/s and update! ms on one GB300.
+
+Workload (the default): a 200^3 = 8,000,000-point 3D lattice, spacing 1, uniform noise in
+[-0.25, 0.25], Float32, search radius 3, FullGridCellList over [-1, 201]^3, velocities
+N(0, 0.1^2).  A step is the hot path once over the whole cloud:
+  update!(positions displaced by N(0, 0.05^2))   (ParallelIncrementalUpdate)
+  WCSPH density sweep (Wendland C2, h = 1.5) + Tait EOS
+  WCSPH force sweep (pressure + Monaghan viscosity)
+pair-evals/s = 2 sweeps x (ordered pairs with d^2 <= r^2, self included) per step / time.
+`value` is device time with the inputs resident in HBM; `e2e` is the same step through the
+C ABI with the coordinates and velocities copied from pinned host memory and the density
+and acceleration copied back inside the timed region.
+
+`--impl reference` times the CPU restatement of the reference's algorithm (the oracle:
+threaded cell-list build + per-point traversal, pair math in FP64) on the host cores, on a
+bounded sample of query points of the same workload.
+
+Multi-GPU (`--gpus N` under torchrun): independent replicas, one per GPU (the search does
+not exchange data between GPUs); the time is the max over ranks and the value sums all
+ranks' pairs.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+METRIC = "WCSPH pair-evals/s (8M pts, FP32, r=3, density+force+incremental update!)"
+UNIT = "pair-evals/s"
+# Algorithmic bytes per point of one force sweep (FP32): read x 12, v 12, rho 4, the
+# point's index 4, write the acceleration 12.
+FORCE_BYTES_PER_POINT = {"float32": 44, "float64": 84}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n-side", type=int, default=200, help="lattice points per dimension")
+    ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--cpu-sample", type=int, default=400_000,
+                    help="query points in the CPU baseline sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ distributed
+
+def dist_setup(backend: str):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend)
+    return rank, world, local
+
+
+def aggregate(local_seconds: float, local_pairs: float, world: int, device=None):
+    """Max of the timed region over ranks, sum of the evaluated pairs."""
+    if world == 1:
+        return local_seconds, local_pairs
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([local_seconds], dtype=torch.float64, device=device)
+    p = torch.tensor([local_pairs], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(p, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(p.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ------------------------------------------------------------------ clocks
+
+CLOCK_FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+                "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+
+class ClockSampler:
+    def __init__(self, gpu_index: int):
+        self.path = tempfile.mktemp(prefix="pn_clocks_", suffix=".csv")
+        self.proc = None
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={CLOCK_FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+# ------------------------------------------------------------------ GPU arm
+
+def run_gpu(args, rank, world, local):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    P = __graft_entry__.package()
+    W = P.workloads
+    torch.cuda.set_device(local)
+    dt = np.float32 if args.dtype == "float32" else np.float64
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    n_side = args.n_side
+    x0, v, dx = W.wcsph_cloud(n_side, seed=1, dtype=dt)
+    x1 = (x0.astype(np.float64) + dx).astype(dt)
+    n = len(x0)
+    r = dt(3.0)
+    cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt), max_corner=np.full(3, n_side + 1.0, dt),
+                            search_radius=r, max_points_per_cell=0)
+    nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                   update_strategy=P.ParallelIncrementalUpdate())
+    x0d = torch.as_tensor(x0, device="cuda").T
+    x1d = torch.as_tensor(x1, device="cuda").T
+    vd = torch.as_tensor(v, device="cuda").reshape(-1)
+    rho = torch.zeros(n, dtype=tdt, device="cuda")
+    prs = torch.zeros(n, dtype=tdt, device="cuda")
+    acc = torch.zeros(3 * n, dtype=tdt, device="cuda")
+    dens = P.WCSPHDensity(density=rho, pressure=prs, velocity=vd, **W.WCSPH)
+    force = P.WCSPHForce(density=rho, pressure=prs, velocity=vd, accel=acc, reuse_state=True,
+                         **W.WCSPH)
+    P.initialize(nhs, x0d, x0d)
+
+    def step(x):
+        P.update(nhs, x, x, check=False)
+        P.foreach_point_neighbor(dens, x, x, nhs, check=False)
+        P.foreach_point_neighbor(force, x, x, nhs, check=False)
+
+    # pairs per sweep at the step's positions (untimed)
+    P.update(nhs, x1d, x1d)
+    cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt), x1d, x1d, nhs)
+    pairs_per_sweep = int(cnt.to(torch.int64).sum())
+    del cnt
+
+    for _ in range(args.warmup):
+        step(x1d)
+    torch.cuda.synchronize()
+    if P.lib().pn_sync(nhs.handle) != 0:
+        raise RuntimeError("warm-up reported an error")
+
+    K = args.steps
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    launches0 = P.lib().pn_launch_count()
+    barrier(world)
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    t0.record()
+    for k in range(K):
+        e = ev[k]
+        e[0].record()
+        P.update(nhs, x1d, x1d, check=False)
+        e[1].record()
+        P.foreach_point_neighbor(dens, x1d, x1d, nhs, check=False)
+        e[2].record()
+        P.foreach_point_neighbor(force, x1d, x1d, nhs, check=False)
+        e[3].record()
+    t1.record()
+    torch.cuda.synchronize()
+    barrier(world)
+    wall = time.perf_counter() - wall0
+    launches = P.lib().pn_launch_count() - launches0
+    clocks = sampler.stop() if sampler else None
+    st = P.lib().pn_sync(nhs.handle)
+    if st != 0:
+        raise RuntimeError(f"timed region reported status {st}")
+    dev_s = t0.elapsed_time(t1) / 1e3
+    upd = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
+    den = [ev[k][1].elapsed_time(ev[k][2]) for k in range(K)]
+    frc = [ev[k][2].elapsed_time(ev[k][3]) for k in range(K)]
+    max_s, all_pairs = aggregate(dev_s, 2.0 * pairs_per_sweep * K, world,
+                                 device=torch.device("cuda"))
+    value = all_pairs / max_s
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        x1_h = torch.as_tensor(x1).pin_memory()
+        v_h = torch.as_tensor(v).reshape(-1).pin_memory()
+        rho_h = torch.empty(n, dtype=tdt).pin_memory()
+        acc_h = torch.empty(3 * n, dtype=tdt).pin_memory()
+        x1dev = torch.empty((n, 3), dtype=tdt, device="cuda")
+        xb = x1dev.T
+
+        def e2e_step():
+            x1dev.copy_(x1_h, non_blocking=True)
+            vd.copy_(v_h, non_blocking=True)
+            P.update(nhs, xb, xb, check=False)
+            P.foreach_point_neighbor(dens, xb, xb, nhs, check=False)
+            P.foreach_point_neighbor(force, xb, xb, nhs, check=False)
+            rho_h.copy_(rho, non_blocking=True)
+            acc_h.copy_(acc, non_blocking=True)
+
+        for _ in range(max(3, args.warmup // 2)):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier(world)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record()
+        for _ in range(K):
+            e2e_step()
+        a1.record()
+        torch.cuda.synchronize()
+        barrier(world)
+        e2e_s, e2e_pairs = aggregate(a0.elapsed_time(a1) / 1e3, 2.0 * pairs_per_sweep * K, world,
+                                     device=torch.device("cuda"))
+        if P.lib().pn_sync(nhs.handle) != 0:
+            raise RuntimeError("e2e region reported an error")
+        tb = 4 if dt == np.float32 else 8
+        e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 6 * n * tb,
+               "d2h_bytes_per_step": 4 * n * tb, "ms_per_step": 1e3 * e2e_s / K,
+               "path": "pinned host -> cudaMemcpyAsync -> pn_update + pn_foreach_point_neighbor "
+                       "(density, force) -> device->host density and acceleration"}
+
+    peak, peak_kind = hbm_peak()
+    t_force = statistics.median(frc) / 1e3
+    alg = FORCE_BYTES_PER_POINT[args.dtype] * n
+    achieved = alg / t_force / 1e9
+    roofline = {"bound": "hbm", "kernel": "k_trav_sorted<FForce> (force sweep)",
+                "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": None,
+                "algorithmic_bytes_per_launch": alg}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(x1, v, args, dt)
+
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": 1e3 * max_s / K, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == np.float32 else "f64",
+        "data": "synthetic (seeded perturbed lattice, numpy PCG64)",
+        "config": {"workload": f"WCSPH step, {n_side}^3 = {n:,} points 3D lattice, spacing 1, "
+                               "U[-0.25,0.25] noise, r=3, FullGridCellList [-1,201]^3, "
+                               "displacement N(0,0.05^2), ParallelIncrementalUpdate",
+                   "n_points": n, "search_radius": 3.0,
+                   "pairs_per_sweep": pairs_per_sweep,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "working set > L2 (coordinates, sorted copies and outputs ~1 GB), no flush"},
+        "update_ms": statistics.median(upd), "density_ms": statistics.median(den),
+        "force_ms": statistics.median(frc), "wall_ms_per_step": 1e3 * wall / K,
+        "gpu_launches": int(launches), "launches_per_step": launches / K,
+        "roofline": roofline, "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu,
+        "gpu": torch.cuda.get_device_name(),
+    }
+    if rank == 0:
+        print(json.dumps(out))
+
+
+# ------------------------------------------------------------------ CPU (oracle)
+
+def cpu_measure(x1, v, sample_n, dt, repeats=1):
+    """Time the oracle on the host cores: threaded build of all points, then the density
+    and force sweeps for `sample_n` query points.  Returns a dict of timings."""
+    from oracle import pn_oracle as O
+    from __graft_entry__ import package
+    W = package().workloads
+    n = len(x1)
+    side = round(n ** (1 / 3))
+    nthreads = O.n_threads_default()
+    g = O.grid_create(3, dt(3.0), np.full(3, -1.0, dt), np.full(3, side + 1.0, dt),
+                      max_ppc=64, dtype=dt)
+    rng = np.random.default_rng(3)
+    sample = np.sort(rng.choice(n, min(sample_n, n), replace=False)).astype(np.int32)
+    t = time.perf_counter()
+    cl = O.build(g, x1, parallel_threads=nthreads)
+    t_build = time.perf_counter() - t
+    prm, keep = O.make_params(**W.WCSPH)
+    cnt = O.foreach(g, cl, x1, x1, O.F_COUNT, points=sample, n_threads=nthreads)
+    pairs = int(cnt[sample].astype(np.int64).sum())
+    best = None
+    for _ in range(repeats):
+        t = time.perf_counter()
+        rho = O.foreach(g, cl, x1, x1, O.F_WCSPH_DENSITY, prm, points=sample, n_threads=nthreads)
+        t_den = time.perf_counter() - t
+        # pressure from the density (Tait), then the force sweep
+        c = W.WCSPH
+        p = c["c0"] ** 2 * c["rho0"] / c["gamma_exp"] * ((rho / c["rho0"]) ** c["gamma_exp"] - 1)
+        rho_full = np.where(rho > 0, rho, 1.0)
+        prm2, keep2 = O.make_params(rho=rho_full, pressure=p, vel=v.astype(np.float64),
+                                    r_min=float(np.sqrt(np.finfo(dt).eps)) * c["h"], **c)
+        t = time.perf_counter()
+        O.foreach(g, cl, x1, x1, O.F_WCSPH_FORCE, prm2, points=sample, n_threads=nthreads)
+        t_frc = time.perf_counter() - t
+        cur = (t_den + t_frc, t_den, t_frc)
+        best = cur if best is None or cur[0] < best[0] else best
+    return {"pairs_sample": 2 * pairs, "t_sweeps": best[0], "t_density": best[1],
+            "t_force": best[2], "t_build": t_build, "threads": nthreads,
+            "sample": len(sample), "n": n}
+
+
+def cpu_baseline(x1, v, args, dt):
+    m = cpu_measure(x1, v, args.cpu_sample, dt)
+    return {"value": m["pairs_sample"] / m["t_sweeps"], "unit": UNIT, "cores": m["threads"],
+            "kind": "port",
+            "sample": f"density+force sweeps for {m['sample']:,} of {m['n']:,} query points "
+                      f"(cell list of all points, built in {m['t_build'] * 1e3:.0f} ms); "
+                      "CPU restatement of the reference algorithm, pair math in FP64",
+            "update_ms": m["t_build"] * 1e3}
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement on the host cores, rank 0 only."""
+    if rank != 0:
+        return
+    from __graft_entry__ import package
+    from oracle import build_oracle
+    build_oracle.build()
+    W = package().workloads
+    dt = np.float32 if args.dtype == "float32" else np.float64
+    x0, v, dx = W.wcsph_cloud(args.n_side, seed=1, dtype=dt)
+    x1 = (x0.astype(np.float64) + dx).astype(dt)
+    # each step is a bounded sample: the full cell-list build plus the two sweeps over a
+    # sample of query points, sized so that warm-up + steps finish within minutes
+    sample = max(10_000, args.cpu_sample // 8)
+    for _ in range(args.warmup):
+        cpu_measure(x1, v, sample // 4, dt)
+    times, pairs, builds = [], 0, []
+    for _ in range(args.steps):
+        m = cpu_measure(x1, v, sample, dt)
+        times.append(m["t_sweeps"])
+        builds.append(m["t_build"])
+        pairs += m["pairs_sample"]
+    value = pairs / sum(times)
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * sum(times) / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32" if dt == np.float32 else "f64", "data": "synthetic (seeded perturbed lattice)",
+        "impl": "reference",
+        "config": {"workload": f"WCSPH step, {args.n_side}^3 points, r=3 (CPU sample of "
+                               f"{sample:,} query points per step)"},
+        "update_ms": 1e3 * statistics.median(builds),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": m["threads"], "kind": "port",
+                         "sample": f"{sample:,} query points per step, full cell-list build"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        world = int(os.environ.get("WORLD_SIZE", "1"))
+        run_reference(args, rank, world)
+        return
+    rank, world, local = dist_setup("nccl")
+    try:
+        run_gpu(args, rank, world, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -140,7 +140,9 @@ typedef struct {
 /* Weakly compressible SPH: Wendland C2 kernel (support 2h), Tait equation of state
  * p = c0^2 rho0 / gamma ((rho/rho0)^gamma - 1), momentum equation with Monaghan artificial
  * viscosity (alpha, beta = 0, mu = h v.x / (d^2 + eps_visc h^2)).
- * DENSITY: density[i] = sum_j m W(d_ij) (self included), pressure[i] = EOS(density[i]).
+ * DENSITY: density[i] = sum_j m W(d_ij) (self included), pressure[i] = EOS(density[i]);
+ *          when x is y and velocity is given, it also keeps a cell-sorted copy of
+ *          (x, p/rho^2) and (v, rho) in the search for a following FORCE call.
  * FORCE:   accel[i] = -sum_{j, d>r_min} m (p_i/rho_i^2 + p_j/rho_j^2 + Pi_ij) grad W_ij,
  *          reading density, pressure, velocity (x == y required).
  * STEP:    DENSITY then FORCE in one call. */
@@ -151,6 +153,11 @@ typedef struct {
   void* pressure;        /* T[n]: out for DENSITY/STEP, in for FORCE                       */
   const void* velocity;  /* T[n * d]: in for FORCE/STEP                                    */
   void* accel;           /* T[n * d]: out for FORCE/STEP                                   */
+  int32_t reuse_state;   /* FORCE: 1 = the previous call on this search was a DENSITY
+                            call (x is y, same velocity) whose cell-sorted copy of
+                            density, pressure and velocity is still valid; 0 = gather
+                            them from the arrays above                                 */
+  int32_t pad_;
 } pn_wcsph_params;
 
 /* ----------------------------------------------------------------- lifetime */
@@ -219,6 +226,9 @@ int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stre
 int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream);
 
 int pn_abi_version(void);
+
+/* Number of CUDA kernels the library has launched in this process (all searches). */
+unsigned long long pn_launch_count(void);
 
 #ifdef __cplusplus
 }

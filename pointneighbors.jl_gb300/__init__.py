@@ -461,8 +461,9 @@ class TruncatedPotential(PairFunction):
 class _WCSPH(PairFunction):
     def __init__(self, *, density=None, pressure=None, velocity=None, accel=None, mass=1.0,
                  h=1.5, c0=10.0, rho0=1.0, gamma_exp=7.0, alpha=0.02, eps_visc=0.01,
-                 r_min=None):
+                 r_min=None, reuse_state=False):
         self.density, self.pressure, self.velocity, self.accel = density, pressure, velocity, accel
+        self.reuse_state = bool(reuse_state)
         self.consts = dict(mass=mass, h=h, c0=c0, rho0=rho0, gamma_exp=gamma_exp, alpha=alpha,
                            eps_visc=eps_visc)
         self.r_min = r_min
@@ -474,7 +475,7 @@ class _WCSPH(PairFunction):
         r_min = self.r_min
         if r_min is None:
             r_min = float(np.sqrt(np.finfo(nhs.eltype).eps)) * self.consts["h"]
-        p = _lib.pn_wcsph_params(r_min=r_min, **self.consts)
+        p = _lib.pn_wcsph_params(r_min=r_min, reuse_state=int(self.reuse_state), **self.consts)
         for name, size in (("density", n), ("pressure", n), ("velocity", n * d),
                            ("accel", n * d)):
             t = getattr(self, name)

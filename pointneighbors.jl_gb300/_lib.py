@@ -84,13 +84,15 @@ class pn_wcsph_params(C.Structure):
         ("mass", C.c_double), ("h", C.c_double), ("c0", C.c_double), ("rho0", C.c_double),
         ("gamma_exp", C.c_double), ("alpha", C.c_double), ("eps_visc", C.c_double),
         ("r_min", C.c_double), ("density", C.c_void_p), ("pressure", C.c_void_p),
-        ("velocity", C.c_void_p), ("accel", C.c_void_p),
+        ("velocity", C.c_void_p), ("accel", C.c_void_p), ("reuse_state", C.c_int32),
+        ("pad_", C.c_int32),
     ]
 
 
 _P = C.c_void_p
 _SIGNATURES = {
     "pn_abi_version": (C.c_int, []),
+    "pn_launch_count": (C.c_ulonglong, []),
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),
     "pn_destroy": (C.c_int, [_P]),

@@ -9,6 +9,7 @@
 //     at least 3 cells per dimension.
 // This file is compiled with -ffp-contract=off for the host compiler as well, so these T
 // expressions are rounded exactly like Julia's.
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -19,6 +20,9 @@
 namespace pn {
 
 int cuda_status(cudaError_t e) { return e == cudaSuccess ? PN_OK : PN_ERR_CUDA; }
+
+static std::atomic<unsigned long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 static void free_points(pn_search* s) {
   void* ptrs[] = {s->d_cell_of, s->d_slot_of, s->d_tmp_perm, s->d_perm, s->d_cell_of_slot,
@@ -124,6 +128,10 @@ static int geometry(pn_search* s) {
       if (nc > 1e9) return PN_ERR_INVALID_ARG;
       s->n_cells[k] = (int64_t)nc;
       s->cell_size[k] = (double)(T)(size / (T)s->n_cells[k]);
+      // The periodic cells 2..n_cells+1 (and the stencil's wrap-around neighbours) must be
+      // cells of the padded grid; the reference's tests always build the cell list over the
+      // periodic box, which gives n_cells + 3 <= grid_size.
+      if (s->n_cells[k] + 2 > s->grid_size[k]) return PN_ERR_INVALID_ARG;
     }
   }
   return PN_OK;
@@ -186,6 +194,8 @@ using namespace pn;
 extern "C" {
 
 int pn_abi_version(void) { return PN_ABI_VERSION; }
+
+unsigned long long pn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, out); }
 

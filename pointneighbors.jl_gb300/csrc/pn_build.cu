@@ -327,7 +327,7 @@ static void launch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* idx
   const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
   k_bin<T, D, PER><<<blocks, BIN_THREADS, 0, st>>>(make_grid<T>(s), y, n_y, idx, m,
                                                    s->d_cell_of, s->d_slot_of, s->d_counts,
-                                                   s->d_err);
+                                                   s->d_err); count_launch();
 }
 
 template <typename T>
@@ -351,9 +351,9 @@ static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st
   T* pos = static_cast<T*>(s->d_pos);
   const int32_t nt = s->n_total;
   switch (s->ndims) {
-    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); break;
-    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); break;
-    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); break;
+    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); count_launch(); break;
+    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); count_launch(); break;
+    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); count_launch(); break;
   }
 }
 
@@ -364,7 +364,7 @@ static void scan_cells(pn_search* s, const int32_t* counts, int32_t* start, cuda
   cudaMemsetAsync(s->d_scan_state, 0, sizeof(unsigned long long) * (s->scan_tiles + 1), st);
   k_scan_cells<<<s->scan_tiles, SCAN_THREADS, 0, st>>>(counts, s->n_total, start,
                                                        s->d_scan_state, s->scan_tiles,
-                                                       max_ppc, base_ptr, s->d_err);
+                                                       max_ppc, base_ptr, s->d_err); count_launch();
 }
 
 template <typename T>
@@ -378,7 +378,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
   if (m > 0) {
     k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
-                                              s->d_start, s->d_tmp_perm, s->d_cell_of_slot);
+                                              s->d_start, s->d_tmp_perm, s->d_cell_of_slot); count_launch();
     // Points rejected by the bounds check are not binned; every kernel that walks the
     // slots bounds itself by start[n_total], read on the device.
     launch_finalize<T>(s, y, (int32_t)m, st);
@@ -397,18 +397,18 @@ static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {
   k_mark_movers<T, D, PER><<<blocks, 256, 0, st>>>(
       make_grid<T>(s), s->d_main_perm, s->d_cell_of_slot, s->d_start + s->n_total, y,
       s->d_perm, static_cast<T*>(s->d_pos), s->d_ovf_counts, s->d_ovf_n, s->d_ovf_list,
-      s->d_ovf_cell, s->d_ovf_slot, s->d_err);
+      s->d_ovf_cell, s->d_ovf_slot, s->d_err); count_launch();
 }
 
 template <typename T, int D>
 static void launch_movers(pn_search* s, const T* y, cudaStream_t st) {
   k_scatter_movers<<<152 * 4, 256, 0, st>>>(s->d_ovf_n, s->d_ovf_list, s->d_ovf_cell,
                                              s->d_ovf_slot, s->d_ovf_start, s->d_tmp_perm,
-                                             s->d_cell_of_slot);
+                                             s->d_cell_of_slot); count_launch();
   k_finalize_movers<T, D><<<152 * 4, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot,
                                                    s->d_ovf_start, s->d_start + s->n_total,
                                                    s->n_total, y, s->d_perm,
-                                                   static_cast<T*>(s->d_pos));
+                                                   static_cast<T*>(s->d_pos)); count_launch();
 }
 
 template <typename T>
@@ -473,9 +473,9 @@ int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t 
   const bool per = s->periodic != 0;
   const int b = div_up(n, 256);
   switch (s->ndims) {
-    case 1: k_cell_coords<T, 1><<<b, 256, 0, st>>>(g, per, x, n, out); break;
-    case 2: k_cell_coords<T, 2><<<b, 256, 0, st>>>(g, per, x, n, out); break;
-    default: k_cell_coords<T, 3><<<b, 256, 0, st>>>(g, per, x, n, out); break;
+    case 1: k_cell_coords<T, 1><<<b, 256, 0, st>>>(g, per, x, n, out); count_launch(); break;
+    case 2: k_cell_coords<T, 2><<<b, 256, 0, st>>>(g, per, x, n, out); count_launch(); break;
+    default: k_cell_coords<T, 3><<<b, 256, 0, st>>>(g, per, x, n, out); count_launch(); break;
   }
   return cuda_status(cudaGetLastError());
 }
@@ -575,9 +575,9 @@ int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_
     if (cudaMalloc(&s->d_part, sizeof(int64_t) * parts) != cudaSuccess) return PN_ERR_OUT_OF_MEMORY;
     s->part_cap = parts;
   }
-  k_s64_reduce<<<(unsigned)parts, S64_THREADS, 0, st>>>(in, n, s->d_part);
-  k_s64_parts<<<1, S64_THREADS, 0, st>>>(s->d_part, parts);
-  k_s64_apply<<<(unsigned)parts, S64_THREADS, 0, st>>>(in, n, s->d_part, out);
+  k_s64_reduce<<<(unsigned)parts, S64_THREADS, 0, st>>>(in, n, s->d_part); count_launch();
+  k_s64_parts<<<1, S64_THREADS, 0, st>>>(s->d_part, parts); count_launch();
+  k_s64_apply<<<(unsigned)parts, S64_THREADS, 0, st>>>(in, n, s->d_part, out); count_launch();
   return cuda_status(cudaGetLastError());
 }
 
@@ -586,10 +586,10 @@ int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_
 // the scratch, then copy the sorted row back.
 __global__ void __launch_bounds__(256)
 k_sort_rows(const int64_t* __restrict__ offsets, int64_t n_rows, int32_t* __restrict__ vals,
-            int32_t* __restrict__ tmp) {
+            int32_t* __restrict__ tmp, int64_t capacity) {
   const int64_t row = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (row >= n_rows) return;
+  if (row >= n_rows || offsets[n_rows] > capacity) return;  // lists not written
   const int64_t s = offsets[row], e = offsets[row + 1];
   for (int64_t a = s + lane; a < e; a += 32) {
     const int32_t v = vals[a];
@@ -601,6 +601,7 @@ k_sort_rows(const int64_t* __restrict__ offsets, int64_t n_rows, int32_t* __rest
   for (int64_t a = s + lane; a < e; a += 32) vals[a] = tmp[a];
 }
 
+// `total` is the capacity of `vals`: rows are only sorted when they were written.
 int sort_rows(pn_search* s, const int64_t* offsets, int64_t n_rows, int32_t* vals,
               int64_t total, cudaStream_t st) {
   if (n_rows == 0 || total == 0) return PN_OK;
@@ -610,7 +611,8 @@ int sort_rows(pn_search* s, const int64_t* offsets, int64_t n_rows, int32_t* val
     if (cudaMalloc(&s->d_sort_tmp, sizeof(int32_t) * total) != cudaSuccess) return PN_ERR_OUT_OF_MEMORY;
     s->sort_tmp_cap = total;
   }
-  k_sort_rows<<<div_up(n_rows * 32, 256), 256, 0, st>>>(offsets, n_rows, vals, s->d_sort_tmp);
+  k_sort_rows<<<div_up(n_rows * 32, 256), 256, 0, st>>>(offsets, n_rows, vals, s->d_sort_tmp,
+                                                        total); count_launch();
   return cuda_status(cudaGetLastError());
 }
 
@@ -660,14 +662,15 @@ template <typename T, int D>
 static int export_cells_t(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st) {
   const int b = div_up(s->n_total, 256);
   const int32_t* ovf = s->ovf_active ? s->d_ovf_start : nullptr;
-  k_export_counts<T, D><<<b, 256, 0, st>>>(s->d_start, ovf, s->d_perm, s->n_total, counts);
+  k_export_counts<T, D><<<b, 256, 0, st>>>(s->d_start, ovf, s->d_perm, s->n_total, counts); count_launch();
   int64_t* out_start = nullptr;
   if (cudaMallocAsync(&out_start, sizeof(int64_t) * (s->n_total + 1), st) != cudaSuccess)
     return PN_ERR_OUT_OF_MEMORY;
   int rc = scan64(s, counts, s->n_total, out_start, st);
-  if (rc == PN_OK && points)
+  if (rc == PN_OK && points) {
     k_export_points<T, D><<<b, 256, 0, st>>>(s->d_start, s->d_perm, ovf, s->d_perm,
-                                              out_start, s->n_total, points);
+                                              out_start, s->n_total, points); count_launch();
+  }
   cudaFreeAsync(out_start, st);
   return rc != PN_OK ? rc : cuda_status(cudaGetLastError());
 }

@@ -81,6 +81,9 @@ struct pn_search {
 
 namespace pn {
 
+// Host-side count of kernel launches made by the library (pn_launch_count()).
+void count_launch();
+
 int ensure_capacity(pn_search* s, int64_t n);
 int ensure_qcount(pn_search* s, int64_t n);
 int cuda_status(cudaError_t e);

@@ -50,10 +50,11 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
   const int key = s->ndims * 2 + (s->periodic ? 1 : 0);
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
-    if (sorted)                                                                         \
-      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
-    else                                                                                \
-      k_trav_list<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);          \
+    if (sorted) {                                                                       \
+      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p); count_launch();        \
+    } else {                                                                            \
+      k_trav_list<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p); count_launch();          \
+    }                                                                                   \
     break;
   switch (key) {
     PN_TRAV_CASE(2, 1, false)
@@ -146,7 +147,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       if (rc != PN_OK) return rc;
       rc = scan64(s, counts, n_q, u->offsets, st);
       if (rc != PN_OK) return rc;
-      k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err);
+      k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err); count_launch();
       if (u->neighbors == nullptr || u->capacity <= 0) return cuda_status(cudaGetLastError());
       EmitParams<T> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
       rc = launch_trav<T, FEmit>(s, a, pe, sorted, n_launch, st);
@@ -176,7 +177,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       DensityParams<T> p{sph_const<T>(s, u), static_cast<T*>(u->density),
                          static_cast<T*>(u->pressure), static_cast<const T*>(u->velocity),
                          nullptr, nullptr};
-      if (step) {
+      if (sorted && u->velocity != nullptr) {
         p.pa = static_cast<T*>(s->d_pa);
         p.pb = static_cast<T*>(s->d_pb);
       }
@@ -197,11 +198,11 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       const T* dn = static_cast<const T*>(u->density);
       const T* pr = static_cast<const T*>(u->pressure);
       const T* ve = static_cast<const T*>(u->velocity);
-      if (b > 0) {
+      if (b > 0 && !u->reuse_state) {
         switch (s->ndims) {
-          case 1: k_gather_state<T, 1><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); break;
-          case 2: k_gather_state<T, 2><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); break;
-          default: k_gather_state<T, 3><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); break;
+          case 1: k_gather_state<T, 1><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
+          case 2: k_gather_state<T, 2><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
+          default: k_gather_state<T, 3><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
         }
       }
       ForceParams<T> pf{sph_const<T>(s, u), pa, pb, static_cast<T*>(u->accel)};

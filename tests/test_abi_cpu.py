@@ -25,7 +25,8 @@ def L(pkg):
 def declared_functions():
     src = open(HEADER).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"^\s*(?:int|const char\*)\s+(pn_\w+)\s*\(", src, flags=re.M)))
+    return sorted(set(re.findall(r"^\s*(?:int|const char\*|unsigned long long)\s+(pn_\w+)\s*\(",
+                                 src, flags=re.M)))
 
 
 def test_library_exports_every_declared_symbol(L):
