@@ -147,8 +147,10 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       if (rc != PN_OK) return rc;
       rc = scan64(s, counts, n_q, u->offsets, st);
       if (rc != PN_OK) return rc;
-      k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err); count_launch();
+      // Without an output buffer the call only counts (the caller sizes the buffer from
+      // offsets[n_q]); with one, rows are written only if they all fit.
       if (u->neighbors == nullptr || u->capacity <= 0) return cuda_status(cudaGetLastError());
+      k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err); count_launch();
       EmitParams<T> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
       rc = launch_trav<T, FEmit>(s, a, pe, sorted, n_launch, st);
       if (rc != PN_OK) return rc;
