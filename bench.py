@@ -57,6 +57,10 @@ def parse():
                     help="query points in the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="wcsph", choices=["wcsph", "nbody2d", "count"],
+                    help="wcsph: the 3D WCSPH step (headline); nbody2d: 2D periodic "
+                         "truncated potential on a 4096^2 lattice; count: neighbour counts "
+                         "of the 50^3 Float64 lattice")
     return ap.parse_args()
 
 
@@ -399,6 +403,79 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def run_gpu_sweep(args, rank, world, local):
+    """Secondary workloads: one traversal per step (no update), device-timed."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    P = __graft_entry__.package()
+    W = P.workloads
+    torch.cuda.set_device(local)
+    if args.workload == "nbody2d":
+        side = 4096 if args.n_side == 200 else args.n_side
+        x, m = W.periodic_nbody_cloud(side, seed=1, dtype=np.float32)
+        n = len(x)
+        box = P.PeriodicBox(min_corner=np.zeros(2, np.float32),
+                            max_corner=np.full(2, float(side), np.float32))
+        cl = P.FullGridCellList(min_corner=box.min_corner, max_corner=box.max_corner,
+                                search_radius=np.float32(2.5), max_points_per_cell=0)
+        nhs = P.GridNeighborhoodSearch(2, search_radius=np.float32(2.5), n_points=n,
+                                       periodic_box=box, cell_list=cl)
+        xd = torch.as_tensor(x, device="cuda").T
+        md = torch.as_tensor(m, device="cuda")
+        e = torch.zeros(n, device="cuda")
+        f = P.TruncatedPotential(md, 2.5, e)
+        desc = (f"2D periodic truncated potential, {side}^2 = {n:,} points, box [0,{side})^2, "
+                "U[-0.3,0.3] noise, r=2.5, FP32")
+        metric = "n-body pair-evals/s (2D periodic, FP32, r=2.5)"
+        dt = "f32"
+    else:
+        x = W.perturbed_lattice((50, 50, 50), 0.25, seed=1, dtype=np.float64)
+        n = len(x)
+        cl = P.FullGridCellList(min_corner=np.full(3, -1.0), max_corner=np.full(3, 51.0),
+                                search_radius=3.0, max_points_per_cell=0)
+        nhs = P.GridNeighborhoodSearch(3, search_radius=3.0, n_points=n, cell_list=cl)
+        xd = torch.as_tensor(x, device="cuda").T
+        cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+        f = P.CountNeighbors(cnt)
+        desc = "neighbour count, 50^3 = 125,000 points, U[-0.25,0.25] noise, r=3, FP64"
+        metric = "count pair-evals/s (50^3, FP64, r=3)"
+        dt = "f64"
+    t = time.perf_counter()
+    P.initialize(nhs, xd, xd)
+    torch.cuda.synchronize()
+    cnt2 = torch.zeros(n, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt2), xd, xd, nhs)
+    pairs = int(cnt2.to(torch.int64).sum())
+    for _ in range(args.warmup):
+        P.foreach_point_neighbor(f, xd, xd, nhs, check=False)
+    torch.cuda.synchronize()
+    b0, b1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    b0.record()
+    P.initialize(nhs, xd, xd, check=False)
+    b1.record()
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = P.lib().pn_launch_count()
+    t0.record()
+    for _ in range(args.steps):
+        P.foreach_point_neighbor(f, xd, xd, nhs, check=False)
+    t1.record()
+    torch.cuda.synchronize()
+    if P.lib().pn_sync(nhs.handle) != 0:
+        raise RuntimeError("timed region reported an error")
+    sec = t0.elapsed_time(t1) / 1e3
+    out = {"metric": metric, "value": pairs * args.steps / sec, "unit": "pair-evals/s",
+           "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": dt, "data": "synthetic (seeded perturbed lattice)",
+           "config": {"workload": desc, "n_points": n, "pairs_per_sweep": pairs},
+           "build_ms": b0.elapsed_time(b1),
+           "gpu_launches": int(P.lib().pn_launch_count() - launches0),
+           "gpu": torch.cuda.get_device_name()}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -408,7 +485,10 @@ def main():
         return
     rank, world, local = dist_setup("nccl")
     try:
-        run_gpu(args, rank, world, local)
+        if args.workload == "wcsph":
+            run_gpu(args, rank, world, local)
+        else:
+            run_gpu_sweep(args, rank, world, local)
     finally:
         if world > 1:
             import torch.distributed as dist

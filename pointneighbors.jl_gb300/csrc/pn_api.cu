@@ -9,6 +9,7 @@
 //     at least 3 cells per dimension.
 // This file is compiled with -ffp-contract=off for the host compiler as well, so these T
 // expressions are rounded exactly like Julia's.
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -51,12 +52,15 @@ int ensure_capacity(pn_search* s, int64_t n) {
   };
   alloc((void**)&s->d_cell_of, i4 * cap);
   alloc((void**)&s->d_slot_of, i4 * cap);
-  alloc((void**)&s->d_tmp_perm, i4 * 2 * cap);
-  alloc((void**)&s->d_perm, i4 * 2 * cap);
-  alloc((void**)&s->d_cell_of_slot, i4 * 2 * cap);
-  alloc(&s->d_pos, tb * 4 * 2 * cap);
-  alloc(&s->d_pa, tb * 4 * 2 * cap);
-  alloc(&s->d_pb, tb * 4 * 2 * cap);
+  // Slot arrays: main and overflow slots, plus SLOT_PAD slots that a candidate scan may
+  // read past the end of a run (those reads are masked off).
+  const int64_t slots = 2 * cap + SLOT_PAD;
+  alloc((void**)&s->d_tmp_perm, i4 * slots);
+  alloc((void**)&s->d_perm, i4 * slots);
+  alloc((void**)&s->d_cell_of_slot, i4 * slots);
+  alloc(&s->d_pos, tb * 4 * slots);
+  alloc(&s->d_pa, tb * 4 * slots);
+  alloc(&s->d_pb, tb * 4 * slots);
   alloc((void**)&s->d_main_perm, i4 * cap);
   alloc((void**)&s->d_ovf_list, i4 * cap);
   alloc((void**)&s->d_ovf_cell, i4 * cap);
@@ -211,8 +215,8 @@ int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points
 int pn_destroy(pn_search* s) {
   if (!s) return PN_OK;
   free_points(s);
-  void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start, s->d_scan_state,
-                  s->d_ovf_counts, s->d_ovf_start, s->d_ovf_n, s->d_qcount,
+  void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
+                  s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
                   s->d_part,       s->d_sort_tmp};
   for (void* p : ptrs)
     if (p) cudaFree(p);

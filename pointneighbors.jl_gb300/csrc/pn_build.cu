@@ -31,7 +31,7 @@ template <typename T, int D, bool PER>
 __global__ void __launch_bounds__(BIN_THREADS)
 k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* __restrict__ idx,
       int32_t m, int32_t* __restrict__ cell_of, int32_t* __restrict__ slot_of,
-      int32_t* __restrict__ counts, int32_t* __restrict__ err) {
+      int32_t* __restrict__ counts, int32_t* __restrict__ outside, int32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
@@ -45,14 +45,18 @@ k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* _
         bool ok = true;
         int32_t lin = 0, stride = 1;
 #pragma unroll
+        bool out = false;
         for (int k = 0; k < D; ++k) {
           int32_t c;
-          ok &= cell_coord_1d(g, PER, k, y[i * D + k], c);
+          const T xk = y[i * D + k];
+          ok &= cell_coord_1d(g, PER, k, xk, c);
+          if (PER) out |= outside_box(g, k, xk);
           lin += (c - 1) * stride;
           stride *= g.n[k];
         }
         if (ok) cell = lin;
         else set_error(err, PN_ERR_OUT_OF_DOMAIN);
+        if (PER && out && *(volatile int32_t*)outside == 0) atomicExch(outside, 1);
       }
     }
     // `base` is uniform over the block, so every lane of the warp reaches this point.
@@ -231,7 +235,8 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
               const T* __restrict__ y, int32_t* __restrict__ perm, T* __restrict__ pos,
               int32_t* __restrict__ ovf_counts, int32_t* __restrict__ ovf_n,
               int32_t* __restrict__ ovf_list, int32_t* __restrict__ ovf_cell,
-              int32_t* __restrict__ ovf_slot, int32_t* __restrict__ err) {
+              int32_t* __restrict__ ovf_slot, int32_t* __restrict__ outside,
+              int32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int32_t nm = *n_main;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nm;
@@ -243,16 +248,18 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
     if (k < nm) {
       i = main_perm[k];
       T p[D];
-      bool ok = true;
+      bool ok = true, out = false;
       int32_t lin = 0, stride = 1;
 #pragma unroll
       for (int d = 0; d < D; ++d) {
         p[d] = y[(int64_t)i * D + d];
         int32_t c;
         ok &= cell_coord_1d(g, PER, d, p[d], c);
+        if (PER) out |= outside_box(g, d, p[d]);
         lin += (c - 1) * stride;
         stride *= g.n[d];
       }
+      if (PER && out && *(volatile int32_t*)outside == 0) atomicExch(outside, 1);
       if (!ok) {
         set_error(err, PN_ERR_OUT_OF_DOMAIN);
       } else if (lin == cell_of_slot[k]) {
@@ -327,7 +334,7 @@ static void launch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* idx
   const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
   k_bin<T, D, PER><<<blocks, BIN_THREADS, 0, st>>>(make_grid<T>(s), y, n_y, idx, m,
                                                    s->d_cell_of, s->d_slot_of, s->d_counts,
-                                                   s->d_err); count_launch();
+                                                   s->d_err + 1, s->d_err); count_launch();
 }
 
 template <typename T>
@@ -374,6 +381,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   int rc = ensure_capacity(s, std::max(m, n_y));
   if (rc != PN_OK) return rc;
   cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * s->n_total, st);
+  cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
   if (m > 0) dispatch_bin<T>(s, y, n_y, idx, (int32_t)m, st);
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
   if (m > 0) {
@@ -397,7 +405,7 @@ static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {
   k_mark_movers<T, D, PER><<<blocks, 256, 0, st>>>(
       make_grid<T>(s), s->d_main_perm, s->d_cell_of_slot, s->d_start + s->n_total, y,
       s->d_perm, static_cast<T*>(s->d_pos), s->d_ovf_counts, s->d_ovf_n, s->d_ovf_list,
-      s->d_ovf_cell, s->d_ovf_slot, s->d_err); count_launch();
+      s->d_ovf_cell, s->d_ovf_slot, s->d_err + 1, s->d_err); count_launch();
 }
 
 template <typename T, int D>
@@ -421,6 +429,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   }
   cudaMemsetAsync(s->d_ovf_counts, 0, sizeof(int32_t) * s->n_total, st);
   cudaMemsetAsync(s->d_ovf_n, 0, sizeof(int32_t), st);
+  cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
   const bool per = s->periodic != 0;
   switch (s->ndims * 2 + (per ? 1 : 0)) {
     case 2: launch_mark<T, 1, false>(s, y, st); break;

@@ -81,6 +81,9 @@ struct pn_search {
 
 namespace pn {
 
+// Spare slots at the end of the slot arrays (candidate scans read up to 7 past a run).
+constexpr int64_t SLOT_PAD = 64;
+
 // Host-side count of kernel launches made by the library (pn_launch_count()).
 void count_launch();
 

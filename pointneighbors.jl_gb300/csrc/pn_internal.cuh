@@ -68,6 +68,7 @@ struct GridDev {
   int32_t pad_;
   T min_pad[3];        // padded min corner (cell (1,1,1) starts here)
   T cell_size[3];
+  T box_min[3], box_max[3];  // periodic box corners
   T box_size[3];       // periodic box size
   T half_box[3];       // box_size / 2
   T r, r2;             // search radius and r*r (both in T)
@@ -117,6 +118,13 @@ __device__ __forceinline__ bool cell_coord_1d(const GridDev<T>& g, bool periodic
   return c <= g.n[k] - 1;
 }
 
+// A point outside the periodic box [min, max) (the periodic traversal then checks every
+// candidate for a periodic image; inside the box it can skip that check in the interior).
+template <typename T>
+__device__ __forceinline__ bool outside_box(const GridDev<T>& g, int k, T xk) {
+  return !(xk >= g.box_min[k] && xk < g.box_max[k]);
+}
+
 // ------------------------------------------------------------------ errors
 // Sticky per-search error word: the first error code set by any kernel wins.
 __device__ __forceinline__ void set_error(int32_t* err, int32_t code) {
@@ -150,6 +158,8 @@ inline GridDev<T> make_grid(const pn_search* s) {
     g.min_pad[k] = used ? (T)s->min_pad[k] : (T)0;
     g.cell_size[k] = used ? (T)s->cell_size[k] : (T)1;
     g.box_size[k] = used && s->periodic ? (T)s->box_size[k] : (T)0;
+    g.box_min[k] = used && s->periodic ? (T)s->cfg.periodic_min[k] : (T)0;
+    g.box_max[k] = used && s->periodic ? (T)s->cfg.periodic_max[k] : (T)0;
     g.half_box[k] = g.box_size[k] / (T)2;
   }
   g.r = (T)s->radius;

@@ -37,6 +37,8 @@ struct TravArgs {
   const int32_t* qlist;         // query point indices (list mode) or null = 0..n_q-1
   int64_t n_q;                  // list mode: number of queries
   int64_t n_x;                  // list mode: number of points in x
+  T r2_lo, r2_hi;               // r^2 (1 -+ 32 eps): the FMA distance test decides outside
+  const int32_t* outside;       // device flag: some binned point lies outside the periodic box
   int32_t* err;
 };
 
@@ -81,6 +83,27 @@ __device__ __forceinline__ void load_pos<double, 1>(const double* __restrict__ p
   v[0] = __ldg(pos + k);
 }
 
+// A candidate's coordinates and, in 3D, the stored 4th component (0 for the plain
+// coordinate copy, p/rho^2 for the WCSPH state).
+template <typename T, int D>
+__device__ __forceinline__ T load_cand(const T* __restrict__ pos, int64_t k, T* v) {
+  if constexpr (D == 3) {
+    if constexpr (sizeof(T) == 4) {
+      const float4 a = __ldg(reinterpret_cast<const float4*>(pos) + k);
+      v[0] = a.x; v[1] = a.y; v[2] = a.z;
+      return a.w;
+    } else {
+      const double2 a = __ldg(reinterpret_cast<const double2*>(pos) + 2 * k);
+      const double2 b = __ldg(reinterpret_cast<const double2*>(pos) + 2 * k + 1);
+      v[0] = a.x; v[1] = a.y; v[2] = b.x;
+      return b.y;
+    }
+  } else {
+    load_pos<T, D>(pos, k, v);
+    return (T)0;
+  }
+}
+
 // 4-component per-slot state (WCSPH): float4 / two double2.
 template <typename T>
 struct V4 { T x, y, z, w; };
@@ -102,13 +125,23 @@ __device__ __forceinline__ void store4(double* p, int64_t k, V4<double> v) {
   reinterpret_cast<double2*>(p)[2 * k + 1] = make_double2(v.z, v.w);
 }
 
-__device__ __forceinline__ float fsqrt(float a) { return sqrtf(a); }
+// Pair-function math (only the sums are compared with the FP64 oracle, within tolerance):
+// FP32 uses the approximate hardware square root and divide; FP64 stays IEEE.
+__device__ __forceinline__ float fsqrt(float a) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
 __device__ __forceinline__ double fsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
 
 // ================================================================== pair functions
-// A functor provides Params, Acc, init(acc, p, query), pair(acc, p, query, slot, pd, d2),
-// finish(acc, p, query) and fail(p, query) (a rejected query: write the empty result where
-// later passes depend on it).  `slot` indexes the cell-sorted arrays.
+// A functor provides Params, Acc, init(acc, p, query), pair(acc, p, query, slot, pd, d2,
+// aux), finish(acc, p, query), fail(p, query) (a rejected query: write the empty result
+// where later passes depend on it) and vacant(p, slot) (a slot vacated by an incremental
+// update); kCountOnly functors take count(acc, n) for n accepted neighbours at once.
+// `slot` indexes the cell-sorted arrays.
 
 template <typename T> struct CountParams { int32_t* counts; int32_t by_row; };
 template <typename T> struct IndexSumParams { int64_t* sums; const int32_t* perm; };
@@ -120,11 +153,15 @@ template <typename T> struct PotentialParams { const T* masses; const int32_t* p
 
 template <typename T, int D>
 struct FCount {
+  static constexpr bool kCountOnly = true;
+  static constexpr bool kInline = false;
   using Params = CountParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   struct Acc { int32_t n; };
   static __device__ __forceinline__ void init(Acc& a, const Params&, const Query<T, D>&) { a.n = 0; }
   static __device__ __forceinline__ void pair(Acc& a, const Params&, const Query<T, D>&, int32_t,
-                                              const T*, T) { ++a.n; }
+                                              const T*, T, T) { ++a.n; }
+  static __device__ __forceinline__ void count(Acc& a, int n) { a.n += n; }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     p.counts[p.by_row ? q.q : q.i] = a.n;
   }
@@ -135,12 +172,15 @@ struct FCount {
 
 template <typename T, int D>
 struct FIndexSum {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
   using Params = IndexSumParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   struct Acc { int64_t s; };
   static __device__ __forceinline__ void init(Acc& a, const Params&, const Query<T, D>&) { a.s = 0; }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
-                                              const T*, T) { a.s += (int64_t)__ldg(&p.perm[js]) + 1; }
+                                              const T*, T, T) { a.s += (int64_t)__ldg(&p.perm[js]) + 1; }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     p.sums[q.i] = a.s;
   }
@@ -148,7 +188,10 @@ struct FIndexSum {
 
 template <typename T, int D>
 struct FEmit {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
   using Params = EmitParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   struct Acc { int64_t o, end; };
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
@@ -159,7 +202,7 @@ struct FEmit {
   // The count pass fixed the row length; the bound check keeps a row inside its slot range
   // even if y changed in between (the reference would read a different neighbour set).
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
-                                              const T*, T) {
+                                              const T*, T, T) {
     if (a.o < a.end) p.nbrs[a.o++] = __ldg(&p.perm[js]);
   }
   static __device__ __forceinline__ void finish(Acc&, const Params&, const Query<T, D>&) {}
@@ -168,7 +211,10 @@ struct FEmit {
 // benchmarks/n_body.jl:41-56
 template <typename T, int D>
 struct FNBody {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
   using Params = NBodyParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   struct Acc { T a[D]; };
   static __device__ __forceinline__ void init(Acc& a, const Params&, const Query<T, D>&) {
@@ -176,10 +222,10 @@ struct FNBody {
     for (int k = 0; k < D; ++k) a.a[k] = (T)0;
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
-                                              const T* pd, T d2) {
+                                              const T* pd, T d2, T) {
     const T r = fsqrt(d2);
     if (r < p.sqrt_eps) return;
-    const T s = -p.G * __ldg(&p.masses[__ldg(&p.perm[js])]) / (r * r * r);
+    const T s = fdiv(-p.G * __ldg(&p.masses[__ldg(&p.perm[js])]), r * r * r);
 #pragma unroll
     for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
   }
@@ -192,7 +238,10 @@ struct FNBody {
 // e_i = sum_j m_i m_j (1/d - 1/R), 0 < d < R
 template <typename T, int D>
 struct FPotential {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
   using Params = PotentialParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   struct Acc { T e; T mi; };
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
@@ -200,10 +249,10 @@ struct FPotential {
     a.mi = p.masses[q.i];
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
-                                              const T*, T d2) {
+                                              const T*, T d2, T) {
     const T r = fsqrt(d2);
     if (r > (T)0 && r < p.cutoff)
-      a.e += __ldg(&p.masses[__ldg(&p.perm[js])]) * ((T)1 / r - p.inv_cutoff);
+      a.e += __ldg(&p.masses[__ldg(&p.perm[js])]) * (fdiv((T)1, r) - p.inv_cutoff);
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     p.energy[q.i] = a.mi * a.e;
@@ -253,19 +302,30 @@ struct ForceParams {
 
 template <typename T, int D>
 struct FDensity {
+  static constexpr bool kCountOnly = false;
+  // inline: the kernel value is cheap, so it is evaluated on the candidate already in
+  // registers instead of re-loading accepted candidates later
+  static constexpr bool kInline = true;
   using Params = DensityParams<T>;
+  // A slot vacated by an incremental update keeps NaN coordinates in the state too, so
+  // that a force sweep reading its candidates from the state never accepts it.
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) {
+    if (p.pa != nullptr) store4(p.pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
+  }
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   struct Acc { T w; };
   static __device__ __forceinline__ void init(Acc& a, const Params&, const Query<T, D>&) { a.w = (T)0; }
-  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t,
-                                              const T*, T d2) {
+  static __device__ __forceinline__ T kernel(const Params& p, T d2) {
     const T q = fsqrt(d2) * p.c.inv_h;
-    if (q < (T)2) {
-      const T t = (T)1 - (T)0.5 * q;
-      const T t2 = t * t;
-      a.w += t2 * t2 * ((T)2 * q + (T)1);
-    }
+    const T t = fmax((T)1 - (T)0.5 * q, (T)0);  // zero beyond the support 2h
+    const T t2 = t * t;
+    return t2 * t2 * ((T)2 * q + (T)1);
   }
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t,
+                                              const T*, T d2, T) {
+    a.w += kernel(p, d2);
+  }
+
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     const T rho = p.c.mass * p.c.sigma * a.w;
     const T pr = sph_pressure(p.c, rho);
@@ -289,7 +349,10 @@ struct FDensity {
 
 template <typename T, int D>
 struct FForce {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
   using Params = ForceParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   struct Acc { T a[D]; T Pi, rhoi; T vi[D]; };
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
@@ -304,26 +367,24 @@ struct FForce {
       a.vi[k] = vb[k];
     }
   }
+  // In 3D the traversal reads the candidates from the state (x, y, z, p/rho^2), and `aux`
+  // is the candidate's p/rho^2; otherwise it is loaded here.
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
-                                              const T* pd, T d2) {
+                                              const T* pd, T d2, T aux) {
     if (d2 < p.c.r_min2) return;
-    const V4<T> sa = load4(p.pa, js);
+    const T Pj = D == 3 ? aux : load4(p.pa, js).w;
     const V4<T> sb = load4(p.pb, js);
     const T vj[3] = {sb.x, sb.y, sb.z};
-    const T r = fsqrt(d2);
-    const T q = r * p.c.inv_h;
-    if (!(q < (T)2)) return;
-    const T t = (T)1 - (T)0.5 * q;
-    const T gw = p.c.dw_coef * t * t * t;  // grad W = gw * pd
+    const T q = fsqrt(d2) * p.c.inv_h;
+    const T t = fmax((T)1 - (T)0.5 * q, (T)0);  // zero beyond the support 2h
+    const T gw = p.c.dw_coef * t * t * t;       // grad W = gw * pd
     T vr = (T)0;
 #pragma unroll
     for (int k = 0; k < D; ++k) vr += (a.vi[k] - vj[k]) * pd[k];
-    T visc = (T)0;
-    if (vr < (T)0) {
-      const T mu = p.c.h * vr / (d2 + p.c.eps_h2);
-      visc = -p.c.alpha * p.c.c0 * mu / ((T)0.5 * (a.rhoi + sb.w));
-    }
-    const T s = -p.c.mass * (a.Pi + sa.w + visc) * gw;
+    // Monaghan: Pi = -alpha c0 mu / rho_mean for approaching pairs (v.x < 0), else 0
+    const T mu = fdiv(p.c.h * vr, d2 + p.c.eps_h2);
+    const T visc = vr < (T)0 ? fdiv(-p.c.alpha * p.c.c0 * mu, (T)0.5 * (a.rhoi + sb.w)) : (T)0;
+    const T s = -p.c.mass * (a.Pi + Pj + visc) * gw;
 #pragma unroll
     for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
   }
@@ -338,138 +399,332 @@ __device__ __forceinline__ int32_t pwrap(int32_t c, int32_t nc) {
   return c < 2 ? c + nc : (c > nc + 1 ? c - nc : c);
 }
 
-template <typename T, int D, bool PER, class F>
-__device__ __forceinline__ void scan_range(const TravArgs<T>& a, const typename F::Params& p,
+template <typename T, int D>
+__device__ __forceinline__ T d2_exact(const T* pd) {
+  T d2 = xmul(pd[0], pd[0]);
+#pragma unroll
+  for (int k = 1; k < D; ++k) d2 = xadd(d2, xmul(pd[k], pd[k]));
+  return d2;
+}
+
+// With FMA contraction: within 6 units in the last place of d2_exact (both are sums of
+// three non-negative products with at most three roundings each).
+template <typename T, int D>
+__device__ __forceinline__ T d2_fast(const T* pd) {
+  T d2 = pd[0] * pd[0];
+#pragma unroll
+  for (int k = 1; k < D; ++k) d2 = fma(pd[k], pd[k], d2);
+  return d2;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ bool wrap_needed(const GridDev<T>& g, const T* pd) {
+  bool w = false;
+#pragma unroll
+  for (int k = 0; k < D; ++k) w |= !(fabs(pd[k]) < g.half_box[k]);
+  return w;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void wrap(const GridDev<T>& g, T* pd) {
+#pragma unroll
+  for (int k = 0; k < D; ++k)
+    pd[k] = xsub(pd[k], xmul(g.box_size[k], xrint(xdiv(pd[k], g.box_size[k]))));
+}
+
+// The reference's pair geometry: pos_diff and d2 exactly as neighborhood_search.jl:547-555
+// and :428-436 compute them.
+template <typename T, int D, bool PER>
+__device__ __forceinline__ T pair_geom(const GridDev<T>& g, const T* xi, const T* yj, T* pd) {
+#pragma unroll
+  for (int k = 0; k < D; ++k) pd[k] = xsub(xi[k], yj[k]);
+  T d2 = d2_exact<T, D>(pd);
+  if (PER && d2 > g.r2 && wrap_needed<T, D>(g, pd)) {
+    wrap<T, D>(g, pd);
+    d2 = d2_exact<T, D>(pd);
+  }
+  return d2;
+}
+
+
+// ------------------------------------------------------------------ candidate scan
+// Candidates are classified without branches.  The exact path (classify, kExact) gives
+// `hit` when the FMA form of d2 is clearly inside r^2 and `slow` when the exact form must
+// decide (d2 in the band around r^2) or, with WRAP, when the pair may need its periodic
+// image.  The fast path (classify_superset) only tests the FMA form against the band's
+// upper edge: a superset of the neighbours whose band members the pair step re-checks
+// exactly (it recomputes the geometry anyway).
+template <typename T, int D, bool WRAP>
+__device__ __forceinline__ void classify(const TravArgs<T>& a, const T* xi, const T* yj,
+                                         uint32_t bit, uint32_t& hit, uint32_t& slow) {
+  T pd[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) pd[k] = xsub(xi[k], yj[k]);
+  const T f = d2_fast<T, D>(pd);
+  const bool near = f <= a.r2_lo;  // false for NaN (vacated slots, NaN points)
+  bool s = !near & (f <= a.r2_hi);
+  if (WRAP) s |= !near & wrap_needed<T, D>(a.g, pd);  // the exact path rejects NaN
+  hit |= near ? bit : 0u;
+  slow |= s ? bit : 0u;
+}
+
+template <typename T, int D>
+__device__ __forceinline__ void classify_superset(const TravArgs<T>& a, const T* xi, const T* yj,
+                                                  uint32_t bit, uint32_t& hit) {
+  T pd[D];
+#pragma unroll
+  for (int k = 0; k < D; ++k) pd[k] = xsub(xi[k], yj[k]);
+  hit |= d2_fast<T, D>(pd) <= a.r2_hi ? bit : 0u;  // false for NaN
+}
+
+// Apply the pair function to candidate slot js.  The geometry is recomputed with the
+// periodic image the neighbour test used; with VERIFY (a superset classification) a
+// candidate inside the band around r^2 is first decided exactly.
+template <typename T, int D, bool WRAP, bool VERIFY, class F>
+__device__ __forceinline__ void apply_pair(const TravArgs<T>& a, const typename F::Params& p,
                                            typename F::Acc& acc, const Query<T, D>& q,
-                                           int32_t beg, int32_t end) {
-  const GridDev<T>& g = a.g;
-  for (int32_t js = beg; js < end; ++js) {
-    T yj[D];
-    load_pos<T, D>(a.pos, js, yj);
-    T pd[D];
-    pd[0] = xsub(q.x[0], yj[0]);
-    T d2 = xmul(pd[0], pd[0]);
+                                           int32_t js) {
+  T yj[D], pd[D];
+  const T aux = load_cand<T, D>(a.pos, js, yj);
 #pragma unroll
-    for (int k = 1; k < D; ++k) {
-      pd[k] = xsub(q.x[k], yj[k]);
-      d2 = xadd(d2, xmul(pd[k], pd[k]));
+  for (int k = 0; k < D; ++k) pd[k] = xsub(q.x[k], yj[k]);
+  T d2 = d2_fast<T, D>(pd);
+  if (VERIFY && d2 > a.r2_lo && !(d2_exact<T, D>(pd) <= a.g.r2)) return;
+  if (WRAP && d2 > a.r2_lo) {
+    const T de = d2_exact<T, D>(pd);
+    if (de > a.g.r2 && wrap_needed<T, D>(a.g, pd)) {
+      wrap<T, D>(a.g, pd);
+      d2 = d2_fast<T, D>(pd);
     }
-    if (PER && d2 > g.r2) {
-      bool wrap = false;
+  }
+  F::pair(acc, p, q, js, pd, d2, aux);
+}
+
+// Classify the candidates [base, base + n) (n <= 32; none when n <= 0) into one word of
+// bits, in groups of eight loads in flight with compile-time bit positions.  Every lane
+// runs the same code; only the number of groups differs, so lanes whose runs end at
+// different points never execute two different code paths.  The last group may read up to
+// seven slots past the run (the slot arrays carry that much padding); their bits are
+// masked off.
+template <typename T, int D, bool WRAP, bool SUPERSET>
+__device__ __forceinline__ void classify_span(const TravArgs<T>& a, const T* xi, int32_t base,
+                                              int n, uint32_t& hit, uint32_t& slow) {
+  hit = 0u;
+  slow = 0u;
+#pragma unroll 1
+  for (int e = 0; e < n; e += 8) {
+    uint32_t gh = 0u, gs = 0u;
 #pragma unroll
-      for (int k = 0; k < D; ++k) wrap |= !(fabs(pd[k]) < g.half_box[k]);
-      if (wrap) {
-#pragma unroll
-        for (int k = 0; k < D; ++k)
-          pd[k] = xsub(pd[k], xmul(g.box_size[k], xrint(xdiv(pd[k], g.box_size[k]))));
-        d2 = xmul(pd[0], pd[0]);
-#pragma unroll
-        for (int k = 1; k < D; ++k) d2 = xadd(d2, xmul(pd[k], pd[k]));
-      }
+    for (int u = 0; u < 8; ++u) {
+      T yj[D];
+      load_cand<T, D>(a.pos, base + e + u, yj);
+      if (SUPERSET) classify_superset<T, D>(a, xi, yj, 1u << u, gh);
+      else classify<T, D, WRAP>(a, xi, yj, 1u << u, gh, gs);
     }
-    if (d2 <= g.r2) F::pair(acc, p, q, js, pd, d2);
+    const int left = n - e;
+    const uint32_t live = left >= 8 ? 0xFFu : (1u << left) - 1u;
+    hit |= (gh & live) << e;
+    slow |= (gs & live) << e;
   }
 }
 
-// The 3^d stencil around cell c (1-based coordinates), rows of three cells along x.
+// The candidates of one chunk of NW x 32 slots starting at c0: resolve the rare `slow` ones
+// exactly, then apply the pair function to every accepted one in slot order (so a lane's
+// sum runs in the reference's candidate order) with the warp's lanes converged.
+template <typename T, int D, bool PER, bool WRAP, bool SUPERSET, class F, int NW>
+__device__ __forceinline__ void chunk_done(const TravArgs<T>& a, const typename F::Params& p,
+                                           typename F::Acc& acc, const Query<T, D>& q,
+                                           int32_t c0, uint32_t* hit, uint32_t* slow) {
+  if (!SUPERSET) {
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      while (slow[w]) {
+        const int e = __ffs(slow[w]) - 1;
+        slow[w] &= slow[w] - 1;
+        T yj[D], pd[D];
+        load_cand<T, D>(a.pos, c0 + 32 * w + e, yj);
+        if (pair_geom<T, D, PER>(a.g, q.x, yj, pd) <= a.g.r2) hit[w] |= 1u << e;
+      }
+    }
+  }
+  if constexpr (F::kCountOnly) {
+    int n = 0;
+#pragma unroll
+    for (int w = 0; w < NW; ++w) n += __popc(hit[w]);
+    F::count(acc, n);
+  } else {
+#pragma unroll
+    for (int w = 0; w < NW; ++w) {
+      uint32_t h = hit[w];
+      while (h) {
+        const int e = __ffs(h) - 1;
+        h &= h - 1;
+        apply_pair<T, D, WRAP, SUPERSET, F>(a, p, acc, q, c0 + 32 * w + e);
+      }
+    }
+  }
+}
+
+// Candidates [beg, end) of one stencil run for this thread's query, in chunks of up to
+// CHUNK_WORDS x 32: the tests are
+// straight-line code, and the pair function runs once per chunk over its accepted
+// candidates, so the lanes of a warp have similar amounts of pair work between the points
+// where they reconverge.
+constexpr int CHUNK_WORDS = 2;
+
+template <typename T, int D, bool PER, bool WRAP, class F>
+__device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F::Params& p,
+                                         typename F::Acc& acc, const Query<T, D>& q,
+                                         int32_t beg, int32_t end) {
+  if constexpr (F::kInline) {
+    // one candidate at a time with the exact test and the pair function applied in place
+    // on the registers just loaded (a cheap pair function needs no compaction)
+    for (int32_t js = beg; js < end; ++js) {
+      T yj[D], pd[D];
+      load_cand<T, D>(a.pos, js, yj);
+      const T d2 = WRAP ? pair_geom<T, D, true>(a.g, q.x, yj, pd)
+                        : pair_geom<T, D, false>(a.g, q.x, yj, pd);
+      if (d2 <= a.g.r2) F::pair(acc, p, q, js, pd, d2, (T)0);
+    }
+    return;
+  }
+  constexpr bool SUPERSET = !WRAP && !F::kCountOnly;
+  for (int32_t c0 = beg; c0 < end; c0 += 32 * CHUNK_WORDS) {
+    uint32_t hit[CHUNK_WORDS], slow[CHUNK_WORDS];
+#pragma unroll
+    for (int w = 0; w < CHUNK_WORDS; ++w)
+      classify_span<T, D, WRAP, SUPERSET>(a, q.x, c0 + 32 * w, min(32, end - (c0 + 32 * w)),
+                                          hit[w], slow[w]);
+    chunk_done<T, D, PER, WRAP, SUPERSET, F, CHUNK_WORDS>(a, p, acc, q, c0, hit, slow);
+  }
+}
+
 template <typename T, int D, bool PER, class F>
-__device__ __forceinline__ void visit_stencil(const TravArgs<T>& a, const typename F::Params& p,
-                                              typename F::Acc& acc, const Query<T, D>& q,
-                                              const int32_t* c) {
+__device__ __forceinline__ void scan_any(const TravArgs<T>& a, const typename F::Params& p,
+                                         typename F::Acc& acc, const Query<T, D>& q,
+                                         bool wrap, int32_t beg, int32_t end) {
+  if (PER && wrap) scan_run<T, D, PER, PER, F>(a, p, acc, q, beg, end);
+  else scan_run<T, D, PER, false, F>(a, p, acc, q, beg, end);
+}
+
+// One query per thread.  A warp holds consecutive queries (in sorted mode: consecutive
+// cell-sorted slots), so its lanes walk the same or shifted stencil rows in lockstep and
+// share most candidate loads.  Rows are visited in the reference's CartesianIndices
+// order; within a row the three cells x-1, x, x+1 are one slot run (main list, then the
+// overflow list), or three runs where a periodic box wraps.
+// With a periodic box the per-candidate image check is needed only near the box's faces:
+// when every point lies inside the box and the query's cell is in [4, n_cells - 1] in every
+// dimension, all its stencil cells are alias-free and |pos_diff| < 2 cell sizes < size / 2,
+// so the reference's correction is the identity.
+template <typename T, int D, bool PER, class F>
+__device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typename F::Params& p,
+                                               Query<T, D>& q, const int32_t* c, bool valid) {
+  typename F::Acc acc;
+  if (valid) F::init(acc, p, q);
   const GridDev<T>& g = a.g;
+  bool wrap = false;
+  if (PER) {
+    wrap = a.outside == nullptr || *a.outside != 0;
+#pragma unroll
+    for (int k = 0; k < D; ++k) wrap |= c[k] < 4 || c[k] > g.ncell[k] - 1;
+  }
   constexpr int OZ = D == 3 ? 1 : 0;
   constexpr int OY = D >= 2 ? 1 : 0;
-  const bool x_contig = !PER || (c[0] >= 3 && c[0] <= g.ncell[0]);
 #pragma unroll 1
   for (int oz = -OZ; oz <= OZ; ++oz) {
-    int32_t rowz = 0;
-    if (D == 3) {
-      const int32_t cz = PER ? pwrap(c[2] + oz, g.ncell[2]) : c[2] + oz;
-      rowz = (cz - 1) * g.n[0] * g.n[1];
-    }
 #pragma unroll 1
     for (int oy = -OY; oy <= OY; ++oy) {
-      int32_t row = rowz;
-      if (D >= 2) {
-        const int32_t cy = PER ? pwrap(c[1] + oy, g.ncell[1]) : c[1] + oy;
-        row += (cy - 1) * g.n[0];
-      }
-      if (x_contig) {
+      if (!valid) continue;
+      int32_t row = 0;
+      if (D == 3) row = ((PER ? pwrap(c[2] + oz, g.ncell[2]) : c[2] + oz) - 1) * g.n[0] * g.n[1];
+      if (D >= 2) row += ((PER ? pwrap(c[1] + oy, g.ncell[1]) : c[1] + oy) - 1) * g.n[0];
+      if (!PER || (c[0] >= 3 && c[0] <= g.ncell[0])) {
         const int32_t l0 = row + c[0] - 2;
-        scan_range<T, D, PER, F>(a, p, acc, q, __ldg(&a.start[l0]), __ldg(&a.start[l0 + 3]));
+        scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.start[l0]), __ldg(&a.start[l0 + 3]));
         if (a.ovf_start)
-          scan_range<T, D, PER, F>(a, p, acc, q, __ldg(&a.ovf_start[l0]), __ldg(&a.ovf_start[l0 + 3]));
+          scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.ovf_start[l0]),
+                                 __ldg(&a.ovf_start[l0 + 3]));
       } else {
 #pragma unroll 1
         for (int ox = -1; ox <= 1; ++ox) {
           const int32_t l = row + pwrap(c[0] + ox, g.ncell[0]) - 1;
-          scan_range<T, D, PER, F>(a, p, acc, q, __ldg(&a.start[l]), __ldg(&a.start[l + 1]));
+          scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.start[l]), __ldg(&a.start[l + 1]));
           if (a.ovf_start)
-            scan_range<T, D, PER, F>(a, p, acc, q, __ldg(&a.ovf_start[l]), __ldg(&a.ovf_start[l + 1]));
+            scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.ovf_start[l]),
+                                   __ldg(&a.ovf_start[l + 1]));
         }
       }
     }
   }
+  if (valid) F::finish(acc, p, q);
 }
 
 // Sorted mode: queries are the cell-sorted slots (x is y, every point binned).  Slots
 // [0, start[n_total]) are the main structure, then the overflow slots up to
 // ovf_start[n_total]; vacated slots (perm < 0) are skipped.
 template <typename T, int D, bool PER, class F>
-__global__ void __launch_bounds__(TRAV_THREADS)
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
 k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
-  if (k >= n_slots) return;
+  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
   Query<T, D> q;
-  q.i = a.perm[k];
-  if (q.i < 0) return;
+  bool valid = k < n_slots;
+  q.i = valid ? a.perm[k] : -1;
+  if (valid && q.i < 0) F::vacant(p, (int32_t)k);
+  valid = valid && q.i >= 0;
   q.q = q.i;
   q.k = (int32_t)k;
-  load_pos<T, D>(a.pos, k, q.x);
-  const int32_t lin = a.cell_of_slot[k];
   int32_t c[3] = {1, 1, 1};
-  c[0] = lin % a.g.n[0] + 1;
-  if (D >= 2) c[1] = (lin / a.g.n[0]) % a.g.n[1] + 1;
-  if (D == 3) c[2] = lin / (a.g.n[0] * a.g.n[1]) + 1;
-  typename F::Acc acc;
-  F::init(acc, p, q);
-  visit_stencil<T, D, PER, F>(a, p, acc, q, c);
-  F::finish(acc, p, q);
+  if (valid) {
+    load_pos<T, D>(a.pos, k, q.x);
+    const int32_t lin = a.cell_of_slot[k];
+    c[0] = lin % a.g.n[0] + 1;
+    if (D >= 2) c[1] = (lin / a.g.n[0]) % a.g.n[1] + 1;
+    if (D == 3) c[2] = lin / (a.g.n[0] * a.g.n[1]) + 1;
+  } else {
+#pragma unroll
+    for (int d = 0; d < D; ++d) q.x[d] = (T)0;
+  }
+  traverse_query<T, D, PER, F>(a, p, q, c, valid);
 }
 
 // List mode: queries are x[:, qlist[q]] (or q) in the given order.  A query whose
 // neighbouring cells fall outside the grid is the reference's BoundsError.
 template <typename T, int D, bool PER, class F>
-__global__ void __launch_bounds__(TRAV_THREADS)
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
 k_trav_list(const TravArgs<T> a, const typename F::Params p) {
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= a.n_q) return;
+  if ((int64_t)blockIdx.x * blockDim.x >= a.n_q) return;  // whole block idle
   Query<T, D> q;
-  q.i = a.qlist ? a.qlist[t] : (int32_t)t;
+  bool valid = t < a.n_q;
+  q.i = valid ? (a.qlist ? a.qlist[t] : (int32_t)t) : -1;
   q.q = (int32_t)t;
   q.k = -1;
-  if (q.i < 0 || q.i >= a.n_x) {
+  int32_t c[3] = {1, 1, 1};
+  if (valid && (q.i < 0 || q.i >= a.n_x)) {
     set_error(a.err, PN_ERR_INVALID_ARG);
     F::fail(p, q);
-    return;
+    valid = false;
   }
-  bool ok = true;
-  int32_t c[3] = {1, 1, 1};
+  if (valid) {
+    bool ok = true;
 #pragma unroll
-  for (int k = 0; k < D; ++k) {
-    q.x[k] = a.x[(int64_t)q.i * D + k];
-    ok &= cell_coord_1d(a.g, PER, k, q.x[k], c[k]);
+    for (int k = 0; k < D; ++k) {
+      q.x[k] = a.x[(int64_t)q.i * D + k];
+      ok &= cell_coord_1d(a.g, PER, k, q.x[k], c[k]);
+    }
+    if (!ok) {
+      set_error(a.err, PN_ERR_BOUNDS);
+      F::fail(p, q);
+      valid = false;
+    }
   }
-  if (!ok) {
-    set_error(a.err, PN_ERR_BOUNDS);
-    F::fail(p, q);
-    return;
+  if (!valid) {
+#pragma unroll
+    for (int d = 0; d < D; ++d) q.x[d] = (T)0;
   }
-  typename F::Acc acc;
-  F::init(acc, p, q);
-  visit_stencil<T, D, PER, F>(a, p, acc, q, c);
-  F::finish(acc, p, q);
+  traverse_query<T, D, PER, F>(a, p, q, c, valid);
 }
 
 }  // namespace pn

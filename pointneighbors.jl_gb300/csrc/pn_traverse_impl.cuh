@@ -25,7 +25,10 @@ k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int3
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_slots_max || k >= *n_slots) return;
   const int32_t i = perm[k];
-  if (i < 0) return;
+  if (i < 0) {  // vacated by an incremental update: never a neighbour
+    store4(pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
+    return;
+  }
   T x[D];
   load_pos<T, D>(pos, k, x);
   const T rho = density[i];
@@ -51,9 +54,11 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
     if (sorted) {                                                                       \
-      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p); count_launch();        \
+      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
+      count_launch();                                                                   \
     } else {                                                                            \
-      k_trav_list<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p); count_launch();          \
+      k_trav_list<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);          \
+      count_launch();                                                                   \
     }                                                                                   \
     break;
   switch (key) {
@@ -118,6 +123,15 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
   a.n_q = n_q;
   a.n_x = n_x;
   a.err = s->d_err;
+  a.outside = s->d_err + 1;
+  {
+    // Band around r^2 outside which the FMA distance test is decisive: 32 units in the
+    // last place on each side (the two forms differ by at most 6).
+    const double u = std::numeric_limits<T>::epsilon() / 2;
+    const double r2 = (double)a.g.r2;
+    a.r2_lo = (T)(r2 * (1.0 - 32.0 * u));
+    a.r2_hi = (T)(r2 * (1.0 + 32.0 * u));
+  }
   // Sorted mode launches one thread per possible slot; the kernel reads the live count.
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   const int64_t n_launch = sorted ? n_sorted : n_q;
@@ -187,6 +201,9 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       if (rc != PN_OK || !step) return rc;
       ForceParams<T> pf{p.c, static_cast<const T*>(s->d_pa), static_cast<const T*>(s->d_pb),
                         static_cast<T*>(u->accel)};
+      // In 3D the state (x, y, z, p/rho^2) has the coordinates' layout: the force sweep
+      // reads its candidates from it and gets p/rho^2 with the same load.
+      if (s->ndims == 3) a.pos = pf.pa;
       return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
     }
     case PN_F_WCSPH_FORCE: {
@@ -208,6 +225,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         }
       }
       ForceParams<T> pf{sph_const<T>(s, u), pa, pb, static_cast<T*>(u->accel)};
+      if (s->ndims == 3) a.pos = pa;
       return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
     }
     default:

@@ -419,6 +419,16 @@ def test_incremental_update_matches_rebuild(P, O):
     assert torch.allclose(outs[0][0], outs[1][0], rtol=1e-6, atol=0)
     scale = outs[1][1].abs().max()
     assert float((outs[0][1] - outs[1][1]).abs().max() / scale) < 1e-4
+    # the standalone force call (state gathered from the arrays) after the incremental
+    # update gives the fused step's result bit for bit
+    rho_i = torch.zeros(n, device="cuda")
+    p_i = torch.zeros(n, device="cuda")
+    P.foreach_point_neighbor(P.WCSPHDensity(density=rho_i, pressure=p_i, **W.WCSPH),
+                             x1d, x1d, nhs_i)
+    acc2 = torch.zeros(3 * n, device="cuda")
+    P.foreach_point_neighbor(P.WCSPHForce(density=rho_i, pressure=p_i, velocity=vd, accel=acc2,
+                                          **W.WCSPH), x1d, x1d, nhs_i)
+    assert torch.equal(rho_i, outs[0][0]) and torch.equal(acc2, outs[0][1])
     # a second update back to the original positions empties the overflow
     P.update(nhs_i, x0d, x0d)
     P.initialize(nhs_f, x0d, x0d)
