@@ -50,7 +50,9 @@ typedef enum {
   PN_ERR_OUT_OF_MEMORY = 8,
   PN_ERR_BOUNDS = 9,         /* a query point whose neighbouring cells are outside the grid
                                 (the reference's BoundsError in points_in_cell)             */
-  PN_ERR_CAPACITY = 10       /* neighbour-list output buffer too small                      */
+  PN_ERR_CAPACITY = 10,      /* neighbour-list output buffer too small                      */
+  PN_ERR_SCRATCH_LIMIT = 11  /* problem larger than pn_count_neighbors_noalloc's fixed
+                                scratch (PN_NOALLOC_SCRATCH_BYTES)                          */
 } pn_status;
 
 typedef enum { PN_FLOAT32 = 0, PN_FLOAT64 = 1 } pn_dtype;
@@ -224,6 +226,31 @@ int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stre
  * counts int32[prod(grid_size)] per linear cell index, points int32[n_binned] with each
  * cell's points ascending. */
 int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream);
+
+/* ----------------------------------------------------------------- no-allocation entry */
+
+/* Size of the fixed device scratch that pn_count_neighbors_noalloc works in. */
+#define PN_NOALLOC_SCRATCH_BYTES (4 * 1024 * 1024)
+
+/* No counterpart in the reference: an entry point for callers that cannot allocate device
+ * memory (a host whose own memory pool owns the device, or a multi-stream time loop that
+ * cudaMalloc/cudaFree would synchronise).  It computes what pn_initialize(y = x) followed by
+ * pn_foreach_point_neighbor(PN_F_COUNT, x, x) computes -- counts[i] = number of points of x
+ * within cfg->search_radius of point i, itself included -- for the geometry `cfg`
+ * describes (FullGridCellList corners, optional periodic box, dtype, max_points_per_cell),
+ * without a pn_search handle and without allocating: it works in a file-scope device array
+ * of PN_NOALLOC_SCRATCH_BYTES that is part of the library image.
+ *  - Limit: 4 bytes per cell of the padded grid + 12 bytes per point + 20 bytes must fit
+ *    PN_NOALLOC_SCRATCH_BYTES, else PN_ERR_SCRATCH_LIMIT (nothing is launched).
+ *  - The first call on a device (the current one) looks up the scratch's address there,
+ *    which can load the library's module: make that first call before any stream capture.
+ *  - Every call shares the scratch, which keeps the last call's contents (each call clears
+ *    what must start at zero); calls that overlap on the GPU race, so serialise calls made
+ *    from several host threads or streams.
+ *  - x and counts are device pointers; the call returns after the counts are written, with
+ *    the kernel's status (PN_ERR_OUT_OF_DOMAIN, PN_ERR_CELL_FULL) as its result. */
+int pn_count_neighbors_noalloc(const pn_config* cfg, const void* x, int64_t n, int32_t* counts,
+                               pn_stream_t stream);
 
 int pn_abi_version(void);
 

@@ -23,6 +23,8 @@ PN_ERR_NOT_INITIALIZED = 7
 PN_ERR_OUT_OF_MEMORY = 8
 PN_ERR_BOUNDS = 9
 PN_ERR_CAPACITY = 10
+PN_ERR_SCRATCH_LIMIT = 11
+PN_NOALLOC_SCRATCH_BYTES = 4 * 1024 * 1024
 
 PN_FLOAT32, PN_FLOAT64 = 0, 1
 PN_PARALLEL_UPDATE, PN_PARALLEL_INCREMENTAL_UPDATE = 0, 1
@@ -108,6 +110,7 @@ _SIGNATURES = {
     "pn_compute_geometry": (C.c_int, [C.POINTER(pn_config), C.POINTER(pn_grid_info)]),
     "pn_cell_coords": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "pn_export_cells": (C.c_int, [_P, _P, _P, _P]),
+    "pn_count_neighbors_noalloc": (C.c_int, [C.POINTER(pn_config), _P, C.c_int64, _P, _P]),
 }
 
 _lib = None

@@ -325,6 +325,9 @@ const char* pn_status_string(int32_t status) {
     case PN_ERR_OUT_OF_MEMORY: return "out of device memory";
     case PN_ERR_BOUNDS: return "BoundsError: a query point's neighbouring cells are outside the grid";
     case PN_ERR_CAPACITY: return "neighbour-list buffer too small";
+    case PN_ERR_SCRATCH_LIMIT:
+      return "the problem needs more than the 4 MiB fixed scratch of the no-allocation entry "
+             "point (4 bytes per grid cell + 12 bytes per point + 20 bytes)";
     default: return "unknown status";
   }
 }
