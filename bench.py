@@ -4,7 +4,8 @@
 Workload (the default): a 200^3 = 8,000,000-point 3D lattice, spacing 1, uniform noise in
 [-0.25, 0.25], Float32, search radius 3, FullGridCellList over [-1, 201]^3, velocities
 N(0, 0.1^2).  A step is the hot path once over the whole cloud:
-  update!(positions displaced by N(0, 0.05^2))   (ParallelIncrementalUpdate)
+  update!(positions of a random walk, N(0, 0.05^2) per component per step)
+                                                 (ParallelIncrementalUpdate)
   WCSPH density sweep (Wendland C2, h = 1.5) + Tait EOS
   WCSPH force sweep (pressure + Monaghan viscosity)
 pair-evals/s = 2 sweeps x (ordered pairs with d^2 <= r^2, self included) per step / time.
@@ -174,7 +175,6 @@ def run_gpu(args, rank, world, local):
     nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
                                    update_strategy=P.ParallelIncrementalUpdate())
     x0d = torch.as_tensor(x0, device="cuda").T
-    x1d = torch.as_tensor(x1, device="cuda").T
     vd = torch.as_tensor(v, device="cuda").reshape(-1)
     rho = torch.zeros(n, dtype=tdt, device="cuda")
     prs = torch.zeros(n, dtype=tdt, device="cuda")
@@ -182,27 +182,38 @@ def run_gpu(args, rank, world, local):
     dens = P.WCSPHDensity(density=rho, pressure=prs, velocity=vd, **W.WCSPH)
     force = P.WCSPHForce(density=rho, pressure=prs, velocity=vd, accel=acc, reuse_state=True,
                          **W.WCSPH)
-    P.initialize(nhs, x0d, x0d)
-
-    def step(x):
-        P.update(nhs, x, x, check=False)
-        P.foreach_point_neighbor(dens, x, x, nhs, check=False)
-        P.foreach_point_neighbor(force, x, x, nhs, check=False)
-
-    # pairs per sweep at the step's positions (untimed)
-    P.update(nhs, x1d, x1d)
+    # positions of every step: a random walk x_{s+1} = x_s + N(0, 0.05^2) per component
+    # (x_0 = the displaced lattice), so every update! re-bins the points that really moved
+    K, Wm = args.steps, args.warmup
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    walk = [torch.as_tensor(x1, device="cuda")]
+    for _ in range(Wm + K - 1):
+        walk.append(walk[-1] + dt(0.05) * torch.randn(walk[-1].shape, generator=gen,
+                                                      device="cuda", dtype=tdt))
+    # ordered pairs (self included) at every step's positions, with a separate search
+    cl2 = P.FullGridCellList(min_corner=np.full(3, -1.0, dt), max_corner=np.full(3, n_side + 1.0, dt),
+                             search_radius=r, max_points_per_cell=0)
+    nhs_count = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl2)
     cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
-    P.foreach_point_neighbor(P.CountNeighbors(cnt), x1d, x1d, nhs)
-    pairs_per_sweep = int(cnt.to(torch.int64).sum())
-    del cnt
+    pairs = []
+    for xs in walk:
+        P.initialize(nhs_count, xs.T, xs.T)
+        P.foreach_point_neighbor(P.CountNeighbors(cnt), xs.T, xs.T, nhs_count)
+        pairs.append(int(cnt.to(torch.int64).sum()))
+    del cnt, nhs_count
+    pairs_timed = sum(pairs[Wm:])
 
-    for _ in range(args.warmup):
-        step(x1d)
+    P.initialize(nhs, x0d, x0d)
+    for s_ in range(Wm):
+        xs = walk[s_].T
+        P.update(nhs, xs, xs, check=False)
+        P.foreach_point_neighbor(dens, xs, xs, nhs, check=False)
+        P.foreach_point_neighbor(force, xs, xs, nhs, check=False)
     torch.cuda.synchronize()
     if P.lib().pn_sync(nhs.handle) != 0:
         raise RuntimeError("warm-up reported an error")
 
-    K = args.steps
     ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
     t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
@@ -213,12 +224,13 @@ def run_gpu(args, rank, world, local):
     t0.record()
     for k in range(K):
         e = ev[k]
+        xs = walk[Wm + k].T
         e[0].record()
-        P.update(nhs, x1d, x1d, check=False)
+        P.update(nhs, xs, xs, check=False)
         e[1].record()
-        P.foreach_point_neighbor(dens, x1d, x1d, nhs, check=False)
+        P.foreach_point_neighbor(dens, xs, xs, nhs, check=False)
         e[2].record()
-        P.foreach_point_neighbor(force, x1d, x1d, nhs, check=False)
+        P.foreach_point_neighbor(force, xs, xs, nhs, check=False)
         e[3].record()
     t1.record()
     torch.cuda.synchronize()
@@ -233,22 +245,24 @@ def run_gpu(args, rank, world, local):
     upd = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
     den = [ev[k][1].elapsed_time(ev[k][2]) for k in range(K)]
     frc = [ev[k][2].elapsed_time(ev[k][3]) for k in range(K)]
-    max_s, all_pairs = aggregate(dev_s, 2.0 * pairs_per_sweep * K, world,
-                                 device=torch.device("cuda"))
+    max_s, all_pairs = aggregate(dev_s, 2.0 * pairs_timed, world, device=torch.device("cuda"))
     value = all_pairs / max_s
+    pairs_per_sweep = pairs_timed / K
 
-    # ---- end to end through the C ABI with host buffers
+    # ---- end to end through the C ABI with host buffers: the same positions walked back
+    # (each step again a N(0, 0.05^2) displacement of the previous one)
     e2e = None
     if not args.no_e2e:
-        x1_h = torch.as_tensor(x1).pin_memory()
+        order = list(range(Wm + K - 1, Wm - 1, -1))
+        walk_h = [walk[i].cpu().pin_memory() for i in order]
         v_h = torch.as_tensor(v).reshape(-1).pin_memory()
         rho_h = torch.empty(n, dtype=tdt).pin_memory()
         acc_h = torch.empty(3 * n, dtype=tdt).pin_memory()
         x1dev = torch.empty((n, 3), dtype=tdt, device="cuda")
         xb = x1dev.T
 
-        def e2e_step():
-            x1dev.copy_(x1_h, non_blocking=True)
+        def e2e_step(xh):
+            x1dev.copy_(xh, non_blocking=True)
             vd.copy_(v_h, non_blocking=True)
             P.update(nhs, xb, xb, check=False)
             P.foreach_point_neighbor(dens, xb, xb, nhs, check=False)
@@ -256,18 +270,18 @@ def run_gpu(args, rank, world, local):
             rho_h.copy_(rho, non_blocking=True)
             acc_h.copy_(acc, non_blocking=True)
 
-        for _ in range(max(3, args.warmup // 2)):
-            e2e_step()
+        for _ in range(3):
+            e2e_step(walk_h[0])
         torch.cuda.synchronize()
         barrier(world)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a0.record()
-        for _ in range(K):
-            e2e_step()
+        for k in range(K):
+            e2e_step(walk_h[k])
         a1.record()
         torch.cuda.synchronize()
         barrier(world)
-        e2e_s, e2e_pairs = aggregate(a0.elapsed_time(a1) / 1e3, 2.0 * pairs_per_sweep * K, world,
+        e2e_s, e2e_pairs = aggregate(a0.elapsed_time(a1) / 1e3, 2.0 * pairs_timed, world,
                                      device=torch.device("cuda"))
         if P.lib().pn_sync(nhs.handle) != 0:
             raise RuntimeError("e2e region reported an error")
@@ -276,6 +290,8 @@ def run_gpu(args, rank, world, local):
                "d2h_bytes_per_step": 4 * n * tb, "ms_per_step": 1e3 * e2e_s / K,
                "path": "pinned host -> cudaMemcpyAsync -> pn_update + pn_foreach_point_neighbor "
                        "(density, force) -> device->host density and acceleration"}
+        del walk_h
+    del walk
 
     peak, peak_kind = hbm_peak()
     t_force = statistics.median(frc) / 1e3
@@ -297,7 +313,7 @@ def run_gpu(args, rank, world, local):
         "data": "synthetic (seeded perturbed lattice, numpy PCG64)",
         "config": {"workload": f"WCSPH step, {n_side}^3 = {n:,} points 3D lattice, spacing 1, "
                                "U[-0.25,0.25] noise, r=3, FullGridCellList [-1,201]^3, "
-                               "displacement N(0,0.05^2), ParallelIncrementalUpdate",
+                               "random walk N(0,0.05^2) per step, ParallelIncrementalUpdate",
                    "n_points": n, "search_radius": 3.0,
                    "pairs_per_sweep": pairs_per_sweep,
                    "parallelism": f"replicas x{world}",

@@ -190,6 +190,16 @@ int pn_initialize(pn_search* s, const void* y, int64_t n_y, const int32_t* eachi
 int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
               int64_t n_eachindex_y, int32_t points_moving_y, pn_stream_t stream);
 
+/* ParallelIncrementalUpdate's policy (no counterpart in the reference, whose incremental
+ * update always moves only the changed points): each pn_update counts the points outside
+ * the cell they had at the last full build and, on the device, keeps them in overflow
+ * lists when they are at most `fraction` of the points, else rebuilds the cell list
+ * (empty overflow).  Results are identical either way; the overflow lists make each
+ * traversal slower in proportion to their length, a rebuild costs about as much as the
+ * mover count.  Default 0.01; 0 rebuilds whenever a point changed cell, a value >= 1
+ * never rebuilds. */
+int pn_set_rebuild_fraction(pn_search* s, double fraction);
+
 /* ----------------------------------------------------------------- traversal */
 
 /* foreach_point_neighbor(f, x, y, nhs; points) (neighborhood_search.jl:183-234,

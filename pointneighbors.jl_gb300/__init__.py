@@ -151,7 +151,16 @@ class ParallelUpdate:
 
 
 class ParallelIncrementalUpdate:
-    """Re-bin only the points whose cell changed (nhs_grid.jl:146-156, 408-467)."""
+    """Re-bin only the points whose cell changed (nhs_grid.jl:146-156, 408-467).
+
+    `rebuild_fraction` (not in the reference): when more than this fraction of the points
+    are outside the cell they had at the last full build, update! rebuilds the cell list
+    instead of extending its overflow lists (decided on the device; same results)."""
+
+    def __init__(self, rebuild_fraction: float = 0.01):
+        if not rebuild_fraction >= 0:
+            raise ArgumentError("rebuild_fraction must be >= 0")
+        self.rebuild_fraction = float(rebuild_fraction)
 
     def __repr__(self):
         return "ParallelIncrementalUpdate()"
@@ -223,6 +232,8 @@ class GridNeighborhoodSearch:
                                     "NHS for very small problems.")
             _raise(rc, "GridNeighborhoodSearch")
         self._h = h
+        if isinstance(update_strategy, ParallelIncrementalUpdate):
+            lib().pn_set_rebuild_fraction(h, update_strategy.rebuild_fraction)
         self._cfg = cfg
 
     def __del__(self):
@@ -341,7 +352,7 @@ def copy_neighborhood_search(nhs: GridNeighborhoodSearch, search_radius, n_point
                               max_points_per_cell=cl.max_points_per_cell)
     return GridNeighborhoodSearch(nhs.ndims, search_radius=T(search_radius), n_points=n_points,
                                   periodic_box=nhs.periodic_box, cell_list=new_cl,
-                                  update_strategy=type(nhs.update_strategy)())
+                                  update_strategy=nhs.update_strategy)
 
 
 def initialize(nhs: GridNeighborhoodSearch, x, y, *, eachindex_y=None, check=True):

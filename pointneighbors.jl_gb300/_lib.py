@@ -98,6 +98,7 @@ _SIGNATURES = {
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),
     "pn_destroy": (C.c_int, [_P]),
+    "pn_set_rebuild_fraction": (C.c_int, [_P, C.c_double]),
     "pn_initialize": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P]),
     "pn_update": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, C.c_int32, _P]),
     "pn_foreach_point_neighbor": (C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.c_int64,

@@ -209,7 +209,15 @@ int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points
   pn_config c = tmpl->cfg;
   c.search_radius = search_radius;
   c.n_points = n_points;
-  return create(&c, out);
+  const int rc = create(&c, out);
+  if (rc == PN_OK) (*out)->rebuild_fraction = tmpl->rebuild_fraction;
+  return rc;
+}
+
+int pn_set_rebuild_fraction(pn_search* s, double fraction) {
+  if (!s || !(fraction >= 0.0)) return PN_ERR_INVALID_ARG;
+  s->rebuild_fraction = fraction;
+  return PN_OK;
 }
 
 int pn_destroy(pn_search* s) {
@@ -260,17 +268,11 @@ int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex
   if (eachindex_y != nullptr) return record(s, PN_ERR_INVALID_ARG, st);
   if (!s->initialized) return record(s, PN_ERR_NOT_INITIALIZED, st);
   if (n_y != s->n_y || !s->full_binned) return record(s, PN_ERR_INVALID_ARG, st);
-  // Rebuild policy: once the previous update's movers (read back asynchronously) exceed
-  // rebuild_fraction of the points, a full build resets the main structure.
-  bool rebuild = false;
+  // The choice between overflow lists and a full rebuild is made on the device, after the
+  // movers are counted (update_incremental); the host only refreshes its statistics.
   if (s->ovf_pending && cudaEventQuery(s->ev_ovf) == cudaSuccess) {
     s->n_ovf = *s->h_ovf_n;
     s->ovf_pending = false;
-  }
-  if (s->ovf_active && (double)s->n_ovf > s->rebuild_fraction * (double)s->n_binned) rebuild = true;
-  if (rebuild) {
-    s->n_ovf = 0;
-    return pn_initialize(s, y, n_y, nullptr, 0, stream);
   }
   int rc = s->dtype == PN_FLOAT64 ? update_incremental<double>(s, (const double*)y, n_y, st)
                                   : update_incremental<float>(s, (const float*)y, n_y, st);
@@ -355,7 +357,9 @@ int pn_get_grid_info(const pn_search* s, pn_grid_info* out) {
   }
   out->search_radius = s->radius;
   out->n_binned = s->n_binned;
-  out->n_overflow = s->n_ovf;
+  // the mover count of the last update, once its asynchronous read-back has landed
+  out->n_overflow = (s->ovf_pending && cudaEventQuery(s->ev_ovf) == cudaSuccess)
+                        ? (int64_t)*s->h_ovf_n : s->n_ovf;
   return PN_OK;
 }
 

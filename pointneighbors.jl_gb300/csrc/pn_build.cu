@@ -26,12 +26,19 @@ constexpr unsigned long long FLAG_AGG = 1ull << 32;
 constexpr unsigned long long FLAG_INCL = 2ull << 32;
 constexpr long long SCAN_SPIN_LIMIT = 1ll << 22;
 
+// ParallelIncrementalUpdate decides on the device, after counting the movers, between
+// keeping the main structure plus overflow lists and a full rebuild; the kernels of both
+// paths are launched and each returns at once unless the decision word selects it.
+constexpr int32_t GATE_OVERFLOW = 0, GATE_REBUILD = 1;
+
 // ---------------------------------------------------------------- 1. histogram
 template <typename T, int D, bool PER>
 __global__ void __launch_bounds__(BIN_THREADS)
 k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* __restrict__ idx,
       int32_t m, int32_t* __restrict__ cell_of, int32_t* __restrict__ slot_of,
-      int32_t* __restrict__ counts, int32_t* __restrict__ outside, int32_t* __restrict__ err) {
+      int32_t* __restrict__ counts, int32_t* __restrict__ outside, int32_t* __restrict__ err,
+      const int32_t* __restrict__ gate) {
+  if (gate && *gate != GATE_REBUILD) return;
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
@@ -80,7 +87,9 @@ k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* _
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_scan_cells(const int32_t* __restrict__ counts, int32_t n, int32_t* __restrict__ start,
              unsigned long long* __restrict__ state, int32_t n_tiles, int32_t max_ppc,
-             const int32_t* __restrict__ base_ptr, int32_t* __restrict__ err) {
+             const int32_t* __restrict__ base_ptr, int32_t* __restrict__ err,
+             const int32_t* __restrict__ gate, int32_t gate_want) {
+  if (gate && *gate != gate_want) return;  // the same word for every block
   __shared__ int s_tile, s_prefix;
   __shared__ int s_warp[SCAN_THREADS / 32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -168,7 +177,9 @@ k_scan_cells(const int32_t* __restrict__ counts, int32_t n, int32_t* __restrict_
 __global__ void __launch_bounds__(256)
 k_scatter(const int32_t* __restrict__ cell_of, const int32_t* __restrict__ slot_of,
           const int32_t* __restrict__ idx, int32_t m, const int32_t* __restrict__ start,
-          int32_t* __restrict__ tmp_perm, int32_t* __restrict__ cell_of_slot) {
+          int32_t* __restrict__ tmp_perm, int32_t* __restrict__ cell_of_slot,
+          const int32_t* __restrict__ gate) {
+  if (gate && *gate != GATE_REBUILD) return;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
   const int32_t c = cell_of[t];
@@ -209,7 +220,8 @@ template <typename T, int D>
 __global__ void __launch_bounds__(256)
 k_finalize(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
            const int32_t* __restrict__ start, int32_t n_total, const T* __restrict__ y,
-           int32_t* __restrict__ perm, T* __restrict__ pos) {
+           int32_t* __restrict__ perm, T* __restrict__ pos, const int32_t* __restrict__ gate) {
+  if (gate && *gate != GATE_REBUILD) return;
   // Only start[n_total] slots were filled: points that failed the bounds check were not
   // binned, so the slot count is read on the device.
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -303,7 +315,8 @@ __global__ void __launch_bounds__(256)
 k_scatter_movers(const int32_t* __restrict__ ovf_n, const int32_t* __restrict__ ovf_list,
                  const int32_t* __restrict__ ovf_cell, const int32_t* __restrict__ ovf_slot,
                  const int32_t* __restrict__ ovf_start, int32_t* __restrict__ tmp_perm,
-                 int32_t* __restrict__ cell_of_slot) {
+                 int32_t* __restrict__ cell_of_slot, const int32_t* __restrict__ gate) {
+  if (*gate != GATE_OVERFLOW) return;
   const int32_t n = *ovf_n;
   for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < n;
        m += (int64_t)gridDim.x * blockDim.x) {
@@ -320,58 +333,96 @@ __global__ void __launch_bounds__(256)
 k_finalize_movers(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
                   const int32_t* __restrict__ ovf_start, const int32_t* __restrict__ n_main,
                   int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
-                  T* __restrict__ pos) {
+                  T* __restrict__ pos, const int32_t* __restrict__ gate) {
+  if (*gate != GATE_OVERFLOW) return;
   const int32_t k0 = *n_main, k1 = ovf_start[n_total];
   for (int64_t k = k0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < k1;
        k += (int64_t)gridDim.x * blockDim.x)
     finalize_slot<T, D>(tmp_perm, cell_of_slot, ovf_start, k, y, perm, pos);
 }
 
+// The decision: rebuild when the points outside their main cell exceed `fraction` of the
+// binned points (the traversal cost of the overflow lists grows with them, while a full
+// rebuild costs about as much as marking the movers).
+__global__ void k_decide_update(const int32_t* __restrict__ ovf_n,
+                                const int32_t* __restrict__ n_main, double fraction,
+                                int32_t* __restrict__ gate) {
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+    *gate = (double)*ovf_n > fraction * (double)*n_main ? GATE_REBUILD : GATE_OVERFLOW;
+}
+
+__global__ void __launch_bounds__(256)
+k_zero_if_rebuild(int32_t* __restrict__ a, int32_t n, const int32_t* __restrict__ gate) {
+  if (*gate != GATE_REBUILD) return;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    a[c] = 0;
+}
+
+// After a rebuild the new structure is the main one: empty overflow lists, main_perm = perm.
+__global__ void __launch_bounds__(256)
+k_reset_overflow(const int32_t* __restrict__ start, int32_t n_total,
+                 const int32_t* __restrict__ perm, int32_t* __restrict__ main_perm,
+                 int32_t* __restrict__ ovf_start, int32_t* __restrict__ ovf_n,
+                 const int32_t* __restrict__ gate) {
+  if (*gate != GATE_REBUILD) return;
+  const int32_t nm = start[n_total];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c <= n_total; c += stride)
+    ovf_start[c] = nm;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nm; k += stride)
+    main_perm[k] = perm[k];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *ovf_n = 0;
+}
+
 // ---------------------------------------------------------------- host side
 template <typename T, int D, bool PER>
 static void launch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int32_t m,
-                       cudaStream_t st) {
+                       cudaStream_t st, const int32_t* gate) {
   const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
   k_bin<T, D, PER><<<blocks, BIN_THREADS, 0, st>>>(make_grid<T>(s), y, n_y, idx, m,
                                                    s->d_cell_of, s->d_slot_of, s->d_counts,
-                                                   s->d_err + 1, s->d_err); count_launch();
+                                                   s->d_err + 1, s->d_err, gate); count_launch();
 }
 
 template <typename T>
 static void dispatch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* idx,
-                         int32_t m, cudaStream_t st) {
+                         int32_t m, cudaStream_t st, const int32_t* gate = nullptr) {
   const bool per = s->periodic != 0;
   switch (s->ndims * 2 + (per ? 1 : 0)) {
-    case 2: launch_bin<T, 1, false>(s, y, n_y, idx, m, st); break;
-    case 3: launch_bin<T, 1, true>(s, y, n_y, idx, m, st); break;
-    case 4: launch_bin<T, 2, false>(s, y, n_y, idx, m, st); break;
-    case 5: launch_bin<T, 2, true>(s, y, n_y, idx, m, st); break;
-    case 6: launch_bin<T, 3, false>(s, y, n_y, idx, m, st); break;
-    default: launch_bin<T, 3, true>(s, y, n_y, idx, m, st); break;
+    case 2: launch_bin<T, 1, false>(s, y, n_y, idx, m, st, gate); break;
+    case 3: launch_bin<T, 1, true>(s, y, n_y, idx, m, st, gate); break;
+    case 4: launch_bin<T, 2, false>(s, y, n_y, idx, m, st, gate); break;
+    case 5: launch_bin<T, 2, true>(s, y, n_y, idx, m, st, gate); break;
+    case 6: launch_bin<T, 3, false>(s, y, n_y, idx, m, st, gate); break;
+    default: launch_bin<T, 3, true>(s, y, n_y, idx, m, st, gate); break;
   }
 }
 
 template <typename T>
-static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st) {
+static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st,
+                            const int32_t* gate = nullptr) {
   const int blocks = div_up(m, 256);
   if (blocks == 0) return;
   T* pos = static_cast<T*>(s->d_pos);
   const int32_t nt = s->n_total;
   switch (s->ndims) {
-    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); count_launch(); break;
-    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); count_launch(); break;
-    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos); count_launch(); break;
+    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate); count_launch(); break;
+    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate); count_launch(); break;
+    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate); count_launch(); break;
   }
 }
 
 // Exclusive scan of the cell histogram into s->d_start (one launch).
 // start[c] = *base_ptr + sum(counts[0..c)) when base_ptr is given.
 static void scan_cells(pn_search* s, const int32_t* counts, int32_t* start, cudaStream_t st,
-                       const int32_t* base_ptr = nullptr, int32_t max_ppc = 0) {
+                       const int32_t* base_ptr = nullptr, int32_t max_ppc = 0,
+                       const int32_t* gate = nullptr, int32_t gate_want = 0) {
   cudaMemsetAsync(s->d_scan_state, 0, sizeof(unsigned long long) * (s->scan_tiles + 1), st);
   k_scan_cells<<<s->scan_tiles, SCAN_THREADS, 0, st>>>(counts, s->n_total, start,
                                                        s->d_scan_state, s->scan_tiles,
-                                                       max_ppc, base_ptr, s->d_err); count_launch();
+                                                       max_ppc, base_ptr, s->d_err, gate,
+                                                       gate_want); count_launch();
 }
 
 template <typename T>
@@ -386,7 +437,8 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
   if (m > 0) {
     k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
-                                              s->d_start, s->d_tmp_perm, s->d_cell_of_slot); count_launch();
+                                              s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
+                                              nullptr); count_launch();
     // Points rejected by the bounds check are not binned; every kernel that walks the
     // slots bounds itself by start[n_total], read on the device.
     launch_finalize<T>(s, y, (int32_t)m, st);
@@ -410,13 +462,14 @@ static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {
 
 template <typename T, int D>
 static void launch_movers(pn_search* s, const T* y, cudaStream_t st) {
+  const int32_t* gate = s->d_err + 2;
   k_scatter_movers<<<152 * 4, 256, 0, st>>>(s->d_ovf_n, s->d_ovf_list, s->d_ovf_cell,
                                              s->d_ovf_slot, s->d_ovf_start, s->d_tmp_perm,
-                                             s->d_cell_of_slot); count_launch();
+                                             s->d_cell_of_slot, gate); count_launch();
   k_finalize_movers<T, D><<<152 * 4, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot,
                                                    s->d_ovf_start, s->d_start + s->n_total,
                                                    s->n_total, y, s->d_perm,
-                                                   static_cast<T*>(s->d_pos)); count_launch();
+                                                   static_cast<T*>(s->d_pos), gate); count_launch();
 }
 
 template <typename T>
@@ -439,12 +492,29 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
     case 6: launch_mark<T, 3, false>(s, y, st); break;
     default: launch_mark<T, 3, true>(s, y, st); break;
   }
-  scan_cells(s, s->d_ovf_counts, s->d_ovf_start, st, s->d_start + s->n_total);
+  int32_t* gate = s->d_err + 2;
+  k_decide_update<<<1, 32, 0, st>>>(s->d_ovf_n, s->d_start + s->n_total, s->rebuild_fraction,
+                                    gate); count_launch();
+  // overflow path
+  scan_cells(s, s->d_ovf_counts, s->d_ovf_start, st, s->d_start + s->n_total, 0, gate,
+             GATE_OVERFLOW);
   switch (s->ndims) {
     case 1: launch_movers<T, 1>(s, y, st); break;
     case 2: launch_movers<T, 2>(s, y, st); break;
     default: launch_movers<T, 3>(s, y, st); break;
   }
+  // rebuild path (every point is binned: the incremental strategy has no eachindex_y)
+  const int32_t m = (int32_t)s->n_binned;
+  k_zero_if_rebuild<<<std::max(1, std::min(div_up(s->n_total, 256), 152 * 4)), 256, 0, st>>>(
+      s->d_counts, s->n_total, gate); count_launch();
+  dispatch_bin<T>(s, y, n_y, nullptr, m, st, gate);
+  scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell, gate,
+             GATE_REBUILD);
+  k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, nullptr, m, s->d_start,
+                                            s->d_tmp_perm, s->d_cell_of_slot, gate); count_launch();
+  launch_finalize<T>(s, y, m, st, gate);
+  k_reset_overflow<<<152 * 4, 256, 0, st>>>(s->d_start, s->n_total, s->d_perm, s->d_main_perm,
+                                            s->d_ovf_start, s->d_ovf_n, gate); count_launch();
   s->ovf_active = true;
   // The mover count feeds the rebuild policy of the next update; it is read back lazily.
   cudaMemcpyAsync(s->h_ovf_n, s->d_ovf_n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);

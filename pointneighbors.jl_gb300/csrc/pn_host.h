@@ -66,7 +66,7 @@ struct pn_search {
   int64_t n_ovf = 0;                   // movers after the last update (host view)
   bool ovf_active = false;             // overflow lists in use
   bool main_perm_valid = false;
-  double rebuild_fraction = 0.25;      // full rebuild when movers exceed this fraction
+  double rebuild_fraction = 0.01;      // full rebuild when movers exceed this fraction
   int32_t updates_since_build = 0;
 
   // state

@@ -176,17 +176,19 @@ CLOUDS = [(10, 11), (100, 90), (9, 10, 7), (39, 40, 41)]
 
 @pytest.mark.parametrize("shape", CLOUDS)
 @pytest.mark.parametrize("seed", [1, 2])
-@pytest.mark.parametrize("incremental", [False, True])
+@pytest.mark.parametrize("incremental", [None, 1.0, 0.0])
 def test_grid_equals_trivial(P, O, shape, seed, incremental):
     """test/neighborhood_search.jl:186-469: neighbour lists equal brute force after
-    initialize! (seed 1) or initialize! + update! (seed 2), for both update strategies."""
+    initialize! (seed 1) or initialize! + update! (seed 2), for ParallelUpdate and for
+    ParallelIncrementalUpdate both keeping overflow lists (rebuild_fraction 1) and
+    rebuilding on the device (rebuild_fraction 0)."""
     W = P.workloads
     r = 2.5
     coords = W.reference_test_cloud(shape, r, seed=seed)
     coords_init = W.reference_test_cloud(shape, r, seed=1)
     d = len(shape)
     mn, mx = coords.min(0) - r, coords.max(0) + r
-    strat = P.ParallelIncrementalUpdate() if incremental else P.ParallelUpdate()
+    strat = P.ParallelUpdate() if incremental is None else P.ParallelIncrementalUpdate(incremental)
     nhs = make_nhs(P, d, r, mn, mx, len(coords), strategy=strat)
     xi, x = dcoords(coords_init), dcoords(coords)
     P.initialize(nhs, xi, xi)
@@ -386,15 +388,18 @@ def test_periodic_potential_2d_vs_oracle(P, O):
     assert _rel_err(e.cpu().numpy().astype(np.float64), oe, oab) < TOL_F32
 
 
-def test_incremental_update_matches_rebuild(P, O):
-    """ParallelIncrementalUpdate after an N(0, 0.05^2) displacement: the same cell list and
-    neighbour sets as a full rebuild, sums within tolerance (summation order differs)."""
+@pytest.mark.parametrize("fraction", [1.0, 0.0])
+def test_incremental_update_matches_rebuild(P, O, fraction):
+    """ParallelIncrementalUpdate after an N(0, 0.05^2) displacement, with overflow lists
+    (fraction 1) or a device-side rebuild (fraction 0): the same cell list and neighbour
+    sets as a full rebuild, sums within tolerance (summation order differs with overflow
+    lists; identical after a rebuild)."""
     W = P.workloads
     x, v, dx = W.wcsph_cloud(40, seed=7, dtype=np.float32)
     x1 = (x + dx).astype(np.float32)
     n = len(x)
     nhs_i = make_nhs(P, 3, np.float32(3.0), [-1.0] * 3, [41.0] * 3, n, dtype=np.float32,
-                     strategy=P.ParallelIncrementalUpdate())
+                     strategy=P.ParallelIncrementalUpdate(fraction))
     nhs_f = make_nhs(P, 3, np.float32(3.0), [-1.0] * 3, [41.0] * 3, n, dtype=np.float32)
     x0d, x1d = dcoords(x), dcoords(x1)
     P.initialize(nhs_i, x0d, x0d)
@@ -419,6 +424,9 @@ def test_incremental_update_matches_rebuild(P, O):
     assert torch.allclose(outs[0][0], outs[1][0], rtol=1e-6, atol=0)
     scale = outs[1][1].abs().max()
     assert float((outs[0][1] - outs[1][1]).abs().max() / scale) < 1e-4
+    if fraction == 0.0:  # rebuilt: the same layout, hence the same sums bit for bit
+        assert torch.equal(outs[0][0], outs[1][0]) and torch.equal(outs[0][1], outs[1][1])
+        assert nhs_i.grid_info()["n_overflow"] == 0
     # the standalone force call (state gathered from the arrays) after the incremental
     # update gives the fused step's result bit for bit
     rho_i = torch.zeros(n, device="cuda")
@@ -435,6 +443,40 @@ def test_incremental_update_matches_rebuild(P, O):
     ci, pi = P.export_cells(nhs_i)
     cf, pf = P.export_cells(nhs_f)
     assert np.array_equal(ci, cf) and np.array_equal(pi, pf)
+
+
+def test_incremental_random_walk(P):
+    """Ten update! calls along a random walk (N(0, 0.05^2) per step, ~8 % of the points
+    change cell per step) with rebuild_fraction 0.1: the device switches between overflow
+    lists and rebuilds; after every step the cell list and the neighbour lists equal a
+    fresh ParallelUpdate build."""
+    W = P.workloads
+    x, _, _ = W.wcsph_cloud(30, seed=5, dtype=np.float32)
+    n = len(x)
+    nhs_i = make_nhs(P, 3, np.float32(3.0), [-1.0] * 3, [31.0] * 3, n, dtype=np.float32,
+                     strategy=P.ParallelIncrementalUpdate(0.1))
+    nhs_f = make_nhs(P, 3, np.float32(3.0), [-1.0] * 3, [31.0] * 3, n, dtype=np.float32)
+    rng = np.random.default_rng(11)
+    xs = x.astype(np.float64)
+    xd = dcoords(x)
+    P.initialize(nhs_i, xd, xd)
+    seen = set()
+    for _ in range(10):
+        xs = xs + rng.normal(0, 0.05, size=xs.shape)
+        xd = dcoords(xs.astype(np.float32))
+        P.update(nhs_i, xd, xd)
+        P.initialize(nhs_f, xd, xd)
+        ci, pi = P.export_cells(nhs_i)
+        cf, pf = P.export_cells(nhs_f)
+        assert np.array_equal(ci, cf) and np.array_equal(pi, pf)
+        oi, ni = P.neighbor_lists(xd, xd, nhs_i)
+        of, nf = P.neighbor_lists(xd, xd, nhs_f)
+        assert torch.equal(oi, of) and torch.equal(ni, nf)
+        torch.cuda.synchronize()
+        n_ovf = nhs_i.grid_info()["n_overflow"]
+        assert n_ovf <= 0.1 * n
+        seen.add(n_ovf == 0)
+    assert seen == {True, False}  # both paths were taken
 
 
 def test_determinism(P):
