@@ -58,10 +58,12 @@ def parse():
                     help="query points in the CPU baseline sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="wcsph", choices=["wcsph", "nbody2d", "count"],
+    ap.add_argument("--workload", default="wcsph",
+                    choices=["wcsph", "nbody2d", "count", "adjoint"],
                     help="wcsph: the 3D WCSPH step (headline); nbody2d: 2D periodic "
                          "truncated potential on a 4096^2 lattice; count: neighbour counts "
-                         "of the 50^3 Float64 lattice")
+                         "of the 50^3 Float64 lattice; adjoint: loss + dL/dx on the "
+                         "100^3 lattice (backward/forward ratio)")
     return ap.parse_args()
 
 
@@ -492,6 +494,75 @@ def run_gpu_sweep(args, rank, world, local):
         print(json.dumps(out))
 
 
+def run_gpu_adjoint(args, rank, world, local):
+    """The adjoint workload: 100^3 = 1,000,000 points (lattice + U[-0.25, 0.25]), r = 3,
+    L = sum (rho - 1)^2 + 0.01 E; a step is the forward sweep (density, loss terms, FP64
+    loss) and the backward sweep (dL/dx, neighbour set fixed), both device-timed."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    P = __graft_entry__.package()
+    torch.cuda.set_device(local)
+    side = 100 if args.n_side == 200 else args.n_side
+    dt = np.float32 if args.dtype == "float32" else np.float64
+    tdt = torch.float32 if dt == np.float32 else torch.float64
+    x = P.workloads.perturbed_lattice((side,) * 3, 0.25, seed=1, dtype=dt)
+    n = len(x)
+    r = dt(3.0)
+    cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt), max_corner=np.full(3, side + 1.0, dt),
+                            search_radius=r, max_points_per_cell=0)
+    nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl)
+    xd = torch.as_tensor(x, device="cuda").T
+    P.initialize(nhs, xd, xd)
+    cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt), xd, xd, nhs)
+    pairs = int(cnt.to(torch.int64).sum())
+    consts = dict(mass=1.0, h=1.5, cutoff=3.0, lambda_pot=0.01)
+    rho = torch.empty(n, dtype=tdt, device="cuda")
+    terms = torch.empty(n, dtype=tdt, device="cuda")
+    loss = torch.empty(1, dtype=torch.float64, device="cuda")
+    grad = torch.empty(3 * n, dtype=tdt, device="cuda")
+    fwd = P.AdjointLossForward(density=rho, terms=terms, loss=loss, **consts)
+    bwd = P.AdjointLossBackward(grad=grad, reuse_state=True, **consts)
+    for _ in range(args.warmup):
+        P.foreach_point_neighbor(fwd, xd, xd, nhs, check=False)
+        P.foreach_point_neighbor(bwd, xd, xd, nhs, check=False)
+    torch.cuda.synchronize()
+    K = args.steps
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+    launches0 = P.lib().pn_launch_count()
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    torch.cuda.synchronize()
+    for k in range(K):
+        ev[k][0].record()
+        P.foreach_point_neighbor(fwd, xd, xd, nhs, check=False)
+        ev[k][1].record()
+        P.foreach_point_neighbor(bwd, xd, xd, nhs, check=False)
+        ev[k][2].record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop() if sampler else None
+    if P.lib().pn_sync(nhs.handle) != 0:
+        raise RuntimeError("timed region reported an error")
+    f_ms = statistics.median(ev[k][0].elapsed_time(ev[k][1]) for k in range(K))
+    b_ms = statistics.median(ev[k][1].elapsed_time(ev[k][2]) for k in range(K))
+    tot_s = sum(ev[k][0].elapsed_time(ev[k][2]) for k in range(K)) / 1e3
+    out = {"metric": f"adjoint pair-evals/s (1M pts, {'FP32' if dt == np.float32 else 'FP64'}, "
+                     "r=3, forward loss + backward dL/dx)",
+           "value": 2.0 * pairs * K / tot_s, "unit": UNIT, "n_gpus": world, "steps": K,
+           "warmup": args.warmup, "ms_per_step": 1e3 * tot_s / K, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32" if dt == np.float32 else "f64", "data": "synthetic (seeded perturbed lattice)",
+           "config": {"workload": f"adjoint loss sum (rho-1)^2 + 0.01 E, {side}^3 = {n:,} points, "
+                                  "U[-0.25,0.25] noise, r=3, Wendland h=1.5, 1/r potential cutoff 3",
+                      "pairs_per_sweep": pairs},
+           "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+           "loss": float(loss.item()),
+           "gpu_launches": int(P.lib().pn_launch_count() - launches0), "clocks": clocks,
+           "gpu": torch.cuda.get_device_name()}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -503,6 +574,8 @@ def main():
     try:
         if args.workload == "wcsph":
             run_gpu(args, rank, world, local)
+        elif args.workload == "adjoint":
+            run_gpu_adjoint(args, rank, world, local)
         else:
             run_gpu_sweep(args, rank, world, local)
     finally:

@@ -72,7 +72,9 @@ typedef enum {
   PN_F_WCSPH_DENSITY = 4,  /* pn_wcsph_params                                             */
   PN_F_WCSPH_FORCE = 5,    /* pn_wcsph_params                                             */
   PN_F_WCSPH_STEP = 6,     /* pn_wcsph_params: density + EOS, then force, one call        */
-  PN_F_INDEX_SUM = 7       /* pn_index_sum_params: mapreduce_neighbor(+) of j (1-based)   */
+  PN_F_INDEX_SUM = 7,      /* pn_index_sum_params: mapreduce_neighbor(+) of j (1-based)   */
+  PN_F_ADJOINT_FORWARD = 8,  /* pn_adjoint_params: density, loss terms, loss              */
+  PN_F_ADJOINT_BACKWARD = 9  /* pn_adjoint_params: dL/dx with the neighbour set fixed     */
 } pn_functor;
 
 /* GridNeighborhoodSearch{NDIMS}(; search_radius, n_points, periodic_box,
@@ -161,6 +163,30 @@ typedef struct {
                             them from the arrays above                                 */
   int32_t pad_;
 } pn_wcsph_params;
+
+/* Differentiable form (no counterpart in the reference, which has no adjoint): the loss
+ *   L = sum_i (rho_i - 1)^2 + lambda * E,   rho_i = sum_j m W(d_ij) (Wendland C2 as for
+ *   WCSPH, self included),   E = 1/2 sum_i sum_{j != i, 0 < d_ij < cutoff} m^2 (1/d_ij - 1/cutoff)
+ * over the neighbour pairs of the search (x == y), and its gradient
+ *   dL/dx_k = sum_j [(g_k + g_j) m W'(d_kj) + lambda phi'(d_kj)] (x_k - x_j) / d_kj,
+ *   g = 2 (rho - 1), phi(d) = m^2 (1/d - 1/cutoff),
+ * with the neighbour set held fixed (the search is piecewise constant in x).  Both sweeps
+ * re-traverse the cell list; no pair list is stored.
+ * FORWARD writes density[i], terms[i] = (rho_i - 1)^2 + lambda/2 * e_i, loss[0] = sum of
+ *   the terms in FP64 (fixed summation order), and keeps (x, g) in slot order for BACKWARD.
+ * BACKWARD writes grad[i * d + k] = scale * dL/dx_ik, scale = *grad_scale (device
+ *   pointer; NULL = 1); reuse_state = 1 uses the state of the preceding FORWARD call on
+ *   this search, 0 rebuilds it from `density`. */
+typedef struct {
+  double mass, h, cutoff, lambda_pot;  /* lambda_pot: the weight lambda of E */
+  void* density;            /* T[n]: out (FORWARD), in (BACKWARD without reuse_state)      */
+  void* terms;              /* T[n]: out (FORWARD)                                          */
+  double* loss;             /* double[1]: out (FORWARD)                                     */
+  void* grad;               /* T[n * d]: out (BACKWARD)                                     */
+  const double* grad_scale; /* double[1] or NULL (BACKWARD)                                 */
+  int32_t reuse_state;
+  int32_t pad_;
+} pn_adjoint_params;
 
 /* ----------------------------------------------------------------- lifetime */
 

@@ -36,6 +36,7 @@ __all__ = [
     "requires_update", "copy_neighborhood_search", "cell_coords", "eachneighbor",
     "neighbor_lists", "CountNeighbors", "NeighborIndexSum", "NBodyAcceleration",
     "TruncatedPotential", "WCSPHDensity", "WCSPHForce", "WCSPHStep",
+    "AdjointLossForward", "AdjointLossBackward", "adjoint_loss",
     "ArgumentError", "BoundsError", "PointNeighborsError", "UnsupportedFunctorError",
 ]
 
@@ -363,6 +364,7 @@ def initialize(nhs: GridNeighborhoodSearch, x, y, *, eachindex_y=None, check=Tru
     rc = lib().pn_initialize(nhs._h, _ptr(y), y.shape[1], _ptr(idx),
                              0 if idx is None else idx.numel(), _stream())
     nhs._y_src, nhs._y_keep = y_src, y
+    nhs._generation = getattr(nhs, "_generation", 0) + 1
     _finish(nhs, rc, check, "initialize!")
     return nhs
 
@@ -384,6 +386,7 @@ def update(nhs: GridNeighborhoodSearch, x, y, *, points_moving=(True, True), eac
     rc = lib().pn_update(nhs._h, _ptr(y), y.shape[1], _ptr(idx),
                          0 if idx is None else idx.numel(), 1, _stream())
     nhs._y_src, nhs._y_keep = y_src, y
+    nhs._generation = getattr(nhs, "_generation", 0) + 1
     _finish(nhs, rc, check, "update!")
     return nhs
 
@@ -516,12 +519,53 @@ class WCSPHStep(_WCSPH):
     functor = _lib.PN_F_WCSPH_STEP
 
 
+class _Adjoint(PairFunction):
+    def __init__(self, *, density=None, terms=None, loss=None, grad=None, grad_scale=None,
+                 mass=1.0, h=1.5, cutoff=3.0, lambda_pot=0.01, reuse_state=False):
+        self.density, self.terms, self.loss = density, terms, loss
+        self.grad, self.grad_scale = grad, grad_scale
+        self.consts = dict(mass=float(mass), h=float(h), cutoff=float(cutoff),
+                           lambda_pot=float(lambda_pot))
+        self.reuse_state = bool(reuse_state)
+
+    def params(self, nhs, x, y, n_q):
+        torch = _torch()
+        T = _tdtype(nhs)
+        n = x.shape[1]
+        p = _lib.pn_adjoint_params(reuse_state=int(self.reuse_state), **self.consts)
+        for name, size, dt in (("density", n, T), ("terms", n, T), ("grad", n * nhs.ndims, T),
+                               ("loss", 1, torch.float64), ("grad_scale", 1, torch.float64)):
+            t = getattr(self, name)
+            if t is not None:
+                _out(t, name, size, dt)
+                setattr(p, name, t.data_ptr())
+        return p
+
+
+class AdjointLossForward(_Adjoint):
+    """L = sum_i (rho_i - 1)^2 + lambda E over the search's pairs (x must be y):
+    density[i] = rho_i (Wendland C2, support 2h), terms[i] = (rho_i - 1)^2 + lambda/2 e_i
+    with e_i = sum_{j != i, 0 < d < cutoff} m^2 (1/d - 1/cutoff), loss[0] = sum of the terms
+    (FP64, fixed order).  Keeps (x, 2 (rho - 1)) in the search for AdjointLossBackward."""
+
+    functor = _lib.PN_F_ADJOINT_FORWARD
+
+
+class AdjointLossBackward(_Adjoint):
+    """grad[i * d + k] = grad_scale * dL/dx_ik with the neighbour set fixed; reuse_state
+    takes the state of the preceding AdjointLossForward call, otherwise it is rebuilt from
+    `density`."""
+
+    functor = _lib.PN_F_ADJOINT_BACKWARD
+
+
 def foreach_point_neighbor(f, x, y, nhs: GridNeighborhoodSearch, *, points=None, check=True):
     """foreach_point_neighbor(f, x, y, nhs; points) (neighborhood_search.jl:183-201)."""
     if not isinstance(f, PairFunction):
         raise UnsupportedFunctorError(
             "only the compiled pair functions (CountNeighbors, NBodyAcceleration, "
-            "TruncatedPotential, WCSPHDensity, WCSPHForce, WCSPHStep, NeighborIndexSum) run "
+            "TruncatedPotential, WCSPHDensity, WCSPHForce, WCSPHStep, NeighborIndexSum, "
+            "AdjointLossForward, AdjointLossBackward) run "
             "on the GPU; an arbitrary Python callable cannot be compiled into the kernels")
     x, y = _bound(nhs, x, "x"), _bound(nhs, y, "y")
     pts = _index_tensor(points, x.shape[1], "points")
@@ -605,3 +649,6 @@ def eachneighbor(coords, nhs: GridNeighborhoodSearch):
                       ((cc[2] - 1) * n[0] * n[1] if d > 2 else 0)
                 out.extend(pts[starts[lin]:starts[lin + 1]].tolist())
     return np.asarray(out, dtype=np.int64)
+
+
+from .adjoint import adjoint_loss  # noqa: E402  (uses the API above)

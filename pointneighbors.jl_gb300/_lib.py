@@ -37,6 +37,8 @@ PN_F_WCSPH_DENSITY = 4
 PN_F_WCSPH_FORCE = 5
 PN_F_WCSPH_STEP = 6
 PN_F_INDEX_SUM = 7
+PN_F_ADJOINT_FORWARD = 8
+PN_F_ADJOINT_BACKWARD = 9
 
 D3 = C.c_double * 3
 I3 = C.c_int64 * 3
@@ -88,6 +90,15 @@ class pn_wcsph_params(C.Structure):
         ("r_min", C.c_double), ("density", C.c_void_p), ("pressure", C.c_void_p),
         ("velocity", C.c_void_p), ("accel", C.c_void_p), ("reuse_state", C.c_int32),
         ("pad_", C.c_int32),
+    ]
+
+
+class pn_adjoint_params(C.Structure):
+    _fields_ = [
+        ("mass", C.c_double), ("h", C.c_double), ("cutoff", C.c_double),
+        ("lambda_pot", C.c_double), ("density", C.c_void_p), ("terms", C.c_void_p),
+        ("loss", C.c_void_p), ("grad", C.c_void_p), ("grad_scale", C.c_void_p),
+        ("reuse_state", C.c_int32), ("pad_", C.c_int32),
     ]
 
 

@@ -77,6 +77,16 @@ int ensure_capacity(pn_search* s, int64_t n) {
   return PN_OK;
 }
 
+int ensure_sum_part(pn_search* s) {
+  if (s->d_sum_part) return PN_OK;
+  if (cudaMalloc(&s->d_sum_part, sizeof(double) * SUM_BLOCKS) != cudaSuccess) {
+    cudaGetLastError();
+    s->d_sum_part = nullptr;
+    return PN_ERR_OUT_OF_MEMORY;
+  }
+  return PN_OK;
+}
+
 int ensure_qcount(pn_search* s, int64_t n) {
   if (n <= s->qcount_cap) return PN_OK;
   if (s->d_qcount) cudaFree(s->d_qcount);
@@ -225,7 +235,7 @@ int pn_destroy(pn_search* s) {
   free_points(s);
   void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
-                  s->d_part,       s->d_sort_tmp};
+                  s->d_part,       s->d_sort_tmp,   s->d_sum_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->h_ovf_n) cudaFreeHost(s->h_ovf_n);

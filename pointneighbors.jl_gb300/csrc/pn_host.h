@@ -51,6 +51,7 @@ struct pn_search {
   int64_t part_cap = 0;
   int32_t* d_sort_tmp = nullptr;   // row-sort scratch of the neighbour lists
   int64_t sort_tmp_cap = 0;
+  double* d_sum_part = nullptr;    // [SUM_BLOCKS] partial sums of the adjoint loss
 
   // incremental update (overflow lists relative to the main structure)
   int32_t* d_main_perm = nullptr;      // [cap] perm of the last full build
@@ -89,6 +90,8 @@ void count_launch();
 
 int ensure_capacity(pn_search* s, int64_t n);
 int ensure_qcount(pn_search* s, int64_t n);
+constexpr int SUM_BLOCKS = 256;
+int ensure_sum_part(pn_search* s);
 int cuda_status(cudaError_t e);
 
 // pn_build.cu

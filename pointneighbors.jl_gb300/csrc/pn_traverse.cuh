@@ -394,6 +394,93 @@ struct FForce {
   }
 };
 
+// ================================================================== adjoint (loss, dL/dx)
+// L = sum_i (rho_i - 1)^2 + lambda E, rho_i = sum_j m W(d_ij), E = 1/2 sum_i sum_j phi(d_ij),
+// phi(d) = m^2 (1/d - 1/R) for 0 < d < R.  The forward sweep stores g = 2 (rho - 1) beside
+// the coordinates in slot order; the backward sweep reads it for every candidate:
+// dL/dx_k = sum_j [(g_k + g_j) m W'(d) / d + lambda phi'(d) / d] (x_k - x_j).
+template <typename T>
+struct AdjointParams {
+  SphConst<T> c;         // mass, inv_h, sigma, dw_coef = -5 sigma / h^2
+  T cutoff, inv_cutoff, lambda;
+  T* density;            // forward: out, original order
+  T* terms;              // forward: out, original order
+  T* pa;                 // sorted state (x, y, z, g): forward writes, backward reads
+  T* grad;               // backward: out, original order
+  const double* scale;   // backward: upstream dL (device), or null
+};
+
+template <typename T, int D>
+struct FAdjointForward {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = true;
+  using Params = AdjointParams<T>;
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) {
+    if (p.pa != nullptr) store4(p.pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
+  }
+  static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
+  struct Acc { T w, e; };
+  static __device__ __forceinline__ void init(Acc& a, const Params&, const Query<T, D>&) {
+    a.w = (T)0;
+    a.e = (T)0;
+  }
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t,
+                                              const T*, T d2, T) {
+    const T r = fsqrt(d2);
+    const T q = r * p.c.inv_h;
+    const T t = fmax((T)1 - (T)0.5 * q, (T)0);
+    const T t2 = t * t;
+    a.w += t2 * t2 * ((T)2 * q + (T)1);
+    if (r > (T)0 && r < p.cutoff) a.e += fdiv((T)1, r) - p.inv_cutoff;
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
+    const T rho = p.c.mass * p.c.sigma * a.w;
+    const T dr = rho - (T)1;
+    p.density[q.i] = rho;
+    p.terms[q.i] = dr * dr + (T)0.5 * p.lambda * p.c.mass * p.c.mass * a.e;
+    if (p.pa != nullptr && q.k >= 0) {
+      V4<T> va{(T)0, (T)0, (T)0, (T)2 * dr};
+      T* xa = &va.x;
+#pragma unroll
+      for (int k = 0; k < D; ++k) xa[k] = q.x[k];
+      store4(p.pa, q.k, va);
+    }
+  }
+};
+
+template <typename T, int D>
+struct FAdjointBackward {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
+  using Params = AdjointParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
+  static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
+  struct Acc { T a[D]; T gk; };
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
+    a.gk = load4(p.pa, q.k).w;
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.a[k] = (T)0;
+  }
+  // In 3D the candidates come from the state itself and `aux` is their g.
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
+                                              const T* pd, T d2, T aux) {
+    if (!(d2 > (T)0)) return;  // the point itself (and coincident points): no direction
+    const T gj = D == 3 ? aux : load4(p.pa, js).w;
+    const T r = fsqrt(d2);
+    const T q = r * p.c.inv_h;
+    const T t = fmax((T)1 - (T)0.5 * q, (T)0);
+    T s = (a.gk + gj) * p.c.mass * p.c.dw_coef * (t * t * t);
+    if (r < p.cutoff) s -= fdiv(p.lambda * p.c.mass * p.c.mass, d2 * r);
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
+    const T sc = p.scale != nullptr ? (T)*p.scale : (T)1;
+#pragma unroll
+    for (int k = 0; k < D; ++k) p.grad[(int64_t)q.i * D + k] = sc * a.a[k];
+  }
+};
+
 // ================================================================== traversal kernel
 __device__ __forceinline__ int32_t pwrap(int32_t c, int32_t nc) {
   return c < 2 ? c + nc : (c > nc + 1 ? c - nc : c);

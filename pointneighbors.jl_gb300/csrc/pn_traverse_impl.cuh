@@ -45,6 +45,63 @@ k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int3
   store4(pb, k, vb);
 }
 
+// Adjoint state (x, g = 2 (rho - 1)) in slot order from a density array (original order).
+template <typename T, int D>
+__global__ void __launch_bounds__(256)
+k_gather_adjoint(const int32_t* __restrict__ perm, const T* __restrict__ pos,
+                 int32_t n_slots_max, const int32_t* __restrict__ n_slots,
+                 const T* __restrict__ density, T* __restrict__ pa) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n_slots_max || k >= *n_slots) return;
+  const int32_t i = perm[k];
+  if (i < 0) {
+    store4(pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
+    return;
+  }
+  T x[D];
+  load_pos<T, D>(pos, k, x);
+  V4<T> va{(T)0, (T)0, (T)0, (T)2 * (density[i] - (T)1)};
+  T* xa = &va.x;
+#pragma unroll
+  for (int d = 0; d < D; ++d) xa[d] = x[d];
+  store4(pa, k, va);
+}
+
+// Deterministic FP64 sum of n values: block b sums a fixed contiguous range in a fixed
+// order, then one block sums the SUM_BLOCKS partials.
+__device__ __forceinline__ double block_sum_f64(double v, double* sm) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) sm[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += sm[w];
+  return t;  // valid in thread 0
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+k_sum_partials(const T* __restrict__ v, int64_t n, double* __restrict__ part) {
+  __shared__ double sm[8];
+  const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = (int64_t)blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  double acc = 0.0;
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) acc += (double)v[i];
+  const double t = block_sum_f64(acc, sm);
+  if (threadIdx.x == 0) part[blockIdx.x] = t;
+}
+
+static __global__ void __launch_bounds__(256)
+k_sum_final(const double* __restrict__ part, int n_part, double* __restrict__ out) {
+  __shared__ double sm[8];
+  double acc = 0.0;
+  for (int i = threadIdx.x; i < n_part; i += blockDim.x) acc += part[i];
+  const double t = block_sum_f64(acc, sm);
+  if (threadIdx.x == 0) *out = t;
+}
+
 template <typename T, template <typename, int> class F>
 static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename F<T, 1>::Params& p,
                        bool sorted, int64_t n_launch, cudaStream_t st) {
@@ -227,6 +284,51 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       ForceParams<T> pf{sph_const<T>(s, u), pa, pb, static_cast<T*>(u->accel)};
       if (s->ndims == 3) a.pos = pa;
       return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
+    }
+    case PN_F_ADJOINT_FORWARD:
+    case PN_F_ADJOINT_BACKWARD: {
+      const auto* u = static_cast<const pn_adjoint_params*>(params);
+      if (!sorted || !(u->cutoff > 0.0) || !(u->h > 0.0)) return PN_ERR_INVALID_ARG;
+      pn_wcsph_params w{};
+      w.mass = u->mass;
+      w.h = u->h;
+      w.c0 = w.rho0 = w.gamma_exp = 1.0;
+      AdjointParams<T> p{};
+      p.c = sph_const<T>(s, &w);
+      p.cutoff = (T)u->cutoff;
+      p.inv_cutoff = (T)(1.0 / u->cutoff);
+      p.lambda = (T)u->lambda_pot;
+      p.pa = static_cast<T*>(s->d_pa);
+      if (functor == PN_F_ADJOINT_FORWARD) {
+        if (!u->density || !u->terms || !u->loss) return PN_ERR_INVALID_ARG;
+        int rc = ensure_sum_part(s);
+        if (rc != PN_OK) return rc;
+        p.density = static_cast<T*>(u->density);
+        p.terms = static_cast<T*>(u->terms);
+        rc = launch_trav<T, FAdjointForward>(s, a, p, sorted, n_launch, st);
+        if (rc != PN_OK) return rc;
+        k_sum_partials<T><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
+        k_sum_final<<<1, 256, 0, st>>>(s->d_sum_part, SUM_BLOCKS, u->loss); count_launch();
+        return cuda_status(cudaGetLastError());
+      }
+      if (!u->grad || (!u->reuse_state && !u->density)) return PN_ERR_INVALID_ARG;
+      if (!u->reuse_state) {
+        const int b = div_up(n_sorted, 256);
+        const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
+        const T* pos = static_cast<const T*>(s->d_pos);
+        const T* dn = static_cast<const T*>(u->density);
+        if (b > 0) {
+          switch (s->ndims) {
+            case 1: k_gather_adjoint<T, 1><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, p.pa); count_launch(); break;
+            case 2: k_gather_adjoint<T, 2><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, p.pa); count_launch(); break;
+            default: k_gather_adjoint<T, 3><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, p.pa); count_launch(); break;
+          }
+        }
+      }
+      p.grad = static_cast<T*>(u->grad);
+      p.scale = u->grad_scale;
+      if (s->ndims == 3) a.pos = p.pa;
+      return launch_trav<T, FAdjointBackward>(s, a, p, sorted, n_launch, st);
     }
     default:
       return PN_ERR_UNSUPPORTED_FUNCTOR;
