@@ -44,6 +44,10 @@ UNIT = "pair-evals/s"
 # Algorithmic bytes per point of one force sweep (FP32): read x 12, v 12, rho 4, the
 # point's index 4, write the acceleration 12.
 FORCE_BYTES_PER_POINT = {"float32": 44, "float64": 84}
+# DRAM bytes per point of one force sweep measured by ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum, 4,096,000-point capture of the same workload; the ncu summary is
+# profiles/trav_force_density_wcsph_4M.md).
+FORCE_TRAFFIC_BYTES_PER_POINT = {"float32": 49.1}
 
 
 def parse():
@@ -301,8 +305,12 @@ def run_gpu(args, rank, world, local):
     achieved = alg / t_force / 1e9
     roofline = {"bound": "hbm", "kernel": "k_trav_sorted<FForce> (force sweep)",
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
-                "frac": achieved / peak, "traffic": None,
-                "algorithmic_bytes_per_launch": alg}
+                "frac": achieved / peak,
+                "traffic": (FORCE_TRAFFIC_BYTES_PER_POINT[args.dtype] * n
+                            if args.dtype in FORCE_TRAFFIC_BYTES_PER_POINT else None),
+                "algorithmic_bytes_per_launch": alg,
+                "note": "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
+                        "93 % (density), DRAM < 2 % of peak"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
