@@ -63,11 +63,12 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",
-                    choices=["wcsph", "nbody2d", "count", "adjoint"],
+                    choices=["wcsph", "nbody2d", "count", "adjoint", "batched"],
                     help="wcsph: the 3D WCSPH step (headline); nbody2d: 2D periodic "
                          "truncated potential on a 4096^2 lattice; count: neighbour counts "
                          "of the 50^3 Float64 lattice; adjoint: loss + dL/dx on the "
-                         "100^3 lattice (backward/forward ratio)")
+                         "100^3 lattice (backward/forward ratio); batched: 512 clouds, "
+                         "one CUDA-graph step vs per-cloud launches")
     return ap.parse_args()
 
 
@@ -571,6 +572,164 @@ def run_gpu_adjoint(args, rank, world, local):
         print(json.dumps(out))
 
 
+def run_gpu_batched(args, rank, world, local):
+    """512 independent 3D FP32 clouds (N log-uniform in [1e3, 2e5], perturbed cubic
+    lattices, radius U[2, 3.5], h = r/2): a step is update! (every point displaced by
+    N(0, 0.05^2)) + WCSPH density + force of every cloud.  Timed three ways on the same GPU: one search per
+    cloud with its own launches (C ABI calls in a loop), the batch's direct calls, and the
+    batch's captured CUDA graph (including the copy of the step's positions into the graph's
+    input buffer)."""
+    import ctypes as C
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    P = __graft_entry__.package()
+    L = P._lib
+    lib = P.lib()
+    torch.cuda.set_device(local)
+    clouds = P.workloads.batched_clouds(n_clouds=512, seed=1)
+    ncl = len(clouds)
+    sizes = [len(c["x"]) for c in clouds]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    N = int(off[-1])
+    searches = []
+    for c in clouds:
+        r = np.float32(c["radius"])
+        cl = P.FullGridCellList(min_corner=np.asarray(c["min_corner"], np.float32),
+                                max_corner=np.asarray(c["max_corner"], np.float32),
+                                search_radius=r, max_points_per_cell=0)
+        searches.append(P.GridNeighborhoodSearch(3, search_radius=r, n_points=len(c["x"]),
+                                                 cell_list=cl))
+    K, Wm = args.steps, args.warmup
+    # positions: the lattices x0 and x1 = x0 + N(0, 0.05^2), alternating (every update!
+    # re-bins all points; each step moves every point by one displacement)
+    x0 = torch.as_tensor(np.concatenate([c["x"] for c in clouds]), device="cuda")
+    x1 = x0 + torch.as_tensor(np.concatenate([c["dx"] for c in clouds]), device="cuda")
+    walk = [x1 if s_ % 2 == 0 else x0 for s_ in range(Wm + K)]
+    v = torch.as_tensor(np.concatenate([c["v"] for c in clouds]), device="cuda").reshape(-1)
+    Wc = dict(P.workloads.WCSPH)
+    h = [c["radius"] / 2 for c in clouds]
+    stream = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def outputs():
+        return (torch.zeros(N, device="cuda"), torch.zeros(N, device="cuda"),
+                torch.zeros(3 * N, device="cuda"))
+
+    # ---- per-cloud searches, their own launches
+    rho1, prs1, acc1 = outputs()
+    eps = float(np.sqrt(np.finfo(np.float32).eps))
+    dens_p, forc_p = [], []
+    for k in range(ncl):
+        common = dict(mass=Wc["mass"], h=h[k], c0=Wc["c0"], rho0=Wc["rho0"],
+                      gamma_exp=Wc["gamma_exp"], alpha=Wc["alpha"], eps_visc=Wc["eps_visc"],
+                      r_min=eps * h[k], density=rho1.data_ptr() + 4 * int(off[k]),
+                      pressure=prs1.data_ptr() + 4 * int(off[k]),
+                      velocity=v.data_ptr() + 12 * int(off[k]))
+        dens_p.append(L.pn_wcsph_params(**common))
+        forc_p.append(L.pn_wcsph_params(accel=acc1.data_ptr() + 12 * int(off[k]), reuse_state=1,
+                                        **common))
+    handles = [s.handle for s in searches]
+    for k in range(ncl):
+        xk = C.c_void_p(x0.data_ptr() + 12 * int(off[k]))
+        if lib.pn_initialize(handles[k], xk, sizes[k], None, 0, stream) != 0:
+            raise RuntimeError("per-cloud initialize failed")
+
+    def per_cloud_step(xs):
+        base = xs.data_ptr()
+        for k in range(ncl):
+            xk = C.c_void_p(base + 12 * int(off[k]))
+            lib.pn_update(handles[k], xk, sizes[k], None, 0, 1, stream)
+            lib.pn_foreach_point_neighbor(handles[k], L.PN_F_WCSPH_DENSITY, xk, sizes[k], xk,
+                                          sizes[k], None, 0, C.byref(dens_p[k]), stream)
+            lib.pn_foreach_point_neighbor(handles[k], L.PN_F_WCSPH_FORCE, xk, sizes[k], xk,
+                                          sizes[k], None, 0, C.byref(forc_p[k]), stream)
+
+    def timed(fn):
+        for s_ in range(Wm):
+            fn(walk[s_])
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for s_ in range(K):
+            fn(walk[Wm + s_])
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / K
+
+    launches0 = lib.pn_launch_count()
+    per_cloud_ms = timed(per_cloud_step)
+    per_cloud_launches = (lib.pn_launch_count() - launches0) / (Wm + K)
+    for k, hd in enumerate(handles):
+        st = lib.pn_sync(hd)
+        if st != 0:
+            raise RuntimeError(f"per-cloud path reported status {st} on cloud {k}")
+
+    # ---- the batch: direct calls, then the captured graph
+    batch = P.BatchedNeighborhoodSearch(searches)
+    rho2, prs2, acc2 = outputs()
+    step = P.WCSPHStep(density=rho2, pressure=prs2, velocity=v, accel=acc2, **dict(Wc, h=h))
+    batch.initialize(x0.T)
+    dens = P.WCSPHDensity(density=rho2, pressure=prs2, velocity=v, **dict(Wc, h=h))
+    forc = P.WCSPHForce(density=rho2, pressure=prs2, velocity=v, accel=acc2, reuse_state=True,
+                        **dict(Wc, h=h))
+    t_tune = time.perf_counter()
+    sched = {"density": batch.autotune(dens, x0.T, reps=3),
+             "force": batch.autotune(forc, x0.T, reps=3)}
+    t_tune = time.perf_counter() - t_tune
+
+    def batch_step(xs):
+        batch.update(xs.T, check=False)
+        batch.foreach_point_neighbor(step, xs.T, check=False)
+
+    launches0 = lib.pn_launch_count()
+    batch_ms = timed(batch_step)
+    batch_launches = (lib.pn_launch_count() - launches0) / (Wm + K)
+    batch.sync()
+    same_direct = bool(torch.equal(rho1, rho2) and torch.equal(acc1, acc2))
+
+    xbuf = x0.clone()
+    batch.capture_step(xbuf.T, step)
+
+    def graph_step(xs):
+        xbuf.copy_(xs)
+        batch.launch_step()
+
+    sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+    launches0 = lib.pn_launch_count()
+    graph_ms = timed(graph_step)
+    clocks = sampler.stop() if sampler else None
+    batch.sync()
+    same_graph = bool(torch.equal(rho1, rho2) and torch.equal(acc1, acc2))
+
+    # ordered pairs (self included) at the timed positions, for pair-evals/s
+    cnt = torch.zeros(N, dtype=torch.int32, device="cuda")
+    pairs = 0
+    for xs in (x0, x1):
+        batch.update(xs.T)
+        batch.foreach_point_neighbor(P.CountNeighbors(cnt), xs.T)
+        pairs += int(cnt.to(torch.int64).sum()) * sum(1 for s_ in range(Wm, Wm + K)
+                                                      if walk[s_] is xs)
+    out = {"metric": "batched WCSPH step speed-up: per-cloud launches / CUDA-graph batch "
+                     "(512 clouds, same GPU)",
+           "value": per_cloud_ms / graph_ms, "unit": "x", "n_gpus": world, "steps": K,
+           "warmup": Wm, "ms_per_step": graph_ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded perturbed lattices)",
+           "config": {"workload": f"512 clouds, N log-uniform [1e3, 2e5] (side round(N^(1/3)), "
+                                  f"total {N:,} points), radius U[2, 3.5], h = r/2, box "
+                                  "[-1, side+1]^3, positions alternating x0 / x0 + N(0,0.05^2), "
+                                  "update! + WCSPH density + force",
+                      "n_points": N, "pairs_per_step": pairs // K},
+           "per_cloud_ms": per_cloud_ms, "batch_direct_ms": batch_ms, "batch_graph_ms": graph_ms,
+           "pair_evals_per_s_graph": 2.0 * pairs / K / (graph_ms / 1e3),
+           "launches_per_step": {"per_cloud": per_cloud_launches, "batch": batch_launches},
+           "schedules": sched, "autotune_s": t_tune,
+           "identical_results": {"direct": same_direct, "graph": same_graph},
+           "gpu_launches": int(batch_launches * K), "clocks": clocks,
+           "gpu": torch.cuda.get_device_name()}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -584,6 +743,8 @@ def main():
             run_gpu(args, rank, world, local)
         elif args.workload == "adjoint":
             run_gpu_adjoint(args, rank, world, local)
+        elif args.workload == "batched":
+            run_gpu_batched(args, rank, world, local)
         else:
             run_gpu_sweep(args, rank, world, local)
     finally:

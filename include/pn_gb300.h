@@ -263,6 +263,53 @@ int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stre
  * cell's points ascending. */
 int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream);
 
+/* ----------------------------------------------------------------- batched form */
+
+/* Many independent clouds, each its own GridNeighborhoodSearch (own corners, radius and
+ * size), built and traversed together: no counterpart in the reference, where each cloud
+ * is a separate search (copy_neighborhood_search, nhs_grid.jl:640-649) with its own
+ * launches.  Here the clouds' cell lists are concatenated in one set of arrays, one build
+ * bins all points, and one persistent traversal kernel takes (cloud, tile of slots) work
+ * items from a device queue, so a batch step is a handful of launches whatever the number
+ * of clouds; the whole update! + WCSPH step can be captured in a CUDA graph.
+ * Scope: 3D, Float32, non-periodic clouds; update! re-bins every point (the rebuild of
+ * ParallelUpdate).  Coordinates: one T[3, N] array (N = sum of n_points), clouds
+ * concatenated in order; outputs are indexed by the same global point index. */
+typedef struct pn_batch pn_batch;
+
+/* Tile schedule of one batched traversal: block size (64, 128 or 256 query slots per
+ * tile), tile order (0: cloud order, 1: costliest clouds first, by radius^3), and
+ * persistent (1: one wave of blocks pulling tiles from a device queue; 0: one block per
+ * tile). */
+typedef struct { int32_t block, order, persistent, pad_; } pn_batch_schedule;
+
+int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_clouds,
+                    pn_batch** out);
+int pn_batch_destroy(pn_batch* b);
+/* initialize! / update! of every cloud (a full re-bin of all points). */
+int pn_batch_initialize(pn_batch* b, const void* y, pn_stream_t stream);
+int pn_batch_update(pn_batch* b, const void* y, pn_stream_t stream);
+/* foreach_point_neighbor over every cloud (x is y): functor PN_F_COUNT (params: one
+ * pn_count_params per cloud) or PN_F_WCSPH_DENSITY / PN_F_WCSPH_FORCE (reuse_state = 1
+ * required) / PN_F_WCSPH_STEP (one pn_wcsph_params per cloud: the constants may differ per
+ * cloud, the array pointers must be the same global arrays for all clouds). */
+int pn_batch_foreach_point_neighbor(pn_batch* b, int32_t functor, const void* y,
+                                    const void* params, pn_stream_t stream);
+/* Time every schedule on this batch (reps launches each, CUDA events) and keep the
+ * fastest for `functor` (PN_F_COUNT, PN_F_WCSPH_DENSITY or PN_F_WCSPH_FORCE); results do
+ * not depend on the schedule. */
+int pn_batch_autotune(pn_batch* b, int32_t functor, const void* y, const void* params,
+                      int32_t reps, pn_stream_t stream);
+int pn_batch_get_schedule(const pn_batch* b, int32_t functor, pn_batch_schedule* out);
+int pn_batch_set_schedule(pn_batch* b, int32_t functor, const pn_batch_schedule* sched);
+/* Capture update!(y) + WCSPH density + force of every cloud into a CUDA graph (the
+ * library's own stream; no launch happens), replayed by pn_batch_launch_step on any
+ * stream.  The graph reads y and writes the arrays of `params` at the captured addresses. */
+int pn_batch_capture_step(pn_batch* b, const void* y, const pn_wcsph_params* params);
+int pn_batch_launch_step(pn_batch* b, pn_stream_t stream);
+/* Wait for the stream of the last call; return (and clear) the sticky error. */
+int pn_batch_sync(pn_batch* b);
+
 /* ----------------------------------------------------------------- no-allocation entry */
 
 /* Size of the fixed device scratch that pn_count_neighbors_noalloc works in. */

@@ -36,7 +36,7 @@ __all__ = [
     "requires_update", "copy_neighborhood_search", "cell_coords", "eachneighbor",
     "neighbor_lists", "CountNeighbors", "NeighborIndexSum", "NBodyAcceleration",
     "TruncatedPotential", "WCSPHDensity", "WCSPHForce", "WCSPHStep",
-    "AdjointLossForward", "AdjointLossBackward", "adjoint_loss",
+    "AdjointLossForward", "AdjointLossBackward", "adjoint_loss", "BatchedNeighborhoodSearch",
     "ArgumentError", "BoundsError", "PointNeighborsError", "UnsupportedFunctorError",
 ]
 
@@ -224,6 +224,7 @@ class GridNeighborhoodSearch:
         cfg.update_strategy = _STRATEGIES[type(update_strategy)]
         cfg.n_points = self.n_points
         cfg.max_points_per_cell = cell_list.max_points_per_cell
+        self._cfg = cfg
         h = C.c_void_p()
         rc = lib().pn_create(C.byref(cfg), C.byref(h))
         if rc != _lib.PN_OK:
@@ -652,3 +653,4 @@ def eachneighbor(coords, nhs: GridNeighborhoodSearch):
 
 
 from .adjoint import adjoint_loss  # noqa: E402  (uses the API above)
+from .batch import BatchedNeighborhoodSearch  # noqa: E402

@@ -102,6 +102,11 @@ class pn_adjoint_params(C.Structure):
     ]
 
 
+class pn_batch_schedule(C.Structure):
+    _fields_ = [("block", C.c_int32), ("order", C.c_int32), ("persistent", C.c_int32),
+                ("pad_", C.c_int32)]
+
+
 _P = C.c_void_p
 _SIGNATURES = {
     "pn_abi_version": (C.c_int, []),
@@ -123,6 +128,18 @@ _SIGNATURES = {
     "pn_cell_coords": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "pn_export_cells": (C.c_int, [_P, _P, _P, _P]),
     "pn_count_neighbors_noalloc": (C.c_int, [C.POINTER(pn_config), _P, C.c_int64, _P, _P]),
+    "pn_batch_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(C.c_int64), C.c_int32,
+                                  C.POINTER(_P)]),
+    "pn_batch_destroy": (C.c_int, [_P]),
+    "pn_batch_initialize": (C.c_int, [_P, _P, _P]),
+    "pn_batch_update": (C.c_int, [_P, _P, _P]),
+    "pn_batch_foreach_point_neighbor": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
+    "pn_batch_autotune": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int32, _P]),
+    "pn_batch_get_schedule": (C.c_int, [_P, C.c_int32, C.POINTER(pn_batch_schedule)]),
+    "pn_batch_set_schedule": (C.c_int, [_P, C.c_int32, C.POINTER(pn_batch_schedule)]),
+    "pn_batch_capture_step": (C.c_int, [_P, _P, _P]),
+    "pn_batch_launch_step": (C.c_int, [_P, _P]),
+    "pn_batch_sync": (C.c_int, [_P]),
 }
 
 _lib = None

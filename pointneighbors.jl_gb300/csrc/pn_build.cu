@@ -51,8 +51,8 @@ k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* _
       } else {
         bool ok = true;
         int32_t lin = 0, stride = 1;
-#pragma unroll
         bool out = false;
+#pragma unroll
         for (int k = 0; k < D; ++k) {
           int32_t c;
           const T xk = y[i * D + k];
@@ -450,6 +450,44 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   s->updates_since_build = 0;
   return cuda_status(cudaGetLastError());
 }
+
+// ---------------------------------------------------------------- pieces of the batched build
+// (pn_batch.cu bins the points of many clouds itself, then reuses these on the
+// concatenated cell and slot arrays.)
+void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long long* state,
+                 int32_t tiles, int32_t* err, cudaStream_t st) {
+  cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), st);
+  k_scan_cells<<<tiles, SCAN_THREADS, 0, st>>>(counts, n, start, state, tiles, 0, nullptr, err,
+                                               nullptr, 0); count_launch();
+}
+
+int32_t scan_tile_count(int64_t n) { return div_up(n, SCAN_TILE); }
+
+void scatter_slots(const int32_t* cell_of, const int32_t* slot_of, int32_t m,
+                   const int32_t* start, int32_t* tmp_perm, int32_t* cell_of_slot,
+                   cudaStream_t st) {
+  if (m <= 0) return;
+  k_scatter<<<div_up(m, 256), 256, 0, st>>>(cell_of, slot_of, nullptr, m, start, tmp_perm,
+                                            cell_of_slot, nullptr); count_launch();
+}
+
+template <typename T>
+void finalize_slots(int ndims, const int32_t* tmp_perm, const int32_t* cell_of_slot,
+                    const int32_t* start, int32_t n_total, const T* y, int32_t m, int32_t* perm,
+                    T* pos, cudaStream_t st) {
+  const int blocks = div_up(m, 256);
+  if (blocks == 0) return;
+  switch (ndims) {
+    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(tmp_perm, cell_of_slot, start, n_total, y, perm, pos, nullptr); break;
+    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(tmp_perm, cell_of_slot, start, n_total, y, perm, pos, nullptr); break;
+    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(tmp_perm, cell_of_slot, start, n_total, y, perm, pos, nullptr); break;
+  }
+  count_launch();
+}
+template void finalize_slots<float>(int, const int32_t*, const int32_t*, const int32_t*, int32_t,
+                                    const float*, int32_t, int32_t*, float*, cudaStream_t);
+template void finalize_slots<double>(int, const int32_t*, const int32_t*, const int32_t*, int32_t,
+                                     const double*, int32_t, int32_t*, double*, cudaStream_t);
 
 template <typename T, int D, bool PER>
 static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {

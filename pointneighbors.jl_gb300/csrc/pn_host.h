@@ -104,6 +104,17 @@ template <typename T>
 int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t st);
 int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
 int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st);
+// generic pieces of the build, reused by the batched build (pn_batch.cu)
+void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long long* state,
+                 int32_t tiles, int32_t* err, cudaStream_t st);
+int32_t scan_tile_count(int64_t n);
+void scatter_slots(const int32_t* cell_of, const int32_t* slot_of, int32_t m,
+                   const int32_t* start, int32_t* tmp_perm, int32_t* cell_of_slot,
+                   cudaStream_t st);
+template <typename T>
+void finalize_slots(int ndims, const int32_t* tmp_perm, const int32_t* cell_of_slot,
+                    const int32_t* start, int32_t n_total, const T* y, int32_t m, int32_t* perm,
+                    T* pos, cudaStream_t st);
 int sort_rows(pn_search* s, const int64_t* offsets, int64_t n_rows, int32_t* vals,
               int64_t total, cudaStream_t st);
 

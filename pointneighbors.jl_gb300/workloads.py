@@ -75,7 +75,8 @@ def batched_clouds(n_clouds=512, n_min=1000, n_max=200000, r_min=2.0, r_max=3.5,
                    dtype=np.float32):
     """Many independent 3D clouds: N log-uniform in [n_min, n_max], each a perturbed cubic
     lattice of side round(N^(1/3)) (so the realised count is side^3), spacing 1, noise
-    U[-0.25, 0.25]; radius U[r_min, r_max]; box = the lattice's extent.  Returns a list of
+    U[-0.25, 0.25]; radius U[r_min, r_max]; box [-1, side + 1]^3 (the lattice 1..side with a
+    margin of 1, as for the 200^3 workload).  Returns a list of
     dicts with x, v, dx, radius, min_corner, max_corner."""
     rng = np.random.default_rng(seed)
     clouds = []
@@ -92,7 +93,7 @@ def batched_clouds(n_clouds=512, n_min=1000, n_max=200000, r_min=2.0, r_max=3.5,
             "v": np.ascontiguousarray(v, dtype=dtype),
             "dx": np.ascontiguousarray(dx, dtype=dtype),
             "radius": r,
-            "min_corner": [0.0, 0.0, 0.0],
+            "min_corner": [-1.0, -1.0, -1.0],
             "max_corner": [side + 1.0] * 3,
         })
     return clouds
