@@ -256,47 +256,95 @@ def run_gpu(args, rank, world, local):
     value = all_pairs / max_s
     pairs_per_sweep = pairs_timed / K
 
-    # ---- end to end through the C ABI with host buffers: the same positions walked back
-    # (each step again a N(0, 0.05^2) displacement of the previous one)
+    # ---- end to end through the C ABI with host buffers: the timed positions again (after a
+    # warm-up at the first of them).  Every step copies
+    # its positions and velocities from pinned host memory and its density and acceleration
+    # back; the copies are double-buffered on two copy streams, so step k+1's inputs arrive
+    # and step k-1's outputs leave while step k computes.
     e2e = None
     if not args.no_e2e:
-        order = list(range(Wm + K - 1, Wm - 1, -1))
+        order = list(range(Wm, Wm + K))
         walk_h = [walk[i].cpu().pin_memory() for i in order]
         v_h = torch.as_tensor(v).reshape(-1).pin_memory()
-        rho_h = torch.empty(n, dtype=tdt).pin_memory()
-        acc_h = torch.empty(3 * n, dtype=tdt).pin_memory()
-        x1dev = torch.empty((n, 3), dtype=tdt, device="cuda")
-        xb = x1dev.T
+        rho_h = [torch.empty(n, dtype=tdt).pin_memory() for _ in range(2)]
+        acc_h = [torch.empty(3 * n, dtype=tdt).pin_memory() for _ in range(2)]
+        xb = [torch.empty((n, 3), dtype=tdt, device="cuda") for _ in range(2)]
+        xbT = [t.T for t in xb]
+        vb = [torch.empty(3 * n, dtype=tdt, device="cuda") for _ in range(2)]
+        rb = [torch.empty(n, dtype=tdt, device="cuda") for _ in range(2)]
+        pb = [torch.empty(n, dtype=tdt, device="cuda") for _ in range(2)]
+        ab = [torch.empty(3 * n, dtype=tdt, device="cuda") for _ in range(2)]
+        dens_b = [P.WCSPHDensity(density=rb[i], pressure=pb[i], velocity=vb[i], **W.WCSPH)
+                  for i in range(2)]
+        force_b = [P.WCSPHForce(density=rb[i], pressure=pb[i], velocity=vb[i], accel=ab[i],
+                                reuse_state=True, **W.WCSPH) for i in range(2)]
+        comp = torch.cuda.current_stream()
+        s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+        ev_in = [torch.cuda.Event() for _ in range(2)]
+        ev_done = [torch.cuda.Event() for _ in range(2)]
+        ev_out = [torch.cuda.Event() for _ in range(2)]
+        for e in ev_done + ev_out:
+            e.record(comp)
 
-        def e2e_step(xh):
-            x1dev.copy_(xh, non_blocking=True)
-            vd.copy_(v_h, non_blocking=True)
-            P.update(nhs, xb, xb, check=False)
-            P.foreach_point_neighbor(dens, xb, xb, nhs, check=False)
-            P.foreach_point_neighbor(force, xb, xb, nhs, check=False)
-            rho_h.copy_(rho, non_blocking=True)
-            acc_h.copy_(acc, non_blocking=True)
+        def h2d(k, xh):
+            bi = k % 2
+            with torch.cuda.stream(s_in):
+                s_in.wait_event(ev_done[bi])  # step k-2 no longer reads buffer bi
+                xb[bi].copy_(xh, non_blocking=True)
+                vb[bi].copy_(v_h, non_blocking=True)
+                ev_in[bi].record(s_in)
 
-        for _ in range(3):
-            e2e_step(walk_h[0])
+        def compute(k):
+            bi = k % 2
+            comp.wait_event(ev_in[bi])
+            comp.wait_event(ev_out[bi])  # step k-2's outputs have left
+            P.update(nhs, xbT[bi], xbT[bi], check=False)
+            P.foreach_point_neighbor(dens_b[bi], xbT[bi], xbT[bi], nhs, check=False)
+            P.foreach_point_neighbor(force_b[bi], xbT[bi], xbT[bi], nhs, check=False)
+            ev_done[bi].record(comp)
+
+        def d2h(k):
+            bi = k % 2
+            with torch.cuda.stream(s_out):
+                s_out.wait_event(ev_done[bi])
+                rho_h[bi].copy_(rb[bi], non_blocking=True)
+                acc_h[bi].copy_(ab[bi], non_blocking=True)
+                ev_out[bi].record(s_out)
+
+        def run(steps, src):
+            h2d(0, src(0))
+            for k in range(steps):
+                if k + 1 < steps:
+                    h2d(k + 1, src(k + 1))
+                compute(k)
+                d2h(k)
+            comp.wait_event(ev_out[(steps - 1) % 2])
+
+        run(3, lambda k: walk_h[0])
         torch.cuda.synchronize()
         barrier(world)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a0.record()
-        for k in range(K):
-            e2e_step(walk_h[k])
-        a1.record()
+        a0.record(comp)
+        s_in.wait_event(a0)
+        run(K, lambda k: walk_h[k])
+        a1.record(comp)
         torch.cuda.synchronize()
         barrier(world)
         e2e_s, e2e_pairs = aggregate(a0.elapsed_time(a1) / 1e3, 2.0 * pairs_timed, world,
                                      device=torch.device("cuda"))
         if P.lib().pn_sync(nhs.handle) != 0:
             raise RuntimeError("e2e region reported an error")
+        # the last step's outputs equal the device-timed run's (same positions, same search)
+        same = bool(torch.equal(rho_h[(K - 1) % 2], rho.cpu()) and
+                    torch.equal(acc_h[(K - 1) % 2], acc.cpu()))
         tb = 4 if dt == np.float32 else 8
         e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 6 * n * tb,
                "d2h_bytes_per_step": 4 * n * tb, "ms_per_step": 1e3 * e2e_s / K,
-               "path": "pinned host -> cudaMemcpyAsync -> pn_update + pn_foreach_point_neighbor "
-                       "(density, force) -> device->host density and acceleration"}
+               "outputs_equal_device_run": same,
+               "path": "pinned host -> cudaMemcpyAsync (copy stream, double-buffered) -> "
+                       "pn_update + pn_foreach_point_neighbor (density, force) -> "
+                       "cudaMemcpyAsync (second copy stream) -> pinned host density and "
+                       "acceleration"}
         del walk_h
     del walk
 

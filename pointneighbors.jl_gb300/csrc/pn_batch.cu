@@ -487,6 +487,12 @@ int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_cl
       a.pos = b->d_pos;
       a.err = b->d_err;
       a.outside = b->d_err + 1;
+      a.unsorted = nullptr;  // the batch always re-bins: every cell sorted by x
+      for (int k = 0; k < 3; ++k) {
+        const double mn = a.g.min_pad[k], mx = mn + a.g.n[k] * (double)a.g.cell_size[k];
+        a.clip_m[k] = (float)(16.0 * (double)std::numeric_limits<float>::epsilon() *
+                              (std::fabs(mn) + std::fabs(mx) + a.g.cell_size[k]));
+      }
       const double r2 = (double)a.g.r2;
       a.r2_lo = (float)(r2 * (1.0 - 32.0 * u));
       a.r2_hi = (float)(r2 * (1.0 + 32.0 * u));

@@ -206,8 +206,15 @@ __device__ __forceinline__ void finalize_slot(const int32_t* __restrict__ tmp_pe
   const int32_t c = cell_of_slot[k];
   const int32_t s = start[c], e = start[c + 1];
   const int32_t v = tmp_perm[k];
+  // inside the cell: ascending first coordinate, ties by point index (a total order, so
+  // the layout is deterministic); a stencil row's three cells are then one x-sorted run
+  const T xv = y[(int64_t)v * D];
   int32_t rank = 0;
-  for (int32_t q = s; q < e; ++q) rank += (__ldg(&tmp_perm[q]) < v);
+  for (int32_t q = s; q < e; ++q) {
+    const int32_t u = __ldg(&tmp_perm[q]);
+    const T xu = __ldg(&y[(int64_t)u * D]);
+    rank += (xu < xv) || (xu == xv && u < v);
+  }
   const int32_t dst = s + rank;
   perm[dst] = v;
   T p[D];
@@ -344,11 +351,16 @@ k_finalize_movers(const int32_t* __restrict__ tmp_perm, const int32_t* __restric
 // The decision: rebuild when the points outside their main cell exceed `fraction` of the
 // binned points (the traversal cost of the overflow lists grows with them, while a full
 // rebuild costs about as much as marking the movers).
+// gate[1] ("unsorted") tells the traversal that the main slots are no longer sorted by x
+// inside their cells (the overflow path refreshes positions in place).
 __global__ void k_decide_update(const int32_t* __restrict__ ovf_n,
                                 const int32_t* __restrict__ n_main, double fraction,
                                 int32_t* __restrict__ gate) {
-  if (threadIdx.x == 0 && blockIdx.x == 0)
-    *gate = (double)*ovf_n > fraction * (double)*n_main ? GATE_REBUILD : GATE_OVERFLOW;
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const int32_t m = (double)*ovf_n > fraction * (double)*n_main ? GATE_REBUILD : GATE_OVERFLOW;
+    gate[0] = m;
+    gate[1] = m == GATE_OVERFLOW ? 1 : 0;
+  }
 }
 
 __global__ void __launch_bounds__(256)
@@ -433,6 +445,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   if (rc != PN_OK) return rc;
   cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * s->n_total, st);
   cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
+  cudaMemsetAsync(s->d_err + 3, 0, sizeof(int32_t), st);  // cells sorted by x again
   if (m > 0) dispatch_bin<T>(s, y, n_y, idx, (int32_t)m, st);
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
   if (m > 0) {
@@ -760,18 +773,17 @@ __global__ void k_export_points(const int32_t* __restrict__ start, const int32_t
   const int64_t o0 = o;
   for (int32_t k = start[c]; k < start[c + 1]; ++k)
     if (perm[k] >= 0) points[o++] = perm[k];
-  if (ovf_start) {
+  if (ovf_start)
     for (int32_t k = ovf_start[c]; k < ovf_start[c + 1]; ++k) points[o++] = ovf_perm[k];
-    // insertion sort of the merged cell (short lists)
-    for (int64_t a = o0 + 1; a < o; ++a) {
-      const int32_t v = points[a];
-      int64_t b = a - 1;
-      while (b >= o0 && points[b] > v) {
-        points[b + 1] = points[b];
-        --b;
-      }
-      points[b + 1] = v;
+  // ascending point index (a cell is stored sorted by coordinate); insertion sort
+  for (int64_t a = o0 + 1; a < o; ++a) {
+    const int32_t v = points[a];
+    int64_t b = a - 1;
+    while (b >= o0 && points[b] > v) {
+      points[b + 1] = points[b];
+      --b;
     }
+    points[b + 1] = v;
   }
 }
 

@@ -40,6 +40,14 @@ struct TravArgs {
   T r2_lo, r2_hi;               // r^2 (1 -+ 32 eps): the FMA distance test decides outside
   const int32_t* outside;       // device flag: some binned point lies outside the periodic box
   int32_t* err;
+  // Row clipping: inside every cell the points are sorted by their first coordinate, so a
+  // stencil row's three cells are one x-sorted run and a query only scans the part of it
+  // within x +- sqrt(r^2 - dy^2 - dz^2) (dy, dz: distance to the row's band).  `unsorted`
+  // (device flag, or null = sorted) is set while an incremental update keeps overflow lists
+  // (positions refreshed in place); `clip_m` is a per-dimension margin that covers the
+  // rounding of the cell edges, so the clipped run is always a superset of the neighbours.
+  const int32_t* unsorted;
+  T clip_m[3];
 };
 
 template <typename T, int D>
@@ -123,6 +131,26 @@ __device__ __forceinline__ void store4(float* p, int64_t k, V4<float> v) {
 __device__ __forceinline__ void store4(double* p, int64_t k, V4<double> v) {
   reinterpret_cast<double2*>(p)[2 * k] = make_double2(v.x, v.y);
   reinterpret_cast<double2*>(p)[2 * k + 1] = make_double2(v.z, v.w);
+}
+
+// Packed FP32 pairs (Blackwell f32x2 arithmetic, round to nearest like the scalar forms).
+__device__ __forceinline__ uint64_t pack_f32x2(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void unpack_f32x2(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t sub_f32x2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ uint64_t mul_f32x2(uint64_t a, uint64_t b) {
+  uint64_t r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
 }
 
 // Pair-function math (only the sums are compared with the FP64 oracle, within tolerance):
@@ -666,6 +694,26 @@ __device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F:
   if constexpr (F::kInline) {
     // one candidate at a time with the exact test and the pair function applied in place
     // on the registers just loaded (a cheap pair function needs no compaction)
+    if constexpr (sizeof(T) == 4 && D == 3 && !WRAP) {
+      // the x and y differences and squares as packed pairs (sub/mul.rn.f32x2: the same
+      // correctly rounded operations as the scalar exact form, two per instruction)
+      const uint64_t qxy = pack_f32x2(q.x[0], q.x[1]);
+      for (int32_t js = beg; js < end; ++js) {
+        const float4 cj = __ldg(reinterpret_cast<const float4*>(a.pos) + js);
+        const uint64_t dxy = sub_f32x2(qxy, pack_f32x2(cj.x, cj.y));
+        float sx, sy;
+        unpack_f32x2(mul_f32x2(dxy, dxy), sx, sy);
+        const float dz = __fsub_rn(q.x[2], cj.z);
+        const float d2 = __fadd_rn(__fadd_rn(sx, sy), __fmul_rn(dz, dz));
+        if (d2 <= a.g.r2) {
+          T pd[3];
+          unpack_f32x2(dxy, pd[0], pd[1]);
+          pd[2] = dz;
+          F::pair(acc, p, q, js, pd, d2, (T)0);
+        }
+      }
+      return;
+    }
     for (int32_t js = beg; js < end; ++js) {
       T yj[D], pd[D];
       load_cand<T, D>(a.pos, js, yj);
@@ -694,6 +742,49 @@ __device__ __forceinline__ void scan_any(const TravArgs<T>& a, const typename F:
   else scan_run<T, D, PER, false, F>(a, p, acc, q, beg, end);
 }
 
+// Rows this short are scanned whole: the two binary searches would cost more than the
+// candidates they skip.
+constexpr int32_t CLIP_MIN_RUN = 32;
+
+// First slot of the x-sorted run [b, e) with x >= v (lower) or x > v (upper).
+template <typename T, int D, bool UPPER>
+__device__ __forceinline__ int32_t bound_x(const T* __restrict__ pos, int32_t b, int32_t e, T v) {
+  constexpr int S = PS<D>::value;
+  int32_t n = e - b;
+  while (n > 0) {
+    const int32_t h = n >> 1;
+    const T xk = __ldg(&pos[(int64_t)(b + h) * S]);
+    if (UPPER ? !(v < xk) : (xk < v)) {
+      b += h + 1;
+      n -= h + 1;
+    } else {
+      n = h;
+    }
+  }
+  return b;
+}
+
+// Clip the x-sorted run [b0, e0) of the stencil row (oy, oz) to the query's reach
+// x +- sqrt(r^2 - dy^2 - dz^2); an unreachable row becomes empty.  below/above: the query's
+// distance (less the margin) to the lower/upper edge of its cell in y and z.
+template <typename T, int D>
+__device__ __forceinline__ void clip_row(const TravArgs<T>& a, const Query<T, D>& q,
+                                         const T* below, const T* above, int oy, int oz,
+                                         int32_t& b0, int32_t& e0) {
+  if (e0 - b0 <= CLIP_MIN_RUN) return;
+  const T dy = oy < 0 ? below[1] : (oy > 0 ? above[1] : (T)0);
+  const T dz = oz < 0 ? below[2] : (oz > 0 ? above[2] : (T)0);
+  // slack for the rounding of these few operations (the exact test decides)
+  const T rem = a.g.r2 * (T)1.00001 - dy * dy - dz * dz;
+  if (rem < (T)0) {
+    e0 = b0;
+    return;
+  }
+  const T w = fsqrt(rem) * (T)1.00001 + a.clip_m[0];
+  b0 = bound_x<T, D, false>(a.pos, b0, e0, q.x[0] - w);
+  e0 = bound_x<T, D, true>(a.pos, b0, e0, q.x[0] + w);
+}
+
 // One query per thread.  A warp holds consecutive queries (in sorted mode: consecutive
 // cell-sorted slots), so its lanes walk the same or shifted stencil rows in lockstep and
 // share most candidate loads.  Rows are visited in the reference's CartesianIndices
@@ -715,6 +806,18 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
 #pragma unroll
     for (int k = 0; k < D; ++k) wrap |= c[k] < 4 || c[k] > g.ncell[k] - 1;
   }
+  // row clipping (see TravArgs): the query's distance to the lower and upper edge of its
+  // cell in y and z, reduced by the margin; rows near a periodic face are not clipped
+  const bool clip = valid && !(PER && wrap) && (a.unsorted == nullptr || *a.unsorted == 0);
+  T below[3] = {(T)0, (T)0, (T)0}, above[3] = {(T)0, (T)0, (T)0};
+  if (clip) {
+#pragma unroll
+    for (int k = 1; k < D; ++k) {
+      const T lo = g.min_pad[k] + xfloor((q.x[k] - g.min_pad[k]) / g.cell_size[k]) * g.cell_size[k];
+      below[k] = fmax(q.x[k] - lo - a.clip_m[k], (T)0);
+      above[k] = fmax(lo + g.cell_size[k] - q.x[k] - a.clip_m[k], (T)0);
+    }
+  }
   constexpr int OZ = D == 3 ? 1 : 0;
   constexpr int OY = D >= 2 ? 1 : 0;
 #pragma unroll 1
@@ -727,7 +830,12 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
       if (D >= 2) row += ((PER ? pwrap(c[1] + oy, g.ncell[1]) : c[1] + oy) - 1) * g.n[0];
       if (!PER || (c[0] >= 3 && c[0] <= g.ncell[0])) {
         const int32_t l0 = row + c[0] - 2;
-        scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.start[l0]), __ldg(&a.start[l0 + 3]));
+        int32_t b0 = __ldg(&a.start[l0]), e0 = __ldg(&a.start[l0 + 3]);
+        if (clip) {
+          clip_row<T, D>(a, q, below, above, oy, oz, b0, e0);
+          if (b0 >= e0) continue;  // no point of this row is within r
+        }
+        scan_any<T, D, PER, F>(a, p, acc, q, wrap, b0, e0);
         if (a.ovf_start)
           scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.ovf_start[l0]),
                                  __ldg(&a.ovf_start[l0 + 3]));

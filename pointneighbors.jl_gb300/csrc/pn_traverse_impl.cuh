@@ -181,6 +181,10 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
   a.n_x = n_x;
   a.err = s->d_err;
   a.outside = s->d_err + 1;
+  a.unsorted = s->d_err + 3;
+  for (int k = 0; k < 3; ++k)
+    a.clip_m[k] = (T)(16.0 * (double)std::numeric_limits<T>::epsilon() *
+                      (std::fabs(s->min_pad[k]) + std::fabs(s->max_pad[k]) + s->cell_size[k]));
   {
     // Band around r^2 outside which the FMA distance test is decisive: 32 units in the
     // last place on each side (the two forms differ by at most 6).
