@@ -263,6 +263,46 @@ int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stre
  * cell's points ascending. */
 int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream);
 
+/* ----------------------------------------------------------------- precomputed lists */
+
+/* PrecomputedNeighborhoodSearch{NDIMS}(; search_radius, n_points, periodic_box,
+ *   update_strategy, max_neighbors, sort_neighbor_lists) (nhs_precomputed.jl:67-124) with
+ * a FullGridCellList grid search (cfg) computing the lists (update_neighborhood_search).
+ * max_neighbors > 0 keeps the reference's capacity error (PN_ERR_CELL_FULL when a point has
+ * more neighbours); 0 = no limit.  The lists are stored per query as slots of the grid
+ * search's cell-sorted arrays, in groups of 32 rows transposed (the reference's
+ * transpose_backend layout for GPUs, without a fixed column height). */
+typedef struct pn_precomputed pn_precomputed;
+int pn_pre_create(const pn_config* cfg, int32_t max_neighbors, pn_precomputed** out);
+int pn_pre_destroy(pn_precomputed* s);
+/* initialize!(search, x, y) (nhs_precomputed.jl:130-147): the grid search bins y, then the
+ * neighbour lists of every point of x are built (one host synchronisation to size them).
+ * eachindex_y other than all points is the reference's "does not support inactive points"
+ * error (PN_ERR_INVALID_ARG). */
+int pn_pre_initialize(pn_precomputed* s, const void* x, int64_t n_x, const void* y,
+                      int64_t n_y, const int32_t* eachindex_y, int64_t n_eachindex_y,
+                      pn_stream_t stream);
+/* update!(search, x, y; points_moving) (nhs_precomputed.jl:149-167). */
+int pn_pre_update(pn_precomputed* s, const void* x, int64_t n_x, const void* y, int64_t n_y,
+                  const int32_t* eachindex_y, int64_t n_eachindex_y, int32_t points_moving_x,
+                  int32_t points_moving_y, pn_stream_t stream);
+/* foreach_point_neighbor over the stored lists (nhs_precomputed.jl:206-247): pos_diff and
+ * distance recomputed (periodic image when d^2 > r^2), no distance check; any functor of
+ * pn_foreach_point_neighbor.  x and y must be the arrays of the last initialize!/update!
+ * (requires_update is (true, true)). */
+int pn_pre_foreach_point_neighbor(pn_precomputed* s, int32_t functor, const void* x,
+                                  int64_t n_x, const void* y, int64_t n_y,
+                                  const int32_t* points, int64_t n_points, const void* params,
+                                  pn_stream_t stream);
+/* The lists as CSR over the points of x: offsets int64[n_x + 1] (always written), neighbour
+ * point indices int32[capacity] (written when they fit, else PN_ERR_CAPACITY), each row
+ * sorted ascending when `sort` (the reference's sorteach!, sort_neighbor_lists). */
+int pn_pre_neighbor_lists(pn_precomputed* s, int32_t sort, int64_t* offsets, int32_t* neighbors,
+                          int64_t capacity, pn_stream_t stream);
+int pn_pre_sync(pn_precomputed* s);
+/* requires_update(::PrecomputedNeighborhoodSearch) == (true, true) (nhs_precomputed.jl:128). */
+int pn_pre_requires_update(const pn_precomputed* s, int32_t out[2]);
+
 /* ----------------------------------------------------------------- batched form */
 
 /* Many independent clouds, each its own GridNeighborhoodSearch (own corners, radius and

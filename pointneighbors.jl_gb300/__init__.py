@@ -37,6 +37,7 @@ __all__ = [
     "neighbor_lists", "CountNeighbors", "NeighborIndexSum", "NBodyAcceleration",
     "TruncatedPotential", "WCSPHDensity", "WCSPHForce", "WCSPHStep",
     "AdjointLossForward", "AdjointLossBackward", "adjoint_loss", "BatchedNeighborhoodSearch",
+    "PrecomputedNeighborhoodSearch",
     "ArgumentError", "BoundsError", "PointNeighborsError", "UnsupportedFunctorError",
 ]
 
@@ -251,6 +252,12 @@ class GridNeighborhoodSearch:
     def handle(self) -> C.c_void_p:
         return self._h
 
+    def _sync(self) -> int:
+        return lib().pn_sync(self._h)
+
+    def _clear_error(self):
+        lib().pn_get_error(self._h, 1)
+
     def grid_info(self) -> dict:
         gi = _lib.pn_grid_info()
         rc = lib().pn_get_grid_info(self._h, C.byref(gi))
@@ -329,24 +336,29 @@ def _ptr(t):
 
 def _finish(nhs, rc, check, what):
     if rc != _lib.PN_OK:
-        lib().pn_get_error(nhs._h, 1)
+        nhs._clear_error()
         _raise(rc, what)
     if check:
-        st = lib().pn_sync(nhs._h)
+        st = nhs._sync()
         if st != _lib.PN_OK:
             _raise(st, what)
 
 
 # ------------------------------------------------------------------------- API
 
-def requires_update(nhs: GridNeighborhoodSearch):
-    """(x_changed, y_changed) -> (False, True) (nhs_grid.jl:133)."""
+def requires_update(nhs):
+    """(x_changed, y_changed) -> (False, True) (nhs_grid.jl:133); (True, True) for the
+    precomputed search (nhs_precomputed.jl:128)."""
+    if getattr(nhs, "_precomputed", False):
+        return (True, True)
     return (False, True)
 
 
-def copy_neighborhood_search(nhs: GridNeighborhoodSearch, search_radius, n_points):
+def copy_neighborhood_search(nhs, search_radius, n_points):
     """Same corners, periodic box, strategy and cell capacity; new radius and size
-    (nhs_grid.jl:640-649)."""
+    (nhs_grid.jl:640-649, nhs_precomputed.jl:249-266)."""
+    if getattr(nhs, "_precomputed", False):
+        return nhs._copy(search_radius, n_points)
     cl = nhs.cell_list
     T = _eltype(search_radius)
     new_cl = FullGridCellList(min_corner=cl._min.astype(T), max_corner=cl._max.astype(T),
@@ -357,8 +369,10 @@ def copy_neighborhood_search(nhs: GridNeighborhoodSearch, search_radius, n_point
                                   update_strategy=nhs.update_strategy)
 
 
-def initialize(nhs: GridNeighborhoodSearch, x, y, *, eachindex_y=None, check=True):
-    """initialize!(nhs, x, y; eachindex_y) (nhs_grid.jl:220-281)."""
+def initialize(nhs, x, y, *, eachindex_y=None, check=True):
+    """initialize!(nhs, x, y; eachindex_y) (nhs_grid.jl:220-281, nhs_precomputed.jl:130-147)."""
+    if getattr(nhs, "_precomputed", False):
+        return nhs._initialize(x, y, eachindex_y, check)
     y_src = y
     y = _coords(nhs, y, "y")
     idx = _index_tensor(eachindex_y, y.shape[1], "eachindex_y")
@@ -372,7 +386,10 @@ def initialize(nhs: GridNeighborhoodSearch, x, y, *, eachindex_y=None, check=Tru
 
 def update(nhs: GridNeighborhoodSearch, x, y, *, points_moving=(True, True), eachindex_y=None,
            check=True):
-    """update!(nhs, x, y; points_moving, eachindex_y) (nhs_grid.jl:283-292)."""
+    """update!(nhs, x, y; points_moving, eachindex_y) (nhs_grid.jl:283-292,
+    nhs_precomputed.jl:149-167)."""
+    if getattr(nhs, "_precomputed", False):
+        return nhs._update(x, y, points_moving, eachindex_y, check)
     if not points_moving[1]:
         return nhs
     y_src = y
@@ -572,10 +589,10 @@ def foreach_point_neighbor(f, x, y, nhs: GridNeighborhoodSearch, *, points=None,
     pts = _index_tensor(points, x.shape[1], "points")
     n_q = x.shape[1] if pts is None else pts.numel()
     p = f.params(nhs, x, y, n_q)
-    rc = lib().pn_foreach_point_neighbor(nhs._h, f.functor, _ptr(x), x.shape[1], _ptr(y),
-                                         y.shape[1], _ptr(pts),
-                                         0 if pts is None else pts.numel(), C.byref(p),
-                                         _stream())
+    fn = lib().pn_pre_foreach_point_neighbor if getattr(nhs, "_precomputed", False) \
+        else lib().pn_foreach_point_neighbor
+    rc = fn(nhs._h, f.functor, _ptr(x), x.shape[1], _ptr(y), y.shape[1], _ptr(pts),
+            0 if pts is None else pts.numel(), C.byref(p), _stream())
     _finish(nhs, rc, check, "foreach_point_neighbor")
 
 
@@ -584,6 +601,10 @@ def neighbor_lists(x, y, nhs: GridNeighborhoodSearch, *, points=None, sort=True)
     reference test's `push!(neighbors[point], neighbor)` (test/neighborhood_search.jl:
     325-336), rows sorted ascending when `sort`."""
     torch = _torch()
+    if getattr(nhs, "_precomputed", False):
+        if points is not None:
+            raise ArgumentError("the precomputed search exports the lists of all points")
+        return nhs._lists(sort)
     x, y = _bound(nhs, x, "x"), _bound(nhs, y, "y")
     pts = _index_tensor(points, x.shape[1], "points")
     n_q = x.shape[1] if pts is None else pts.numel()
@@ -654,3 +675,4 @@ def eachneighbor(coords, nhs: GridNeighborhoodSearch):
 
 from .adjoint import adjoint_loss  # noqa: E402  (uses the API above)
 from .batch import BatchedNeighborhoodSearch  # noqa: E402
+from .precomputed import PrecomputedNeighborhoodSearch  # noqa: E402

@@ -128,6 +128,16 @@ _SIGNATURES = {
     "pn_cell_coords": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "pn_export_cells": (C.c_int, [_P, _P, _P, _P]),
     "pn_count_neighbors_noalloc": (C.c_int, [C.POINTER(pn_config), _P, C.c_int64, _P, _P]),
+    "pn_pre_create": (C.c_int, [C.POINTER(pn_config), C.c_int32, C.POINTER(_P)]),
+    "pn_pre_destroy": (C.c_int, [_P]),
+    "pn_pre_initialize": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P, C.c_int64, _P]),
+    "pn_pre_update": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P, C.c_int64, C.c_int32,
+                                C.c_int32, _P]),
+    "pn_pre_foreach_point_neighbor": (C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.c_int64,
+                                                _P, C.c_int64, _P, _P]),
+    "pn_pre_neighbor_lists": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int64, _P]),
+    "pn_pre_sync": (C.c_int, [_P]),
+    "pn_pre_requires_update": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "pn_batch_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(C.c_int64), C.c_int32,
                                   C.POINTER(_P)]),
     "pn_batch_destroy": (C.c_int, [_P]),

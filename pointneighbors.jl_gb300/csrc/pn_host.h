@@ -118,9 +118,29 @@ void finalize_slots(int ndims, const int32_t* tmp_perm, const int32_t* cell_of_s
 int sort_rows(pn_search* s, const int64_t* offsets, int64_t n_rows, int32_t* vals,
               int64_t total, cudaStream_t st);
 
+// Precomputed neighbour lists handed to a traversal: row r's t-th neighbour slot is
+// nb[grp[r / 32] + 32 t + r % 32], len[r] of them; rows are slots (by_slot) or queries.
+struct ListsRef {
+  const int32_t* nb;
+  const int64_t* grp;
+  const int32_t* len;
+  const int32_t* row_of;  // point -> slot row (by_slot lists)
+  int32_t by_slot;
+  int64_t n_rows;
+};
+
 // pn_traverse_f32.cu / pn_traverse_f64.cu
 template <typename T>
 int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
-            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st);
+            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st,
+            const ListsRef* lists = nullptr);
+// The precomputed search's list build over the grid search `s` (x against y): row lengths
+// into `len` (slot rows when x is y, else query rows), then the slots into the lists.
+template <typename T>
+int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* len,
+                int32_t* by_slot, int64_t* n_rows, cudaStream_t st);
+template <typename T>
+int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* nb,
+               const int64_t* grp, cudaStream_t st);
 
 }  // namespace pn

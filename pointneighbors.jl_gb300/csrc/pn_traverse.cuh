@@ -48,6 +48,13 @@ struct TravArgs {
   // rounding of the cell edges, so the clipped run is always a superset of the neighbours.
   const int32_t* unsorted;
   T clip_m[3];
+  // Precomputed neighbour lists (or null: the grid traversal).  Row r's t-th neighbour slot
+  // is nb[nb_grp[r / 32] + 32 t + r % 32] (groups of 32 rows stored transposed, so a warp
+  // reads its rows' t-th entries in one coalesced load); nb_len[r] entries per row.
+  const int32_t* nb;
+  const int64_t* nb_grp;
+  const int32_t* nb_len;
+  const int32_t* nb_row_of;  // query point -> its row (lists built by slot), or null: row = point
 };
 
 template <typename T, int D>
@@ -171,6 +178,7 @@ __device__ __forceinline__ double fdiv(double a, double b) { return a / b; }
 // update); kCountOnly functors take count(acc, n) for n accepted neighbours at once.
 // `slot` indexes the cell-sorted arrays.
 
+// by_row: 0 = indexed by point, 1 = by query row, 2 = by slot (cell-sorted queries)
 template <typename T> struct CountParams { int32_t* counts; int32_t by_row; };
 template <typename T> struct IndexSumParams { int64_t* sums; const int32_t* perm; };
 template <typename T> struct EmitParams {
@@ -191,10 +199,10 @@ struct FCount {
                                               const T*, T, T) { ++a.n; }
   static __device__ __forceinline__ void count(Acc& a, int n) { a.n += n; }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
-    p.counts[p.by_row ? q.q : q.i] = a.n;
+    p.counts[p.by_row == 2 ? q.k : (p.by_row ? q.q : q.i)] = a.n;
   }
   static __device__ __forceinline__ void fail(const Params& p, const Query<T, D>& q) {
-    if (p.by_row) p.counts[q.q] = 0;
+    if (p.by_row == 1) p.counts[q.q] = 0;
   }
 };
 
@@ -232,6 +240,33 @@ struct FEmit {
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T*, T, T) {
     if (a.o < a.end) p.nbrs[a.o++] = __ldg(&p.perm[js]);
+  }
+  static __device__ __forceinline__ void finish(Acc&, const Params&, const Query<T, D>&) {}
+};
+
+// The precomputed search's list build: every accepted candidate slot, in traversal order
+// (ascending slots), into the query row's transposed list; the row lengths come from a
+// counting pass over the same search.
+template <typename T> struct EmitListParams {
+  int32_t* nb; const int64_t* grp; int32_t by_slot;
+};
+
+template <typename T, int D>
+struct FEmitList {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
+  using Params = EmitListParams<T>;
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
+  static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
+  struct Acc { int64_t o; };
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
+    const int32_t r = p.by_slot ? q.k : q.q;
+    a.o = p.grp[r >> 5] + (r & 31);
+  }
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
+                                              const T*, T, T) {
+    p.nb[a.o] = js;
+    a.o += 32;
   }
   static __device__ __forceinline__ void finish(Acc&, const Params&, const Query<T, D>&) {}
 };
@@ -920,6 +955,70 @@ k_trav_list(const TravArgs<T> a, const typename F::Params p) {
     for (int d = 0; d < D; ++d) q.x[d] = (T)0;
   }
   traverse_query<T, D, PER, F>(a, p, q, c, valid);
+}
+
+// ================================================================== precomputed lists
+// nhs_precomputed.jl:206-247: every stored neighbour of the query, with pos_diff and d2
+// recomputed exactly (and the periodic image when d2 > r^2); no distance check, like the
+// reference.  `row` is the query's list.
+template <typename T, int D, bool PER, class F>
+__device__ __forceinline__ void list_query(const TravArgs<T>& a, const typename F::Params& p,
+                                           Query<T, D>& q, int32_t row, bool valid) {
+  typename F::Acc acc;
+  if (!valid) return;
+  F::init(acc, p, q);
+  const int32_t n = __ldg(&a.nb_len[row]);
+  const int32_t* nb = a.nb + __ldg(&a.nb_grp[row >> 5]) + (row & 31);
+#pragma unroll 2
+  for (int32_t t = 0; t < n; ++t) {
+    const int32_t js = __ldg(&nb[32 * t]);
+    T yj[D], pd[D];
+    const T aux = load_cand<T, D>(a.pos, js, yj);
+    const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
+    F::pair(acc, p, q, js, pd, d2, aux);
+  }
+  F::finish(acc, p, q);
+}
+
+// Cell-sorted queries (lists built with x is y): row = slot.
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_lists_sorted(const TravArgs<T> a, const typename F::Params p) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
+  Query<T, D> q;
+  bool valid = k < n_slots;
+  q.i = valid ? a.perm[k] : -1;
+  if (valid && q.i < 0) F::vacant(p, (int32_t)k);
+  valid = valid && q.i >= 0;
+  q.q = q.i;
+  q.k = (int32_t)k;
+  if (valid) load_pos<T, D>(a.pos, k, q.x);
+  list_query<T, D, PER, F>(a, p, q, (int32_t)k, valid);
+}
+
+// Queries x[:, qlist[t]] (or t) in the given order: row = t.
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_lists_query(const TravArgs<T> a, const typename F::Params p) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Query<T, D> q;
+  bool valid = t < a.n_q;
+  q.i = valid ? (a.qlist ? a.qlist[t] : (int32_t)t) : -1;
+  q.q = (int32_t)t;
+  q.k = -1;
+  if (valid && (q.i < 0 || q.i >= a.n_x)) {
+    set_error(a.err, PN_ERR_INVALID_ARG);
+    valid = false;
+  }
+  int32_t row = 0;
+  if (valid) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) q.x[k] = a.x[(int64_t)q.i * D + k];
+    row = a.nb_row_of ? a.nb_row_of[q.i] : q.i;
+    q.k = a.nb_row_of ? row : -1;  // the query's own slot, when the rows are slots
+  }
+  list_query<T, D, PER, F>(a, p, q, row, valid);
 }
 
 }  // namespace pn

@@ -110,7 +110,13 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
   const int key = s->ndims * 2 + (s->periodic ? 1 : 0);
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
-    if (sorted) {                                                                       \
+    if (a.nb != nullptr) {                                                              \
+      if (sorted)                                                                       \
+        k_lists_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
+      else                                                                              \
+        k_lists_query<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);      \
+      count_launch();                                                                   \
+    } else if (sorted) {                                                                \
       k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
       count_launch();                                                                   \
     } else {                                                                            \
@@ -157,17 +163,11 @@ static SphConst<T> sph_const(const pn_search* s, const pn_wcsph_params* w) {
   return c;
 }
 
+// Traversal arguments of a search for the queries x[:, points] against y; `sorted`: the
+// queries are the cell-sorted slots (x is y, every point binned).
 template <typename T>
-int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
-            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st) {
-  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
-  if (n_y != s->n_y || n_x < 0 || (points == nullptr && n_points != 0 && n_points != n_x))
-    return PN_ERR_INVALID_ARG;
-  if (params == nullptr) return PN_ERR_INVALID_ARG;
-  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && points == nullptr &&
-                      s->full_binned;
-  const int64_t n_q = points ? n_points : n_x;
-
+static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const int32_t* points,
+                             int64_t n_q) {
   TravArgs<T> a{};
   a.g = make_grid<T>(s);
   a.start = s->d_start;
@@ -192,6 +192,33 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
     const double r2 = (double)a.g.r2;
     a.r2_lo = (T)(r2 * (1.0 - 32.0 * u));
     a.r2_hi = (T)(r2 * (1.0 + 32.0 * u));
+  }
+  return a;
+}
+
+template <typename T>
+int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
+            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st,
+            const ListsRef* lists) {
+  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
+  if (n_y != s->n_y || n_x < 0 || (points == nullptr && n_points != 0 && n_points != n_x))
+    return PN_ERR_INVALID_ARG;
+  if (params == nullptr) return PN_ERR_INVALID_ARG;
+  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && points == nullptr &&
+                      s->full_binned;
+  const int64_t n_q = points ? n_points : n_x;
+  TravArgs<T> a = trav_args<T>(s, x, n_x, points, n_q);
+  if (lists != nullptr) {
+    // rows are slots (lists built with x is y) or the points of x
+    if (lists->by_slot) {
+      if ((const void*)x != (const void*)y || n_x != n_y) return PN_ERR_INVALID_ARG;
+      if (!sorted) a.nb_row_of = lists->row_of;  // a subset of the points
+    } else if (sorted || n_x != lists->n_rows) {
+      return PN_ERR_INVALID_ARG;
+    }
+    a.nb = lists->nb;
+    a.nb_grp = lists->grp;
+    a.nb_len = lists->len;
   }
   // Sorted mode launches one thread per possible slot; the kernel reads the live count.
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
@@ -337,6 +364,32 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
     default:
       return PN_ERR_UNSUPPORTED_FUNCTOR;
   }
+}
+
+// ------------------------------------------------------------------ precomputed lists
+template <typename T>
+int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* len,
+                int32_t* by_slot, int64_t* n_rows, cudaStream_t st) {
+  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
+  if (n_y != s->n_y || n_x < 0) return PN_ERR_INVALID_ARG;
+  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && s->full_binned;
+  TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
+  const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
+  *by_slot = sorted ? 1 : 0;
+  *n_rows = sorted ? n_sorted : n_x;
+  if (sorted) cudaMemsetAsync(len, 0, sizeof(int32_t) * n_sorted, st);  // vacated slots
+  CountParams<T> p{len, sorted ? 2 : 1};
+  return launch_trav<T, FCount>(s, a, p, sorted, *n_rows, st);
+}
+
+template <typename T>
+int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* nb,
+               const int64_t* grp, cudaStream_t st) {
+  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && s->full_binned;
+  TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
+  const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
+  EmitListParams<T> p{nb, grp, sorted ? 1 : 0};
+  return launch_trav<T, FEmitList>(s, a, p, sorted, sorted ? n_sorted : n_x, st);
 }
 
 }  // namespace pn
