@@ -63,12 +63,14 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",
-                    choices=["wcsph", "nbody2d", "count", "adjoint", "batched"],
+                    choices=["wcsph", "nbody2d", "count", "adjoint", "batched",
+                             "precomputed"],
                     help="wcsph: the 3D WCSPH step (headline); nbody2d: 2D periodic "
                          "truncated potential on a 4096^2 lattice; count: neighbour counts "
                          "of the 50^3 Float64 lattice; adjoint: loss + dL/dx on the "
                          "100^3 lattice (backward/forward ratio); batched: 512 clouds, "
-                         "one CUDA-graph step vs per-cloud launches")
+                         "one CUDA-graph step vs per-cloud launches; precomputed: the "
+                         "WCSPH step with PrecomputedNeighborhoodSearch lists")
     return ap.parse_args()
 
 
@@ -778,6 +780,111 @@ def run_gpu_batched(args, rank, world, local):
         print(json.dumps(out))
 
 
+def run_gpu_precomputed(args, rank, world, local):
+    """The 8M-point FP32 WCSPH step with a PrecomputedNeighborhoodSearch: update! rebuilds
+    the neighbour lists (through the grid search), then the density and force sweeps walk
+    them.  Same positions (random walk N(0, 0.05^2)), constants and metric as the default
+    workload; `loops_ms` times the two sweeps alone (lists reused), the case the
+    precomputed search is for."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    P = __graft_entry__.package()
+    W = P.workloads
+    torch.cuda.set_device(local)
+    n_side = args.n_side
+    x0, v, dx = W.wcsph_cloud(n_side, seed=1, dtype=np.float32)
+    x1 = (x0.astype(np.float64) + dx).astype(np.float32)
+    n = len(x0)
+    r = np.float32(3.0)
+    cl = P.FullGridCellList(min_corner=np.full(3, -1.0, np.float32),
+                            max_corner=np.full(3, n_side + 1.0, np.float32), search_radius=r,
+                            max_points_per_cell=0)
+    grid = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                    update_strategy=P.ParallelIncrementalUpdate())
+    # the reference's default capacity (320 neighbours per point in 3D): lists of fixed
+    # capacity, built in one pass without a host synchronisation
+    pre = P.PrecomputedNeighborhoodSearch(3, n_points=n, update_neighborhood_search=grid)
+    K, Wm = args.steps, args.warmup
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    walk = [torch.as_tensor(x1, device="cuda")]
+    for _ in range(Wm + K - 1):
+        walk.append(walk[-1] + 0.05 * torch.randn(walk[-1].shape, generator=gen, device="cuda"))
+    vd = torch.as_tensor(v, device="cuda").reshape(-1)
+    rho = torch.zeros(n, device="cuda")
+    prs = torch.zeros(n, device="cuda")
+    acc = torch.zeros(3 * n, device="cuda")
+    dens = P.WCSPHDensity(density=rho, pressure=prs, velocity=vd, **W.WCSPH)
+    force = P.WCSPHForce(density=rho, pressure=prs, velocity=vd, accel=acc, reuse_state=True,
+                         **W.WCSPH)
+    x0d = torch.as_tensor(x0, device="cuda").T
+    P.initialize(pre, x0d, x0d)
+    for s_ in range(Wm):
+        xs = walk[s_].T
+        P.update(pre, xs, xs)
+        P.foreach_point_neighbor(dens, xs, xs, pre, check=False)
+        P.foreach_point_neighbor(force, xs, xs, pre, check=False)
+    torch.cuda.synchronize()
+    ev = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
+    pairs = 0
+    cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    wall0 = time.perf_counter()
+    upd_wall = 0.0
+    for k in range(K):
+        xs = walk[Wm + k].T
+        e = ev[k]
+        e[0].record()
+        t = time.perf_counter()
+        P.update(pre, xs, xs, check=False)
+        upd_wall += time.perf_counter() - t
+        e[1].record()
+        P.foreach_point_neighbor(dens, xs, xs, pre, check=False)
+        e[2].record()
+        P.foreach_point_neighbor(force, xs, xs, pre, check=False)
+        e[3].record()
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    if pre._sync() != 0:
+        raise RuntimeError("timed region reported an error")
+    for k in range(K):
+        xs = walk[Wm + k].T
+        P.update(pre, xs, xs)
+        P.foreach_point_neighbor(P.CountNeighbors(cnt), xs, xs, pre)
+        pairs += int(cnt.to(torch.int64).sum())
+    upd = [ev[k][0].elapsed_time(ev[k][1]) for k in range(K)]
+    den = [ev[k][1].elapsed_time(ev[k][2]) for k in range(K)]
+    frc = [ev[k][2].elapsed_time(ev[k][3]) for k in range(K)]
+    step_ms = sum(ev[k][0].elapsed_time(ev[k][3]) for k in range(K)) / K
+    # the two sweeps alone, lists reused (the precomputed search's purpose)
+    xs = walk[-1].T
+    P.update(pre, xs, xs)
+    l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0.record()
+    for _ in range(K):
+        P.foreach_point_neighbor(dens, xs, xs, pre, check=False)
+        P.foreach_point_neighbor(force, xs, xs, pre, check=False)
+    l1.record()
+    torch.cuda.synchronize()
+    loops_ms = l0.elapsed_time(l1) / K
+    out = {"metric": "WCSPH pair-evals/s (8M pts, FP32, r=3, PrecomputedNeighborhoodSearch: "
+                     "update! with list rebuild + density + force)",
+           "value": 2.0 * pairs / (step_ms * K / 1e3), "unit": UNIT, "n_gpus": world,
+           "steps": K, "warmup": Wm, "ms_per_step": step_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+           "data": "synthetic (seeded perturbed lattice, numpy PCG64)",
+           "config": {"workload": f"WCSPH step, {n_side}^3 = {n:,} points, as the default "
+                                  "workload, PrecomputedNeighborhoodSearch over the grid search",
+                      "pairs_per_sweep": pairs / K},
+           "update_ms": statistics.median(upd), "density_ms": statistics.median(den),
+           "force_ms": statistics.median(frc), "loops_ms": loops_ms,
+           "loops_pair_evals_per_s": 2.0 * pairs / K / (loops_ms / 1e3),
+           "wall_ms_per_step": 1e3 * wall / K, "update_host_ms": 1e3 * upd_wall / K,
+           "gpu": torch.cuda.get_device_name()}
+    if rank == 0:
+        print(json.dumps(out))
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -793,6 +900,8 @@ def main():
             run_gpu_adjoint(args, rank, world, local)
         elif args.workload == "batched":
             run_gpu_batched(args, rank, world, local)
+        elif args.workload == "precomputed":
+            run_gpu_precomputed(args, rank, world, local)
         else:
             run_gpu_sweep(args, rank, world, local)
     finally:

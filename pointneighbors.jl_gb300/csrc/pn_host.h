@@ -139,8 +139,9 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
 template <typename T>
 int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* len,
                 int32_t* by_slot, int64_t* n_rows, cudaStream_t st);
+// cap > 0 with len: fixed capacity per row, lengths written by the same pass.
 template <typename T>
 int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* nb,
-               const int64_t* grp, cudaStream_t st);
+               const int64_t* grp, int32_t cap, int32_t* len, cudaStream_t st);
 
 }  // namespace pn

@@ -105,8 +105,47 @@ int grow(P** p, int64_t* cap, int64_t need) {
   return PN_OK;
 }
 
-// The lists of x against y (the internal search holds y).  One host synchronisation: the
-// total length decides the allocation, as the reference's resize! of the lists does.
+__global__ void k_fixed_groups(int64_t n_groups, int64_t group_size, int64_t* __restrict__ grp) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g <= n_groups) grp[g] = g * group_size;
+}
+
+void make_row_of(pn_precomputed* s, int64_t n_rows, cudaStream_t st) {
+  pn_search* g = s->grid;
+  const int32_t* n_slots = g->ovf_active ? g->d_ovf_start + g->n_total : g->d_start + g->n_total;
+  k_row_of<<<div_up(n_rows, 256), 256, 0, st>>>(g->d_perm, n_slots, n_rows, s->d_row_of); count_launch();
+}
+
+// max_neighbors > 0: the reference's fixed capacity per point (its DynamicVectorOfVectors
+// with max_neighbors rows, transposed), so one traversal writes the lists and their
+// lengths, with no counting pass and no host synchronisation; a longer row is the
+// "cell list is full" error, reported by the next synchronisation.
+template <typename T>
+int build_fixed(pn_precomputed* s, const T* x, int64_t n_x, const T* y, int64_t n_y,
+                cudaStream_t st) {
+  pn_search* g = s->grid;
+  if (!g->initialized || g->is_template) return PN_ERR_NOT_INITIALIZED;
+  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && g->full_binned;
+  const int64_t n_rows = sorted ? g->n_binned + (g->ovf_active ? g->cap : 0) : n_x;
+  const int64_t n_groups = (n_rows + 31) / 32;
+  const int64_t group_size = 32 * (int64_t)s->max_neighbors;
+  int rc = grow(&s->d_grp, &s->grp_cap, n_groups + 1);
+  if (rc == PN_OK) rc = grow(&s->d_nb, &s->nb_cap, n_groups * group_size + 1);
+  if (rc == PN_OK && sorted) rc = grow(&s->d_row_of, &s->row_of_cap, n_x + 1);
+  if (rc != PN_OK) return rc;
+  k_fixed_groups<<<div_up(n_groups + 1, 256), 256, 0, st>>>(n_groups, group_size, s->d_grp); count_launch();
+  rc = lists_emit<T>(g, x, n_x, y, n_y, s->d_nb, s->d_grp, s->max_neighbors, s->d_len, st);
+  if (rc != PN_OK) return rc;
+  if (sorted) make_row_of(s, n_rows, st);
+  s->ref = ListsRef{s->d_nb, s->d_grp, s->d_len, sorted ? s->d_row_of : nullptr,
+                    sorted ? 1 : 0, n_rows};
+  s->built = true;
+  return cuda_status(cudaGetLastError());
+}
+
+// The lists of x against y (the internal search holds y).  Without a capacity, one host
+// synchronisation: the total length decides the allocation, as the reference's resize! of
+// the lists does.
 template <typename T>
 int build_lists(pn_precomputed* s, const T* x, int64_t n_x, const T* y, int64_t n_y,
                 cudaStream_t st) {
@@ -119,6 +158,7 @@ int build_lists(pn_precomputed* s, const T* x, int64_t n_x, const T* y, int64_t 
   if (rc == PN_OK) rc = grow(&s->d_grp, &s->grp_cap, rows_max / 32 + 2);
   if (rc == PN_OK) rc = grow(&s->d_width, &s->width_cap, rows_max / 32 + 2);
   if (rc != PN_OK) return rc;
+  if (s->max_neighbors > 0) return build_fixed<T>(s, x, n_x, y, n_y, st);
   int32_t by_slot = 0;
   int64_t n_rows = 0;
   rc = lists_count<T>(g, x, n_x, y, n_y, s->d_len, &by_slot, &n_rows, st);
@@ -138,13 +178,12 @@ int build_lists(pn_precomputed* s, const T* x, int64_t n_x, const T* y, int64_t 
   if (rc_dev != PN_OK) return rc_dev;
   rc = grow(&s->d_nb, &s->nb_cap, *s->h_total + 1);
   if (rc != PN_OK) return rc;
-  rc = lists_emit<T>(g, x, n_x, y, n_y, s->d_nb, s->d_grp, st);
+  rc = lists_emit<T>(g, x, n_x, y, n_y, s->d_nb, s->d_grp, 0, nullptr, st);
   if (rc != PN_OK) return rc;
   if (by_slot) {
     rc = grow(&s->d_row_of, &s->row_of_cap, n_x + 1);
     if (rc != PN_OK) return rc;
-    const int32_t* n_slots = g->ovf_active ? g->d_ovf_start + g->n_total : g->d_start + g->n_total;
-    k_row_of<<<div_up(n_rows, 256), 256, 0, st>>>(g->d_perm, n_slots, n_rows, s->d_row_of); count_launch();
+    make_row_of(s, n_rows, st);
   }
   s->ref = ListsRef{s->d_nb, s->d_grp, s->d_len, by_slot ? s->d_row_of : nullptr, by_slot, n_rows};
   s->built = true;

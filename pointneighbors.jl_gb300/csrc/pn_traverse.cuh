@@ -247,28 +247,39 @@ struct FEmit {
 // The precomputed search's list build: every accepted candidate slot, in traversal order
 // (ascending slots), into the query row's transposed list; the row lengths come from a
 // counting pass over the same search.
+// With `len`, the lists have a fixed capacity `cap` per row (groups of 32 rows at grp[g] =
+// 32 cap g) and the emitting pass also writes the row lengths, flagging rows longer than
+// the capacity (the reference's "cell list is full"); without, the rows were sized by a
+// counting pass.
 template <typename T> struct EmitListParams {
-  int32_t* nb; const int64_t* grp; int32_t by_slot;
+  int32_t* nb; const int64_t* grp; int32_t by_slot; int32_t cap; int32_t* len; int32_t* err;
 };
 
 template <typename T, int D>
 struct FEmitList {
   static constexpr bool kCountOnly = false;
-  static constexpr bool kInline = false;
+  static constexpr bool kInline = true;  // a store per accepted candidate: no compaction
   using Params = EmitListParams<T>;
   static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
-  struct Acc { int64_t o; };
+  struct Acc { int64_t o; int32_t n; };
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
     const int32_t r = p.by_slot ? q.k : q.q;
     a.o = p.grp[r >> 5] + (r & 31);
+    a.n = 0;
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T*, T, T) {
-    p.nb[a.o] = js;
+    if (p.len == nullptr || a.n < p.cap) p.nb[a.o] = js;
     a.o += 32;
+    ++a.n;
   }
-  static __device__ __forceinline__ void finish(Acc&, const Params&, const Query<T, D>&) {}
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
+    if (p.len == nullptr) return;
+    const int32_t r = p.by_slot ? q.k : q.q;
+    p.len[r] = min(a.n, p.cap);
+    if (a.n > p.cap) set_error(p.err, PN_ERR_CELL_FULL);
+  }
 };
 
 // benchmarks/n_body.jl:41-56

@@ -8,5 +8,5 @@ template int foreach<float>(pn_search*, int32_t, const float*, int64_t, const fl
 template int lists_count<float>(pn_search*, const float*, int64_t, const float*, int64_t,
                                 int32_t*, int32_t*, int64_t*, cudaStream_t);
 template int lists_emit<float>(pn_search*, const float*, int64_t, const float*, int64_t,
-                               int32_t*, const int64_t*, cudaStream_t);
+                               int32_t*, const int64_t*, int32_t, int32_t*, cudaStream_t);
 }  // namespace pn

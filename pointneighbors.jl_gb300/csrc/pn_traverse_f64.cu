@@ -8,5 +8,5 @@ template int foreach<double>(pn_search*, int32_t, const double*, int64_t, const 
 template int lists_count<double>(pn_search*, const double*, int64_t, const double*, int64_t,
                                  int32_t*, int32_t*, int64_t*, cudaStream_t);
 template int lists_emit<double>(pn_search*, const double*, int64_t, const double*, int64_t,
-                                int32_t*, const int64_t*, cudaStream_t);
+                               int32_t*, const int64_t*, int32_t, int32_t*, cudaStream_t);
 }  // namespace pn

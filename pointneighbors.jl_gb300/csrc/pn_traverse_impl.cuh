@@ -384,11 +384,14 @@ int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, 
 
 template <typename T>
 int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* nb,
-               const int64_t* grp, cudaStream_t st) {
+               const int64_t* grp, int32_t cap, int32_t* len, cudaStream_t st) {
+  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
+  if (n_y != s->n_y || n_x < 0) return PN_ERR_INVALID_ARG;
   const bool sorted = (const void*)x == (const void*)y && n_x == n_y && s->full_binned;
   TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
-  EmitListParams<T> p{nb, grp, sorted ? 1 : 0};
+  if (len != nullptr && sorted) cudaMemsetAsync(len, 0, sizeof(int32_t) * n_sorted, st);
+  EmitListParams<T> p{nb, grp, sorted ? 1 : 0, cap, len, s->d_err};
   return launch_trav<T, FEmitList>(s, a, p, sorted, sorted ? n_sorted : n_x, st);
 }
 
