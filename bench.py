@@ -60,6 +60,9 @@ def parse():
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
     ap.add_argument("--cpu-sample", type=int, default=400_000,
                     help="query points in the CPU baseline sample")
+    ap.add_argument("--pair-cache", type=int, default=320,
+                    help="pair cache capacity (neighbours per point) of the grid search in "
+                         "the WCSPH workload; 0 = off")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",
@@ -182,7 +185,8 @@ def run_gpu(args, rank, world, local):
     cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt), max_corner=np.full(3, n_side + 1.0, dt),
                             search_radius=r, max_points_per_cell=0)
     nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
-                                   update_strategy=P.ParallelIncrementalUpdate())
+                                   update_strategy=P.ParallelIncrementalUpdate(),
+                                   pair_cache=args.pair_cache)
     x0d = torch.as_tensor(x0, device="cuda").T
     vd = torch.as_tensor(v, device="cuda").reshape(-1)
     rho = torch.zeros(n, dtype=tdt, device="cuda")
@@ -377,6 +381,7 @@ def run_gpu(args, rank, world, local):
                                "random walk N(0,0.05^2) per step, ParallelIncrementalUpdate",
                    "n_points": n, "search_radius": 3.0,
                    "pairs_per_sweep": pairs_per_sweep,
+                   "pair_cache": args.pair_cache,
                    "parallelism": f"replicas x{world}",
                    "l2": "working set > L2 (coordinates, sorted copies and outputs ~1 GB), no flush"},
         "update_ms": statistics.median(upd), "density_ms": statistics.median(den),

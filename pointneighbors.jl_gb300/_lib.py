@@ -115,6 +115,7 @@ _SIGNATURES = {
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),
     "pn_destroy": (C.c_int, [_P]),
     "pn_set_rebuild_fraction": (C.c_int, [_P, C.c_double]),
+    "pn_set_pair_cache": (C.c_int, [_P, C.c_int32]),
     "pn_initialize": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P]),
     "pn_update": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, C.c_int32, _P]),
     "pn_foreach_point_neighbor": (C.c_int, [_P, C.c_int32, _P, C.c_int64, _P, C.c_int64,

@@ -224,6 +224,13 @@ int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points
   return rc;
 }
 
+int pn_set_pair_cache(pn_search* s, int32_t max_neighbors) {
+  if (!s || max_neighbors < 0) return PN_ERR_INVALID_ARG;
+  s->pc_cap = max_neighbors;
+  s->pc_valid = false;
+  return PN_OK;
+}
+
 int pn_set_rebuild_fraction(pn_search* s, double fraction) {
   if (!s || !(fraction >= 0.0)) return PN_ERR_INVALID_ARG;
   s->rebuild_fraction = fraction;
@@ -235,7 +242,8 @@ int pn_destroy(pn_search* s) {
   free_points(s);
   void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
-                  s->d_part,       s->d_sort_tmp,   s->d_sum_part};
+                  s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_nb,
+                  s->d_pc_grp,     s->d_pc_len};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->h_ovf_n) cudaFreeHost(s->h_ovf_n);

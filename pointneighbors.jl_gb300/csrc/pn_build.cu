@@ -457,6 +457,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
     launch_finalize<T>(s, y, (int32_t)m, st);
   }
   s->n_binned = m;
+  s->pc_valid = false;
   s->ovf_active = false;
   s->main_perm_valid = false;
   s->n_ovf = 0;
@@ -567,6 +568,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   k_reset_overflow<<<152 * 4, 256, 0, st>>>(s->d_start, s->n_total, s->d_perm, s->d_main_perm,
                                             s->d_ovf_start, s->d_ovf_n, gate); count_launch();
   s->ovf_active = true;
+  s->pc_valid = false;
   // The mover count feeds the rebuild policy of the next update; it is read back lazily.
   cudaMemcpyAsync(s->h_ovf_n, s->d_ovf_n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   cudaEventRecord(s->ev_ovf, st);

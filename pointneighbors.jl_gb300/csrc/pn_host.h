@@ -70,6 +70,18 @@ struct pn_search {
   double rebuild_fraction = 0.01;      // full rebuild when movers exceed this fraction
   int32_t updates_since_build = 0;
 
+  // pair cache (opt-in, pn_set_pair_cache): the neighbour lists of the cell-sorted queries,
+  // written by the first density sweep after a build and walked by the sweeps after it
+  int32_t pc_cap = 0;                // entries per row (0: off)
+  bool pc_valid = false;
+  int32_t* d_pc_nb = nullptr;
+  int64_t pc_nb_cap = 0;
+  int64_t* d_pc_grp = nullptr;
+  int64_t pc_grp_cap = 0;
+  int32_t* d_pc_len = nullptr;       // -1: the row did not fit (walked by the grid instead)
+  int64_t pc_len_cap = 0;
+  int64_t pc_rows = 0;
+
   // state
   bool initialized = false;
   bool full_binned = false;   // every point of y is binned (no eachindex_y subset)

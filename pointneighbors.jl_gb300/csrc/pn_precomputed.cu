@@ -52,7 +52,7 @@ k_group_width(const int32_t* __restrict__ len, int64_t n_rows, int32_t max_nb,
   int32_t m = v;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0 && r < n_rows) width[r >> 5] = 32 * m;
+  if ((threadIdx.x & 31) == 0 && r < n_rows) width[r >> 5] = 32 * ((m + 3) & ~3);  // quads
 }
 
 __global__ void __launch_bounds__(256)
@@ -81,9 +81,9 @@ k_export_rows(const int32_t* __restrict__ len, const int32_t* __restrict__ row_o
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || off[n] > capacity) return;  // nothing is written when the lists do not fit
   const int32_t r = row_of ? row_of[i] : (int32_t)i;
-  const int32_t* row = nb + grp[r >> 5] + (r & 31);
+  const int32_t* row = nb + grp[r >> 5] + 4 * (r & 31);  // quads of 4 entries, 128 apart
   const int64_t o = off[i];
-  for (int32_t t = 0; t < len[r]; ++t) out[o + t] = perm[row[32 * t]];
+  for (int32_t t = 0; t < len[r]; ++t) out[o + t] = perm[row[128 * (t >> 2) + (t & 3)]];
 }
 
 __global__ void k_check_export(const int64_t* total, int64_t capacity, int32_t* err) {
@@ -128,7 +128,7 @@ int build_fixed(pn_precomputed* s, const T* x, int64_t n_x, const T* y, int64_t 
   const bool sorted = (const void*)x == (const void*)y && n_x == n_y && g->full_binned;
   const int64_t n_rows = sorted ? g->n_binned + (g->ovf_active ? g->cap : 0) : n_x;
   const int64_t n_groups = (n_rows + 31) / 32;
-  const int64_t group_size = 32 * (int64_t)s->max_neighbors;
+  const int64_t group_size = 32 * (int64_t)((s->max_neighbors + 3) & ~3);  // whole quads
   int rc = grow(&s->d_grp, &s->grp_cap, n_groups + 1);
   if (rc == PN_OK) rc = grow(&s->d_nb, &s->nb_cap, n_groups * group_size + 1);
   if (rc == PN_OK && sorted) rc = grow(&s->d_row_of, &s->row_of_cap, n_x + 1);

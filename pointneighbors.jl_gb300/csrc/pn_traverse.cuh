@@ -48,13 +48,17 @@ struct TravArgs {
   // rounding of the cell edges, so the clipped run is always a superset of the neighbours.
   const int32_t* unsorted;
   T clip_m[3];
-  // Precomputed neighbour lists (or null: the grid traversal).  Row r's t-th neighbour slot
-  // is nb[nb_grp[r / 32] + 32 t + r % 32] (groups of 32 rows stored transposed, so a warp
-  // reads its rows' t-th entries in one coalesced load); nb_len[r] entries per row.
+  // Precomputed neighbour lists (or null: the grid traversal).  Groups of 32 rows are stored
+  // transposed in quads: row r's entries 4k..4k+3 are the int4 at
+  // nb[nb_grp[r / 32] + 128 k + 4 (r % 32)], so a warp reads its rows' k-th quads in one
+  // coalesced 512-byte load; nb_len[r] entries per row (nb_grp is a multiple of 4).
   const int32_t* nb;
   const int64_t* nb_grp;
   const int32_t* nb_len;
   const int32_t* nb_row_of;  // query point -> its row (lists built by slot), or null: row = point
+  // pair cache: rows that did not fit have length -1; the list kernel skips them and a grid
+  // launch with nb = null and nb_len set traverses exactly those rows
+  int32_t nb_fallback;
 };
 
 template <typename T, int D>
@@ -245,14 +249,17 @@ struct FEmit {
 };
 
 // The precomputed search's list build: every accepted candidate slot, in traversal order
-// (ascending slots), into the query row's transposed list; the row lengths come from a
-// counting pass over the same search.
+// (ascending slots), into the query row's transposed list, a quad (int4) at a time.
 // With `len`, the lists have a fixed capacity `cap` per row (groups of 32 rows at grp[g] =
 // 32 cap g) and the emitting pass also writes the row lengths, flagging rows longer than
 // the capacity (the reference's "cell list is full"); without, the rows were sized by a
 // counting pass.
 template <typename T> struct EmitListParams {
-  int32_t* nb; const int64_t* grp; int32_t by_slot; int32_t cap; int32_t* len; int32_t* err;
+  int32_t* nb; const int64_t* grp; int32_t by_slot;
+  int32_t cap;    // entries a row has room for (a multiple of 4), with `len`
+  int32_t limit;  // max_neighbors: a longer row is an error ...
+  int32_t* len; int32_t* err;
+  int32_t fallback;  // ... or, with fallback, gets length -1 (walked through the stencil)
 };
 
 template <typename T, int D>
@@ -262,23 +269,65 @@ struct FEmitList {
   using Params = EmitListParams<T>;
   static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
-  struct Acc { int64_t o; int32_t n; };
+  struct Acc { int64_t o; int32_t n; int4 quad; };
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
     const int32_t r = p.by_slot ? q.k : q.q;
-    a.o = p.grp[r >> 5] + (r & 31);
+    a.o = p.grp[r >> 5] / 4 + (r & 31);  // int4 index of the row's first quad
     a.n = 0;
+    a.quad = make_int4(-1, -1, -1, -1);
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T*, T, T) {
-    if (p.len == nullptr || a.n < p.cap) p.nb[a.o] = js;
-    a.o += 32;
+    const int e = a.n & 3;
+    a.quad.x = e == 0 ? js : a.quad.x;
+    a.quad.y = e == 1 ? js : a.quad.y;
+    a.quad.z = e == 2 ? js : a.quad.z;
+    a.quad.w = e == 3 ? js : a.quad.w;
     ++a.n;
+    if (e == 3) {
+      if (p.len == nullptr || a.n <= p.cap) reinterpret_cast<int4*>(p.nb)[a.o] = a.quad;
+      a.o += 32;
+    }
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
+    if ((a.n & 3) && (p.len == nullptr || a.n <= p.cap))
+      reinterpret_cast<int4*>(p.nb)[a.o] = a.quad;  // the last, partial quad
     if (p.len == nullptr) return;
     const int32_t r = p.by_slot ? q.k : q.q;
-    p.len[r] = min(a.n, p.cap);
-    if (a.n > p.cap) set_error(p.err, PN_ERR_CELL_FULL);
+    p.len[r] = a.n > p.limit && p.fallback ? -1 : min(a.n, p.cap);
+    if (a.n > p.limit && !p.fallback) set_error(p.err, PN_ERR_CELL_FULL);
+  }
+};
+
+// A pair function that also stores the accepted candidates into the pair cache: both see
+// the same accepted candidates in the same order.
+template <class PF, typename T>
+struct EmitPairParams {
+  PF f;
+  EmitListParams<T> e;
+};
+
+template <typename T, int D, class F>
+struct WithEmit {
+  using E = FEmitList<T, D>;
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = F::kInline;
+  using Params = EmitPairParams<typename F::Params, T>;  // the same type for every D
+  struct Acc { typename F::Acc f; typename E::Acc e; };
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
+  static __device__ __forceinline__ void fail(const Params& p, const Query<T, D>& q) { F::fail(p.f, q); }
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
+    F::init(a.f, p.f, q);
+    E::init(a.e, p.e, q);
+  }
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>& q,
+                                              int32_t js, const T* pd, T d2, T aux) {
+    F::pair(a.f, p.f, q, js, pd, d2, aux);
+    E::pair(a.e, p.e, q, js, pd, d2, aux);
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
+    F::finish(a.f, p.f, q);
+    E::finish(a.e, p.e, q);
   }
 };
 
@@ -554,6 +603,10 @@ struct FAdjointBackward {
     for (int k = 0; k < D; ++k) p.grad[(int64_t)q.i * D + k] = sc * a.a[k];
   }
 };
+
+// Pair functions that build the pair cache while they run.
+template <typename T, int D> using FDensityEmit = WithEmit<T, D, FDensity<T, D>>;
+template <typename T, int D> using FAdjointForwardEmit = WithEmit<T, D, FAdjointForward<T, D>>;
 
 // ================================================================== traversal kernel
 __device__ __forceinline__ int32_t pwrap(int32_t c, int32_t nc) {
@@ -914,6 +967,7 @@ k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
   q.i = valid ? a.perm[k] : -1;
   if (valid && q.i < 0) F::vacant(p, (int32_t)k);
   valid = valid && q.i >= 0;
+  if (a.nb_len != nullptr && valid) valid = __ldg(&a.nb_len[k]) < 0;  // pair-cache rows only
   q.q = q.i;
   q.k = (int32_t)k;
   int32_t c[3] = {1, 1, 1};
@@ -979,14 +1033,22 @@ __device__ __forceinline__ void list_query(const TravArgs<T>& a, const typename 
   if (!valid) return;
   F::init(acc, p, q);
   const int32_t n = __ldg(&a.nb_len[row]);
-  const int32_t* nb = a.nb + __ldg(&a.nb_grp[row >> 5]) + (row & 31);
-#pragma unroll 2
-  for (int32_t t = 0; t < n; ++t) {
-    const int32_t js = __ldg(&nb[32 * t]);
-    T yj[D], pd[D];
-    const T aux = load_cand<T, D>(a.pos, js, yj);
-    const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
-    F::pair(acc, p, q, js, pd, d2, aux);
+  const int4* nb = reinterpret_cast<const int4*>(a.nb) + __ldg(&a.nb_grp[row >> 5]) / 4 +
+                   (row & 31);
+  for (int32_t t = 0; t < n; t += 4) {
+    const int4 quad = __ldg(&nb[8 * t]);  // quad t / 4 of the row: 32 int4 further per quad
+    const int32_t js4[4] = {quad.x, quad.y, quad.z, quad.w};
+    const int m = min(4, n - t);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      if (e < m) {
+        const int32_t js = js4[e];
+        T yj[D], pd[D];
+        const T aux = load_cand<T, D>(a.pos, js, yj);
+        const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
+        F::pair(acc, p, q, js, pd, d2, aux);
+      }
+    }
   }
   F::finish(acc, p, q);
 }
@@ -997,6 +1059,7 @@ __global__ void __launch_bounds__(TRAV_THREADS, 8)
 k_lists_sorted(const TravArgs<T> a, const typename F::Params p) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
+  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
   Query<T, D> q;
   bool valid = k < n_slots;
   q.i = valid ? a.perm[k] : -1;
@@ -1005,6 +1068,7 @@ k_lists_sorted(const TravArgs<T> a, const typename F::Params p) {
   q.q = q.i;
   q.k = (int32_t)k;
   if (valid) load_pos<T, D>(a.pos, k, q.x);
+  if (valid && __ldg(&a.nb_len[k]) < 0) return;  // the grid launch after this one
   list_query<T, D, PER, F>(a, p, q, (int32_t)k, valid);
 }
 

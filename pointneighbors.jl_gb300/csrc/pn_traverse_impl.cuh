@@ -102,6 +102,43 @@ k_sum_final(const double* __restrict__ part, int n_part, double* __restrict__ ou
   if (threadIdx.x == 0) *out = t;
 }
 
+static __global__ void k_pc_groups(int64_t n_groups, int64_t group_size, int64_t* grp) {
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g <= n_groups) grp[g] = g * group_size;
+}
+
+template <typename P>
+static int pc_grow(P** p, int64_t* cap, int64_t need) {
+  if (need <= *cap) return PN_OK;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const int64_t n = need + need / 8;
+  if (cudaMalloc(p, sizeof(P) * n) != cudaSuccess) {
+    cudaGetLastError();
+    return PN_ERR_OUT_OF_MEMORY;
+  }
+  *cap = n;
+  return PN_OK;
+}
+
+// Storage of the pair cache for n_rows sorted queries (fixed capacity per row).
+template <typename T>
+static int pc_prepare(pn_search* s, int64_t n_rows, EmitListParams<T>* pe, cudaStream_t st) {
+  const int64_t n_groups = (n_rows + 31) / 32;
+  const int32_t cap4 = (s->pc_cap + 3) & ~3;
+  const int64_t group_size = 32 * (int64_t)cap4;
+  int rc = pc_grow(&s->d_pc_grp, &s->pc_grp_cap, n_groups + 1);
+  if (rc == PN_OK) rc = pc_grow(&s->d_pc_nb, &s->pc_nb_cap, n_groups * group_size + 4);
+  if (rc == PN_OK) rc = pc_grow(&s->d_pc_len, &s->pc_len_cap, n_rows + 1);
+  if (rc != PN_OK) return rc;
+  k_pc_groups<<<div_up(n_groups + 1, 256), 256, 0, st>>>(n_groups, group_size, s->d_pc_grp); count_launch();
+  cudaMemsetAsync(s->d_pc_len, 0, sizeof(int32_t) * n_rows, st);  // vacated slots
+  *pe = EmitListParams<T>{s->d_pc_nb, s->d_pc_grp, 1, cap4, s->pc_cap, s->d_pc_len, s->d_err, 1};
+  s->pc_rows = n_rows;
+  return PN_OK;
+}
+
 template <typename T, template <typename, int> class F>
 static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename F<T, 1>::Params& p,
                        bool sorted, int64_t n_launch, cudaStream_t st) {
@@ -134,6 +171,13 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
     default: return PN_ERR_INVALID_ARG;
   }
 #undef PN_TRAV_CASE
+  if (a.nb != nullptr && a.nb_fallback && sorted) {
+    // rows that did not fit the pair cache: the stencil traversal, for those rows only
+    TravArgs<T> g = a;
+    g.nb = nullptr;
+    g.nb_fallback = 0;
+    return launch_trav<T, F>(s, g, p, sorted, n_launch, st);
+  }
   return cuda_status(cudaGetLastError());
 }
 
@@ -223,6 +267,15 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
   // Sorted mode launches one thread per possible slot; the kernel reads the live count.
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   const int64_t n_launch = sorted ? n_sorted : n_q;
+  // the pair cache: walked while valid, built by a density / adjoint-forward sweep
+  const bool cache_on = lists == nullptr && sorted && s->pc_cap > 0;
+  auto use_cache = [&]() {
+    a.nb = s->d_pc_nb;
+    a.nb_grp = s->d_pc_grp;
+    a.nb_len = s->d_pc_len;
+    a.nb_fallback = 1;
+  };
+  if (cache_on && s->pc_valid) use_cache();
 
   switch (functor) {
     case PN_F_COUNT: {
@@ -285,7 +338,18 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         p.pa = static_cast<T*>(s->d_pa);
         p.pb = static_cast<T*>(s->d_pb);
       }
-      int rc = launch_trav<T, FDensity>(s, a, p, sorted, n_launch, st);
+      int rc;
+      if (cache_on && !s->pc_valid) {
+        EmitPairParams<DensityParams<T>, T> pp{p, {}};
+        rc = pc_prepare<T>(s, n_sorted, &pp.e, st);
+        if (rc == PN_OK) rc = launch_trav<T, FDensityEmit>(s, a, pp, sorted, n_launch, st);
+        if (rc == PN_OK) {
+          s->pc_valid = true;
+          use_cache();
+        }
+      } else {
+        rc = launch_trav<T, FDensity>(s, a, p, sorted, n_launch, st);
+      }
       if (rc != PN_OK || !step) return rc;
       ForceParams<T> pf{p.c, static_cast<const T*>(s->d_pa), static_cast<const T*>(s->d_pb),
                         static_cast<T*>(u->accel)};
@@ -336,7 +400,14 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         if (rc != PN_OK) return rc;
         p.density = static_cast<T*>(u->density);
         p.terms = static_cast<T*>(u->terms);
-        rc = launch_trav<T, FAdjointForward>(s, a, p, sorted, n_launch, st);
+        if (cache_on && !s->pc_valid) {
+          EmitPairParams<AdjointParams<T>, T> pp{p, {}};
+          rc = pc_prepare<T>(s, n_sorted, &pp.e, st);
+          if (rc == PN_OK) rc = launch_trav<T, FAdjointForwardEmit>(s, a, pp, sorted, n_launch, st);
+          if (rc == PN_OK) s->pc_valid = true;
+        } else {
+          rc = launch_trav<T, FAdjointForward>(s, a, p, sorted, n_launch, st);
+        }
         if (rc != PN_OK) return rc;
         k_sum_partials<T><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
         k_sum_final<<<1, 256, 0, st>>>(s->d_sum_part, SUM_BLOCKS, u->loss); count_launch();
@@ -391,7 +462,7 @@ int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, i
   TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   if (len != nullptr && sorted) cudaMemsetAsync(len, 0, sizeof(int32_t) * n_sorted, st);
-  EmitListParams<T> p{nb, grp, sorted ? 1 : 0, cap, len, s->d_err};
+  EmitListParams<T> p{nb, grp, sorted ? 1 : 0, (cap + 3) & ~3, cap, len, s->d_err};
   return launch_trav<T, FEmitList>(s, a, p, sorted, sorted ? n_sorted : n_x, st);
 }
 

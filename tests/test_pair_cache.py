@@ -1,0 +1,110 @@
+"""The pair cache of the grid search (pn_set_pair_cache): a density sweep stores the
+neighbour lists and the following sweeps walk them.  Against the same search without the
+cache: counts and neighbour lists bit-exact, the density bit-exact (the same sweep), the
+force and the adjoint gradient within the FP32 tolerance of the tests (1e-5 of sum |terms|
+for the force against the FP64 oracle; 1e-4 of max |dL/dx| for the gradient); rows that
+do not fit the capacity, and update!, are covered."""
+import numpy as np
+import pytest
+import torch
+
+from test_gpu_parity import dcoords, _rel_err, TOL_F32
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def P(pkg):
+    import __graft_entry__
+    __graft_entry__.build()
+    return pkg
+
+
+def _nhs(P, n, side, cache, strategy=None):
+    r = np.float32(3.0)
+    cl = P.FullGridCellList(min_corner=np.full(3, -1.0, np.float32),
+                            max_corner=np.full(3, side + 1.0, np.float32), search_radius=r,
+                            max_points_per_cell=0)
+    return P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                    update_strategy=strategy, pair_cache=cache)
+
+
+def _step(P, nhs, x, v):
+    W = P.workloads
+    n = x.shape[1]
+    rho = torch.zeros(n, device="cuda")
+    prs = torch.zeros(n, device="cuda")
+    acc = torch.zeros(3 * n, device="cuda")
+    P.foreach_point_neighbor(P.WCSPHDensity(density=rho, pressure=prs, velocity=v, **W.WCSPH),
+                             x, x, nhs)
+    P.foreach_point_neighbor(P.WCSPHForce(density=rho, pressure=prs, velocity=v, accel=acc,
+                                          reuse_state=True, **W.WCSPH), x, x, nhs)
+    cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt), x, x, nhs)
+    lists = P.neighbor_lists(x, x, nhs)
+    return rho, prs, acc, cnt, lists
+
+
+@pytest.mark.parametrize("cache", [320, 64])
+def test_pair_cache_equals_stencil(P, O, cache):
+    W = P.workloads
+    side = 22
+    x, v, dx = W.wcsph_cloud(side, seed=4, dtype=np.float32)
+    n = len(x)
+    vd = torch.as_tensor(v, device="cuda").reshape(-1)
+    ref = _nhs(P, n, side, 0, P.ParallelIncrementalUpdate())
+    pc = _nhs(P, n, side, cache, P.ParallelIncrementalUpdate())
+    for k, pos in enumerate([x, (x + dx).astype(np.float32), (x - dx).astype(np.float32)]):
+        xd = dcoords(pos)
+        if k == 0:
+            P.initialize(ref, xd, xd)
+            P.initialize(pc, xd, xd)
+        else:
+            P.update(ref, xd, xd)
+            P.update(pc, xd, xd)
+        a = _step(P, ref, xd, vd)
+        b = _step(P, pc, xd, vd)
+        assert torch.equal(a[0], b[0]) and torch.equal(a[1], b[1])  # density, pressure
+        assert torch.equal(a[3], b[3])                             # counts
+        assert torch.equal(a[4][0], b[4][0]) and torch.equal(a[4][1], b[4][1])
+        # force from the cached lists against the FP64 oracle on the same inputs
+        g = O.grid_create(3, np.float32(3.0), np.full(3, -1.0, np.float32),
+                          np.full(3, side + 1.0, np.float32), dtype=np.float32)
+        cl = O.build(g, pos)
+        c = W.WCSPH
+        prm, keep = O.make_params(rho=b[0].cpu().numpy().astype(np.float64),
+                                  pressure=b[1].cpu().numpy().astype(np.float64),
+                                  vel=v.astype(np.float64),
+                                  r_min=float(np.sqrt(np.finfo(np.float32).eps)) * c["h"], **c)
+        oacc, oab = O.foreach(g, cl, pos, pos, O.F_WCSPH_FORCE, prm, want_abs=True)
+        got = b[2].cpu().numpy().reshape(n, 3).astype(np.float64)
+        assert _rel_err(got, oacc, oab) < TOL_F32
+        want = a[2].cpu().numpy().reshape(n, 3).astype(np.float64)
+        assert _rel_err(want, oacc, oab) < TOL_F32
+
+
+def test_pair_cache_adjoint(P):
+    W = P.workloads
+    side = 16
+    x = W.perturbed_lattice((side,) * 3, 0.25, seed=6, dtype=np.float32)
+    n = len(x)
+    consts = dict(mass=1.0, h=1.5, cutoff=3.0, lambda_pot=0.01)
+    out = []
+    for cache in (0, 320):
+        nhs = _nhs(P, n, side, cache)
+        xd = dcoords(x)
+        P.initialize(nhs, xd, xd)
+        rho = torch.empty(n, device="cuda")
+        terms = torch.empty(n, device="cuda")
+        loss = torch.empty(1, dtype=torch.float64, device="cuda")
+        P.foreach_point_neighbor(P.AdjointLossForward(density=rho, terms=terms, loss=loss,
+                                                      **consts), xd, xd, nhs)
+        grad = torch.empty(3 * n, device="cuda")
+        P.foreach_point_neighbor(P.AdjointLossBackward(grad=grad, reuse_state=True, **consts),
+                                 xd, xd, nhs)
+        out.append((rho, loss, grad))
+    assert torch.equal(out[0][0], out[1][0])  # density: the same sweep
+    # the loss terms may round differently (FMA contraction in the fused sweep)
+    assert abs(float(out[0][1]) - float(out[1][1])) <= 1e-6 * abs(float(out[0][1]))
+    g0, g1 = out[0][2], out[1][2]
+    assert float((g0 - g1).abs().max() / g0.abs().max()) < 1e-4
