@@ -45,9 +45,11 @@ UNIT = "pair-evals/s"
 # point's index 4, write the acceleration 12.
 FORCE_BYTES_PER_POINT = {"float32": 44, "float64": 84}
 # DRAM bytes per point of one force sweep measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, 4,096,000-point capture of the same workload; the ncu summary is
-# profiles/trav_force_density_wcsph_4M.md).
-FORCE_TRAFFIC_BYTES_PER_POINT = {"float32": 49.1}
+# dram__bytes_write.sum, 4,096,000-point capture of the same workload): over the pair-cache
+# lists (the default) most of it is the lists themselves; without the cache (stencil) it is
+# 49.1 B/point.  The ncu summaries are profiles/density_emit_force_lists_wcsph_4M.md and
+# profiles/trav_force_density_wcsph_4M.md.
+FORCE_TRAFFIC_BYTES_PER_POINT = {("float32", True): 517.0, ("float32", False): 49.1}
 
 
 def parse():
@@ -358,14 +360,20 @@ def run_gpu(args, rank, world, local):
     t_force = statistics.median(frc) / 1e3
     alg = FORCE_BYTES_PER_POINT[args.dtype] * n
     achieved = alg / t_force / 1e9
-    roofline = {"bound": "hbm", "kernel": "k_trav_sorted<FForce> (force sweep)",
+    roofline = {"bound": "hbm",
+                "kernel": ("k_lists_sorted<FForce> (force sweep over the pair cache)"
+                           if args.pair_cache > 0 else "k_trav_sorted<FForce> (force sweep)"),
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak,
-                "traffic": (FORCE_TRAFFIC_BYTES_PER_POINT[args.dtype] * n
-                            if args.dtype in FORCE_TRAFFIC_BYTES_PER_POINT else None),
+                "traffic": (FORCE_TRAFFIC_BYTES_PER_POINT[(args.dtype, args.pair_cache > 0)] * n
+                            if (args.dtype, args.pair_cache > 0) in FORCE_TRAFFIC_BYTES_PER_POINT
+                            else None),
                 "algorithmic_bytes_per_launch": alg,
-                "note": "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
-                        "93 % (density), DRAM < 2 % of peak"}
+                "note": ("force over the pair-cache lists: L1 load path bound (ncu L1 94.6 %, "
+                         "DRAM 18 %); density + list build: issue-bound (85.7 %)"
+                         if args.pair_cache > 0 else
+                         "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
+                         "93 % (density), DRAM < 2 % of peak")}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
