@@ -62,9 +62,9 @@ def parse():
     ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
     ap.add_argument("--cpu-sample", type=int, default=400_000,
                     help="query points in the CPU baseline sample")
-    ap.add_argument("--pair-cache", type=int, default=320,
-                    help="pair cache capacity (neighbours per point) of the grid search in "
-                         "the WCSPH workload; 0 = off")
+    ap.add_argument("--pair-cache", type=int, default=1,
+                    help="1: the grid search's pair cache (the density sweep records each "
+                         "query's neighbours for the force sweep); 0: off")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",

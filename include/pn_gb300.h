@@ -226,15 +226,15 @@ int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex
  * never rebuilds. */
 int pn_set_rebuild_fraction(pn_search* s, double fraction);
 
-/* Pair cache (no counterpart in the reference; the behaviour of its
- * PrecomputedNeighborhoodSearch inside a GridNeighborhoodSearch): with max_neighbors > 0
- * the first WCSPH-density (or adjoint-forward) sweep with x is y after initialize/update
- * also stores every query's neighbour slots (up to max_neighbors per point, in 32-row
- * groups stored transposed), and the sweeps that follow, until the next initialize/update,
- * walk those lists instead of the cell stencil.  A point with more neighbours is walked
- * through the stencil as before, so results never depend on the cap.  Memory:
- * 4 x max_neighbors bytes per point.  0 (the default) turns it off. */
-int pn_set_pair_cache(pn_search* s, int32_t max_neighbors);
+/* Pair cache (no counterpart in the reference; what its PrecomputedNeighborhoodSearch does,
+ * inside a GridNeighborhoodSearch): with `enable` > 0 the first WCSPH-density (or
+ * adjoint-forward) sweep with x is y after initialize/update also records, for every query
+ * and stencil row, where the row's clipped run starts and which of its (at most 128)
+ * candidates are neighbours; the sweeps that follow, until the next initialize/update,
+ * visit exactly those.  Queries whose rows are not single clipped runs (periodic faces,
+ * incremental overflow lists, runs over 128 slots) keep the stencil, so results never depend
+ * on the cache.  Memory: 20 bytes x 3^(d-1) per slot.  0 (the default) turns it off. */
+int pn_set_pair_cache(pn_search* s, int32_t enable);
 
 /* ----------------------------------------------------------------- traversal */
 

@@ -179,11 +179,12 @@ class GridNeighborhoodSearch:
     """GridNeighborhoodSearch{ndims}(; search_radius, n_points, periodic_box, cell_list,
     update_strategy) over a FullGridCellList (nhs_grid.jl:67-129).
 
-    `pair_cache` (not in the reference): a capacity in neighbours per point.  The first
-    WCSPH-density or adjoint-forward sweep with x is y after initialize/update then also
-    stores the neighbour lists, and the sweeps that follow until the next initialize/update
-    walk them (4 x pair_cache bytes per point; points with more neighbours use the cell
-    stencil, so results do not depend on the capacity).  0 turns it off."""
+    `pair_cache` (not in the reference): when true, the first WCSPH-density or
+    adjoint-forward sweep with x is y after initialize/update also records which candidates
+    of each query's stencil rows are neighbours (a start and a 128-bit mask per row, 20 bytes
+    x 3^(d-1) per point), and the sweeps that follow until the next initialize/update visit
+    exactly those.  Queries the cache cannot describe keep the cell stencil, so results do
+    not depend on it."""
 
     def __init__(self, ndims, *, search_radius=0.0, n_points=0, periodic_box=None,
                  cell_list=None, update_strategy=None, pair_cache=0):
@@ -243,10 +244,9 @@ class GridNeighborhoodSearch:
         self._h = h
         if isinstance(update_strategy, ParallelIncrementalUpdate):
             lib().pn_set_rebuild_fraction(h, update_strategy.rebuild_fraction)
-        self.pair_cache = int(pair_cache or 0)
+        self.pair_cache = bool(pair_cache)
         if self.pair_cache:
-            if lib().pn_set_pair_cache(h, self.pair_cache) != _lib.PN_OK:
-                raise ArgumentError("`pair_cache` must be >= 0")
+            lib().pn_set_pair_cache(h, 1)
         self._cfg = cfg
 
     def __del__(self):

@@ -242,8 +242,8 @@ int pn_destroy(pn_search* s) {
   free_points(s);
   void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
-                  s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_nb,
-                  s->d_pc_grp,     s->d_pc_len};
+                  s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_b0,
+                  s->d_pc_mask};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->h_ovf_n) cudaFreeHost(s->h_ovf_n);

@@ -70,16 +70,15 @@ struct pn_search {
   double rebuild_fraction = 0.01;      // full rebuild when movers exceed this fraction
   int32_t updates_since_build = 0;
 
-  // pair cache (opt-in, pn_set_pair_cache): the neighbour lists of the cell-sorted queries,
-  // written by the first density sweep after a build and walked by the sweeps after it
-  int32_t pc_cap = 0;                // entries per row (0: off)
+  // pair cache (opt-in, pn_set_pair_cache): per cell-sorted query and stencil row, the start
+  // of the clipped run and a 128-bit mask of its neighbours, written by the first density
+  // sweep after a build and walked by the sweeps after it
+  int32_t pc_cap = 0;                   // > 0: on
   bool pc_valid = false;
-  int32_t* d_pc_nb = nullptr;
-  int64_t pc_nb_cap = 0;
-  int64_t* d_pc_grp = nullptr;
-  int64_t pc_grp_cap = 0;
-  int32_t* d_pc_len = nullptr;       // -1: the row did not fit (walked by the grid instead)
-  int64_t pc_len_cap = 0;
+  int32_t* d_pc_b0 = nullptr;           // [rows of 3^(d-1)][slots]; row 0 < 0: stencil fallback
+  int64_t pc_b0_cap = 0;
+  unsigned long long* d_pc_mask = nullptr;  // [rows][slots] x 2 words
+  int64_t pc_mask_cap = 0;
   int64_t pc_rows = 0;
 
   // state

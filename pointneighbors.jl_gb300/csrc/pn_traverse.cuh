@@ -56,9 +56,15 @@ struct TravArgs {
   const int64_t* nb_grp;
   const int32_t* nb_len;
   const int32_t* nb_row_of;  // query point -> its row (lists built by slot), or null: row = point
-  // pair cache: rows that did not fit have length -1; the list kernel skips them and a grid
-  // launch with nb = null and nb_len set traverses exactly those rows
+  // pair cache: queries that could not be cached have a negative nb_len entry; the cached
+  // walk skips them and a grid launch with the cache pointers cleared and nb_len set
+  // traverses exactly those queries
   int32_t nb_fallback;
+  // pair cache as hit masks: for query slot k and stencil row ri, the clipped run start
+  // pc_b0[ri * pc_stride + k] and a 128-bit mask of its accepted candidates
+  const int32_t* pc_b0;
+  const ulonglong2* pc_mask;
+  int64_t pc_stride;
 };
 
 template <typename T, int D>
@@ -301,33 +307,69 @@ struct FEmitList {
 
 // A pair function that also stores the accepted candidates into the pair cache: both see
 // the same accepted candidates in the same order.
-template <class PF, typename T>
-struct EmitPairParams {
+// The pair cache: a pair function that also records, per stencil row of the query, the
+// start of the row's clipped run and a bit for every accepted candidate of it (the run must
+// be at most 128 slots).  traverse_query announces every row (row_begin) when the rows are
+// clipped, contiguous runs; otherwise (periodic wrap, overflow lists) the query is marked
+// for the stencil fallback (no_rows).
+struct MaskParams {
+  int32_t* b0;
+  ulonglong2* mask;
+  int64_t stride;
+};
+template <class PF>
+struct MaskPairParams {
   PF f;
-  EmitListParams<T> e;
+  MaskParams m;
 };
 
+template <class F, class = void>
+struct has_row_hook { static constexpr bool value = false; };
+template <class F>
+struct has_row_hook<F, decltype((void)F::kRowHook)> { static constexpr bool value = F::kRowHook; };
+
 template <typename T, int D, class F>
-struct WithEmit {
-  using E = FEmitList<T, D>;
+struct WithMask {
   static constexpr bool kCountOnly = false;
   static constexpr bool kInline = F::kInline;
-  using Params = EmitPairParams<typename F::Params, T>;  // the same type for every D
-  struct Acc { typename F::Acc f; typename E::Acc e; };
+  static constexpr bool kRowHook = true;
+  using Params = MaskPairParams<typename F::Params>;  // the same type for every D
+  struct Acc { typename F::Acc f; int32_t ri, b0; uint64_t lo, hi; bool fb; };
   static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
   static __device__ __forceinline__ void fail(const Params& p, const Query<T, D>& q) { F::fail(p.f, q); }
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
     F::init(a.f, p.f, q);
-    E::init(a.e, p.e, q);
+    a.ri = -1;
+    a.b0 = 0;
+    a.lo = a.hi = 0;
+    a.fb = false;
   }
+  static __device__ __forceinline__ void flush(Acc& a, const Params& p, const Query<T, D>& q) {
+    if (a.ri < 0) return;
+    const int64_t o = (int64_t)a.ri * p.m.stride + q.k;
+    p.m.b0[o] = a.b0;
+    p.m.mask[o] = make_ulonglong2(a.lo, a.hi);
+  }
+  static __device__ __forceinline__ void row_begin(Acc& a, const Params& p, const Query<T, D>& q,
+                                                   int ri, int32_t b0, int32_t e0) {
+    flush(a, p, q);
+    a.ri = ri;
+    a.b0 = b0;
+    a.lo = a.hi = 0;
+    if (e0 - b0 > 128) a.fb = true;
+  }
+  static __device__ __forceinline__ void no_rows(Acc& a) { a.fb = true; }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>& q,
                                               int32_t js, const T* pd, T d2, T aux) {
     F::pair(a.f, p.f, q, js, pd, d2, aux);
-    E::pair(a.e, p.e, q, js, pd, d2, aux);
+    const uint32_t off = (uint32_t)(js - a.b0);
+    if (off < 64) a.lo |= 1ull << off;
+    else if (off < 128) a.hi |= 1ull << (off - 64);
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     F::finish(a.f, p.f, q);
-    E::finish(a.e, p.e, q);
+    flush(a, p, q);
+    if (a.fb) p.m.b0[q.k] = -1;  // row 0's entry marks the query for the stencil fallback
   }
 };
 
@@ -605,8 +647,8 @@ struct FAdjointBackward {
 };
 
 // Pair functions that build the pair cache while they run.
-template <typename T, int D> using FDensityEmit = WithEmit<T, D, FDensity<T, D>>;
-template <typename T, int D> using FAdjointForwardEmit = WithEmit<T, D, FAdjointForward<T, D>>;
+template <typename T, int D> using FDensityMask = WithMask<T, D, FDensity<T, D>>;
+template <typename T, int D> using FAdjointForwardMask = WithMask<T, D, FAdjointForward<T, D>>;
 
 // ================================================================== traversal kernel
 __device__ __forceinline__ int32_t pwrap(int32_t c, int32_t nc) {
@@ -908,6 +950,9 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
   // row clipping (see TravArgs): the query's distance to the lower and upper edge of its
   // cell in y and z, reduced by the margin; rows near a periodic face are not clipped
   const bool clip = valid && !(PER && wrap) && (a.unsorted == nullptr || *a.unsorted == 0);
+  if constexpr (has_row_hook<F>::value) {
+    if (valid && !clip) F::no_rows(acc);  // rows are not single clipped runs here
+  }
   T below[3] = {(T)0, (T)0, (T)0}, above[3] = {(T)0, (T)0, (T)0};
   if (clip) {
 #pragma unroll
@@ -932,6 +977,8 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
         int32_t b0 = __ldg(&a.start[l0]), e0 = __ldg(&a.start[l0 + 3]);
         if (clip) {
           clip_row<T, D>(a, q, below, above, oy, oz, b0, e0);
+          if constexpr (has_row_hook<F>::value)
+            F::row_begin(acc, p, q, (oz + OZ) * (2 * OY + 1) + (oy + OY), b0, e0);
           if (b0 >= e0) continue;  // no point of this row is within r
         }
         scan_any<T, D, PER, F>(a, p, acc, q, wrap, b0, e0);
@@ -1070,6 +1117,59 @@ k_lists_sorted(const TravArgs<T> a, const typename F::Params p) {
   if (valid) load_pos<T, D>(a.pos, k, q.x);
   if (valid && __ldg(&a.nb_len[k]) < 0) return;  // the grid launch after this one
   list_query<T, D, PER, F>(a, p, q, (int32_t)k, valid);
+}
+
+// Cell-sorted queries over the pair cache's hit masks: for every stencil row, the accepted
+// candidates of the row's clipped run, in slot order; queries marked for the fallback are
+// left to the stencil launch after this one.
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
+  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
+  Query<T, D> q;
+  bool valid = k < n_slots;
+  q.i = valid ? a.perm[k] : -1;
+  if (valid && q.i < 0) F::vacant(p, (int32_t)k);
+  valid = valid && q.i >= 0;
+  if (!valid || __ldg(&a.pc_b0[k]) < 0) return;
+  q.q = q.i;
+  q.k = (int32_t)k;
+  load_pos<T, D>(a.pos, k, q.x);
+  typename F::Acc acc;
+  F::init(acc, p, q);
+  constexpr int NR = D == 3 ? 9 : (D == 2 ? 3 : 1);
+  // One loop over all the query's neighbours (row by row, low then high word): a lane moves
+  // to its next mask word when it has used up the current one, so lanes with different
+  // counts per row do not wait for one another row by row.
+  // wi = 2 row + half indexes the query's 2 NR mask words
+  int wi = 0;
+  int32_t rb0 = __ldg(&a.pc_b0[k]);
+  ulonglong2 m = __ldg(&a.pc_mask[k]);
+  uint64_t w = m.x;
+  for (;;) {
+    while (w == 0) {
+      if (++wi >= 2 * NR) break;
+      if (wi & 1) {
+        w = m.y;
+      } else {
+        const int64_t o = (int64_t)(wi >> 1) * a.pc_stride + k;
+        rb0 = __ldg(&a.pc_b0[o]);
+        m = __ldg(&a.pc_mask[o]);
+        w = m.x;
+      }
+    }
+    if (w == 0) break;
+    const int e = __ffsll((long long)w) - 1;
+    w &= w - 1;
+    const int32_t js = rb0 + 64 * (wi & 1) + e;
+    T yj[D], pd[D];
+    const T aux = load_cand<T, D>(a.pos, js, yj);
+    const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
+    F::pair(acc, p, q, js, pd, d2, aux);
+  }
+  F::finish(acc, p, q);
 }
 
 // Queries x[:, qlist[t]] (or t) in the given order: row = t.

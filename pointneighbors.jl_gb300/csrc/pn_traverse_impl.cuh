@@ -102,11 +102,6 @@ k_sum_final(const double* __restrict__ part, int n_part, double* __restrict__ ou
   if (threadIdx.x == 0) *out = t;
 }
 
-static __global__ void k_pc_groups(int64_t n_groups, int64_t group_size, int64_t* grp) {
-  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g <= n_groups) grp[g] = g * group_size;
-}
-
 template <typename P>
 static int pc_grow(P** p, int64_t* cap, int64_t need) {
   if (need <= *cap) return PN_OK;
@@ -122,19 +117,13 @@ static int pc_grow(P** p, int64_t* cap, int64_t need) {
   return PN_OK;
 }
 
-// Storage of the pair cache for n_rows sorted queries (fixed capacity per row).
-template <typename T>
-static int pc_prepare(pn_search* s, int64_t n_rows, EmitListParams<T>* pe, cudaStream_t st) {
-  const int64_t n_groups = (n_rows + 31) / 32;
-  const int32_t cap4 = (s->pc_cap + 3) & ~3;
-  const int64_t group_size = 32 * (int64_t)cap4;
-  int rc = pc_grow(&s->d_pc_grp, &s->pc_grp_cap, n_groups + 1);
-  if (rc == PN_OK) rc = pc_grow(&s->d_pc_nb, &s->pc_nb_cap, n_groups * group_size + 4);
-  if (rc == PN_OK) rc = pc_grow(&s->d_pc_len, &s->pc_len_cap, n_rows + 1);
+// Storage of the pair cache for n_rows sorted queries: 3^(d-1) stencil rows each.
+static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m) {
+  const int64_t nr = s->ndims == 3 ? 9 : (s->ndims == 2 ? 3 : 1);
+  int rc = pc_grow(&s->d_pc_b0, &s->pc_b0_cap, nr * n_rows + 1);
+  if (rc == PN_OK) rc = pc_grow(&s->d_pc_mask, &s->pc_mask_cap, 2 * (nr * n_rows + 1));
   if (rc != PN_OK) return rc;
-  k_pc_groups<<<div_up(n_groups + 1, 256), 256, 0, st>>>(n_groups, group_size, s->d_pc_grp); count_launch();
-  cudaMemsetAsync(s->d_pc_len, 0, sizeof(int32_t) * n_rows, st);  // vacated slots
-  *pe = EmitListParams<T>{s->d_pc_nb, s->d_pc_grp, 1, cap4, s->pc_cap, s->d_pc_len, s->d_err, 1};
+  *m = MaskParams{s->d_pc_b0, reinterpret_cast<ulonglong2*>(s->d_pc_mask), n_rows};
   s->pc_rows = n_rows;
   return PN_OK;
 }
@@ -147,7 +136,10 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
   const int key = s->ndims * 2 + (s->periodic ? 1 : 0);
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
-    if (a.nb != nullptr) {                                                              \
+    if (a.pc_mask != nullptr && sorted) {                                               \
+      k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);       \
+      count_launch();                                                                   \
+    } else if (a.nb != nullptr) {                                                       \
       if (sorted)                                                                       \
         k_lists_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
       else                                                                              \
@@ -171,10 +163,12 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
     default: return PN_ERR_INVALID_ARG;
   }
 #undef PN_TRAV_CASE
-  if (a.nb != nullptr && a.nb_fallback && sorted) {
-    // rows that did not fit the pair cache: the stencil traversal, for those rows only
+  if ((a.nb != nullptr || a.pc_mask != nullptr) && a.nb_fallback && sorted) {
+    // queries the pair cache could not hold: the stencil traversal, for those only
     TravArgs<T> g = a;
     g.nb = nullptr;
+    g.pc_mask = nullptr;
+    g.pc_b0 = nullptr;
     g.nb_fallback = 0;
     return launch_trav<T, F>(s, g, p, sorted, n_launch, st);
   }
@@ -270,9 +264,10 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
   // the pair cache: walked while valid, built by a density / adjoint-forward sweep
   const bool cache_on = lists == nullptr && sorted && s->pc_cap > 0;
   auto use_cache = [&]() {
-    a.nb = s->d_pc_nb;
-    a.nb_grp = s->d_pc_grp;
-    a.nb_len = s->d_pc_len;
+    a.pc_b0 = s->d_pc_b0;
+    a.pc_mask = reinterpret_cast<const ulonglong2*>(s->d_pc_mask);
+    a.pc_stride = s->pc_rows;
+    a.nb_len = s->d_pc_b0;  // row 0: negative marks the stencil fallback
     a.nb_fallback = 1;
   };
   if (cache_on && s->pc_valid) use_cache();
@@ -340,9 +335,9 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       }
       int rc;
       if (cache_on && !s->pc_valid) {
-        EmitPairParams<DensityParams<T>, T> pp{p, {}};
-        rc = pc_prepare<T>(s, n_sorted, &pp.e, st);
-        if (rc == PN_OK) rc = launch_trav<T, FDensityEmit>(s, a, pp, sorted, n_launch, st);
+        MaskPairParams<DensityParams<T>> pp{p, {}};
+        rc = pc_prepare(s, n_sorted, &pp.m);
+        if (rc == PN_OK) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
         if (rc == PN_OK) {
           s->pc_valid = true;
           use_cache();
@@ -401,9 +396,9 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         p.density = static_cast<T*>(u->density);
         p.terms = static_cast<T*>(u->terms);
         if (cache_on && !s->pc_valid) {
-          EmitPairParams<AdjointParams<T>, T> pp{p, {}};
-          rc = pc_prepare<T>(s, n_sorted, &pp.e, st);
-          if (rc == PN_OK) rc = launch_trav<T, FAdjointForwardEmit>(s, a, pp, sorted, n_launch, st);
+          MaskPairParams<AdjointParams<T>> pp{p, {}};
+          rc = pc_prepare(s, n_sorted, &pp.m);
+          if (rc == PN_OK) rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
           if (rc == PN_OK) s->pc_valid = true;
         } else {
           rc = launch_trav<T, FAdjointForward>(s, a, p, sorted, n_launch, st);

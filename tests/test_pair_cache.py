@@ -1,5 +1,6 @@
-"""The pair cache of the grid search (pn_set_pair_cache): a density sweep stores the
-neighbour lists and the following sweeps walk them.  Against the same search without the
+"""The pair cache of the grid search (pn_set_pair_cache): a density sweep records, per
+query and stencil row, which candidates are neighbours, and the following sweeps visit
+exactly those.  Against the same search without the
 cache: counts and neighbour lists bit-exact, the density bit-exact (the same sweep), the
 force and the adjoint gradient within the FP32 tolerance of the tests (1e-5 of sum |terms|
 for the force against the FP64 oracle; 1e-4 of max |dL/dx| for the gradient); rows that
@@ -20,13 +21,14 @@ def P(pkg):
     return pkg
 
 
-def _nhs(P, n, side, cache, strategy=None):
+def _nhs(P, n, side, cache, strategy=None, periodic=False):
     r = np.float32(3.0)
-    cl = P.FullGridCellList(min_corner=np.full(3, -1.0, np.float32),
-                            max_corner=np.full(3, side + 1.0, np.float32), search_radius=r,
-                            max_points_per_cell=0)
+    lo = np.full(3, 0.0 if periodic else -1.0, np.float32)
+    hi = np.full(3, side + (0.0 if periodic else 1.0), np.float32)
+    box = P.PeriodicBox(min_corner=lo, max_corner=hi) if periodic else None
+    cl = P.FullGridCellList(min_corner=lo, max_corner=hi, search_radius=r, max_points_per_cell=0)
     return P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
-                                    update_strategy=strategy, pair_cache=cache)
+                                    update_strategy=strategy, pair_cache=cache, periodic_box=box)
 
 
 def _step(P, nhs, x, v):
@@ -45,15 +47,19 @@ def _step(P, nhs, x, v):
     return rho, prs, acc, cnt, lists
 
 
-@pytest.mark.parametrize("cache", [320, 64])
-def test_pair_cache_equals_stencil(P, O, cache):
+# rebuild_fraction 1: update! keeps overflow lists, whose queries the cache cannot describe
+# (every query falls back to the stencil); periodic: queries near the faces fall back
+@pytest.mark.parametrize("fraction,periodic", [(0.01, False), (1.0, False), (0.01, True)])
+def test_pair_cache_equals_stencil(P, O, fraction, periodic):
     W = P.workloads
     side = 22
     x, v, dx = W.wcsph_cloud(side, seed=4, dtype=np.float32)
+    if periodic:
+        x = x - np.float32(0.5)  # the lattice 0.5..21.5 inside the box [0, 22)
     n = len(x)
     vd = torch.as_tensor(v, device="cuda").reshape(-1)
-    ref = _nhs(P, n, side, 0, P.ParallelIncrementalUpdate())
-    pc = _nhs(P, n, side, cache, P.ParallelIncrementalUpdate())
+    ref = _nhs(P, n, side, False, P.ParallelIncrementalUpdate(fraction), periodic)
+    pc = _nhs(P, n, side, True, P.ParallelIncrementalUpdate(fraction), periodic)
     for k, pos in enumerate([x, (x + dx).astype(np.float32), (x - dx).astype(np.float32)]):
         xd = dcoords(pos)
         if k == 0:
@@ -68,8 +74,10 @@ def test_pair_cache_equals_stencil(P, O, cache):
         assert torch.equal(a[3], b[3])                             # counts
         assert torch.equal(a[4][0], b[4][0]) and torch.equal(a[4][1], b[4][1])
         # force from the cached lists against the FP64 oracle on the same inputs
-        g = O.grid_create(3, np.float32(3.0), np.full(3, -1.0, np.float32),
-                          np.full(3, side + 1.0, np.float32), dtype=np.float32)
+        lo = np.full(3, 0.0 if periodic else -1.0, np.float32)
+        hi = np.full(3, side + (0.0 if periodic else 1.0), np.float32)
+        g = O.grid_create(3, np.float32(3.0), lo, hi, dtype=np.float32,
+                          periodic_box=(lo, hi) if periodic else None)
         cl = O.build(g, pos)
         c = W.WCSPH
         prm, keep = O.make_params(rho=b[0].cpu().numpy().astype(np.float64),
@@ -90,7 +98,7 @@ def test_pair_cache_adjoint(P):
     n = len(x)
     consts = dict(mass=1.0, h=1.5, cutoff=3.0, lambda_pot=0.01)
     out = []
-    for cache in (0, 320):
+    for cache in (False, True):
         nhs = _nhs(P, n, side, cache)
         xd = dcoords(x)
         P.initialize(nhs, xd, xd)
