@@ -171,8 +171,10 @@ static int create(const pn_config* cfg, pn_search** out) {
     delete s;
     return rc;
   }
-  bool ok = cudaMalloc(&s->d_err, sizeof(int32_t) * 4) == cudaSuccess;
-  ok = ok && cudaMemset(s->d_err, 0, sizeof(int32_t) * 4) == cudaSuccess;
+  // d_err: [0] sticky error, [1] a point outside the periodic box, [2] incremental-update
+  // decision, [3] cells not sorted by x, [4] some query needs the pair cache's fallback
+  bool ok = cudaMalloc(&s->d_err, sizeof(int32_t) * 8) == cudaSuccess;
+  ok = ok && cudaMemset(s->d_err, 0, sizeof(int32_t) * 8) == cudaSuccess;
   ok = ok && cudaMallocHost(&s->h_ovf_n, sizeof(int32_t)) == cudaSuccess;
   ok = ok && cudaEventCreateWithFlags(&s->ev_ovf, cudaEventDisableTiming) == cudaSuccess;
   if (ok && !s->is_template) {

@@ -65,6 +65,7 @@ struct TravArgs {
   const int32_t* pc_b0;
   const ulonglong2* pc_mask;
   int64_t pc_stride;
+  const int32_t* pc_any_fallback;  // device flag: some query was marked for the fallback
 };
 
 template <typename T, int D>
@@ -316,6 +317,7 @@ struct MaskParams {
   int32_t* b0;
   ulonglong2* mask;
   int64_t stride;
+  int32_t* any_fallback;
 };
 template <class PF>
 struct MaskPairParams {
@@ -369,7 +371,10 @@ struct WithMask {
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     F::finish(a.f, p.f, q);
     flush(a, p, q);
-    if (a.fb) p.m.b0[q.k] = -1;  // row 0's entry marks the query for the stencil fallback
+    if (a.fb) {
+      p.m.b0[q.k] = -1;  // row 0's entry marks the query for the stencil fallback
+      if (*(volatile int32_t*)p.m.any_fallback == 0) atomicExch(p.m.any_fallback, 1);
+    }
   }
 };
 
@@ -1009,6 +1014,8 @@ k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
   if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
+  // the pair cache's fallback launch: nothing to do unless some query was marked
+  if (a.nb_len != nullptr && a.pc_any_fallback != nullptr && *a.pc_any_fallback == 0) return;
   Query<T, D> q;
   bool valid = k < n_slots;
   q.i = valid ? a.perm[k] : -1;

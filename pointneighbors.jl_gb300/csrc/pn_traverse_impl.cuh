@@ -118,12 +118,14 @@ static int pc_grow(P** p, int64_t* cap, int64_t need) {
 }
 
 // Storage of the pair cache for n_rows sorted queries: 3^(d-1) stencil rows each.
-static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m) {
+static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m, cudaStream_t st) {
   const int64_t nr = s->ndims == 3 ? 9 : (s->ndims == 2 ? 3 : 1);
   int rc = pc_grow(&s->d_pc_b0, &s->pc_b0_cap, nr * n_rows + 1);
   if (rc == PN_OK) rc = pc_grow(&s->d_pc_mask, &s->pc_mask_cap, 2 * (nr * n_rows + 1));
   if (rc != PN_OK) return rc;
-  *m = MaskParams{s->d_pc_b0, reinterpret_cast<ulonglong2*>(s->d_pc_mask), n_rows};
+  cudaMemsetAsync(s->d_err + 4, 0, sizeof(int32_t), st);
+  *m = MaskParams{s->d_pc_b0, reinterpret_cast<ulonglong2*>(s->d_pc_mask), n_rows,
+                  s->d_err + 4};
   s->pc_rows = n_rows;
   return PN_OK;
 }
@@ -269,6 +271,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
     a.pc_stride = s->pc_rows;
     a.nb_len = s->d_pc_b0;  // row 0: negative marks the stencil fallback
     a.nb_fallback = 1;
+    a.pc_any_fallback = s->d_err + 4;
   };
   if (cache_on && s->pc_valid) use_cache();
 
@@ -336,7 +339,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       int rc;
       if (cache_on && !s->pc_valid) {
         MaskPairParams<DensityParams<T>> pp{p, {}};
-        rc = pc_prepare(s, n_sorted, &pp.m);
+        rc = pc_prepare(s, n_sorted, &pp.m, st);
         if (rc == PN_OK) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
         if (rc == PN_OK) {
           s->pc_valid = true;
@@ -397,7 +400,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         p.terms = static_cast<T*>(u->terms);
         if (cache_on && !s->pc_valid) {
           MaskPairParams<AdjointParams<T>> pp{p, {}};
-          rc = pc_prepare(s, n_sorted, &pp.m);
+          rc = pc_prepare(s, n_sorted, &pp.m, st);
           if (rc == PN_OK) rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
           if (rc == PN_OK) s->pc_valid = true;
         } else {

@@ -567,3 +567,48 @@ def test_periodic_16m_properties(P, O):
     # symmetry: sum_i sum_{j in N(i)} (j+1) == sum_j count_j * (j+1)
     idx1 = torch.arange(1, n + 1, dtype=torch.int64, device="cuda")
     assert int(sums.sum()) == int((cnt.to(torch.int64) * idx1).sum())
+
+
+# ----------------------------------------------------------------- 1D and rectangular boxes
+
+RECT_CASES = [
+    # (ndims, radius, box min, box max, periodic)
+    (1, 1.3, [0.0], [50.0], False),
+    (1, 1.3, [0.0], [50.0], True),
+    (2, 1.5, [0.0, 0.0], [20.0, 7.0], True),
+    (3, 2.2, [0.0, 0.0, 0.0], [12.0, 15.0, 9.0], True),
+    (3, 2.2, [-3.0, 1.0, 0.5], [9.0, 16.0, 9.5], False),
+]
+
+
+@pytest.mark.parametrize("case", RECT_CASES)
+@pytest.mark.parametrize("dt", [np.float32, np.float64])
+def test_grid_equals_trivial_1d_and_rectangular_boxes(P, O, case, dt):
+    """PeriodicBox with different sizes per dimension and 1D searches (nhs_grid.jl:117-124):
+    neighbour lists (periodic images included) equal brute force; sums over the same pairs
+    agree with the oracle."""
+    d, r, lo, hi, per = case
+    lo, hi = np.asarray(lo), np.asarray(hi)
+    rng = np.random.default_rng(d * 10 + int(per))
+    n = 600 if d == 1 else 1500
+    x = (lo + rng.uniform(0, 1, size=(n, d)) * (hi - lo)).astype(dt)
+    box = (lo, hi) if per else None
+    nhs = make_nhs(P, d, r, lo, hi, n, dtype=dt, box=box)
+    xd = dcoords(x)
+    P.initialize(nhs, xd, xd)
+    g = O.grid_create(d, dt(r), lo.astype(dt), hi.astype(dt), dtype=dt,
+                      periodic_box=(lo.astype(dt), hi.astype(dt)) if per else None)
+    toff, tnb = O.trivial_lists(g, x, x)
+    off, nb = P.neighbor_lists(xd, xd, nhs)
+    assert np.array_equal(off.cpu().numpy(), toff)
+    assert np.array_equal(nb.cpu().numpy(), tnb)
+    # the truncated potential over the same pairs (periodic images included)
+    m = rng.uniform(0.5, 1.5, size=n).astype(dt)
+    e = torch.zeros(n, dtype=torch.float32 if dt == np.float32 else torch.float64, device="cuda")
+    P.foreach_point_neighbor(P.TruncatedPotential(torch.as_tensor(m, device="cuda"), r, e),
+                             xd, xd, nhs)
+    cl = O.build(g, x)
+    prm, keep = O.make_params(masses=m.astype(np.float64), cutoff=r)
+    oe, oab = O.foreach(g, cl, x, x, O.F_POTENTIAL, prm, want_abs=True)
+    tol = TOL_F32 if dt == np.float32 else TOL_F64
+    assert _rel_err(e.cpu().numpy().astype(np.float64), oe, oab) < tol
