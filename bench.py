@@ -45,11 +45,11 @@ UNIT = "pair-evals/s"
 # point's index 4, write the acceleration 12.
 FORCE_BYTES_PER_POINT = {"float32": 44, "float64": 84}
 # DRAM bytes per point of one force sweep measured by ncu (dram__bytes_read.sum +
-# dram__bytes_write.sum, 4,096,000-point capture of the same workload): over the pair-cache
-# lists (the default) most of it is the lists themselves; without the cache (stencil) it is
-# 49.1 B/point.  The ncu summaries are profiles/density_emit_force_lists_wcsph_4M.md and
+# dram__bytes_write.sum, 4,096,000-point capture of the same workload): over the pair cache
+# (the default) most of it is the cache's hit masks; without the cache (stencil) it is
+# 49.1 B/point.  The ncu summaries are profiles/density_masks_force_masks_wcsph_4M.md and
 # profiles/trav_force_density_wcsph_4M.md.
-FORCE_TRAFFIC_BYTES_PER_POINT = {("float32", True): 517.0, ("float32", False): 49.1}
+FORCE_TRAFFIC_BYTES_PER_POINT = {("float32", True): 227.8, ("float32", False): 49.1}
 
 
 def parse():
@@ -361,7 +361,7 @@ def run_gpu(args, rank, world, local):
     alg = FORCE_BYTES_PER_POINT[args.dtype] * n
     achieved = alg / t_force / 1e9
     roofline = {"bound": "hbm",
-                "kernel": ("k_lists_sorted<FForce> (force sweep over the pair cache)"
+                "kernel": ("k_masks_sorted<FForce> (force sweep over the pair cache)"
                            if args.pair_cache > 0 else "k_trav_sorted<FForce> (force sweep)"),
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak,
@@ -369,8 +369,8 @@ def run_gpu(args, rank, world, local):
                             if (args.dtype, args.pair_cache > 0) in FORCE_TRAFFIC_BYTES_PER_POINT
                             else None),
                 "algorithmic_bytes_per_launch": alg,
-                "note": ("force over the pair-cache lists: L1 load path bound (ncu L1 94.6 %, "
-                         "DRAM 18 %); density + list build: issue-bound (85.7 %)"
+                "note": ("force over the pair cache's hit masks and density + masks: "
+                         "issue-bound (ncu issue slots 76 % / 87 %, DRAM 5 %)"
                          if args.pair_cache > 0 else
                          "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
                          "93 % (density), DRAM < 2 % of peak")}
