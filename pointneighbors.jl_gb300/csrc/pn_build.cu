@@ -10,8 +10,10 @@
 //   2. k_scan     exclusive scan of the histogram -> cell starts, single pass with
 //                 decoupled look-back (bounded waits), plus the max_points_per_cell check.
 //   3. k_scatter  point -> slot start[cell] + rank.
-//   4. k_finalize rank-sort each cell's points by point index (a deterministic order,
-//                 independent of atomic timing) and write the cell-sorted coordinates.
+//   4. k_finalize rank-sort each cell's points by their first coordinate, ties by point
+//                 index (a deterministic order, independent of atomic timing; a stencil
+//                 row's three cells are then one x-sorted run) and write the cell-sorted
+//                 coordinates.
 #include <algorithm>
 
 #include "pn_internal.cuh"

@@ -12,7 +12,8 @@
 // Device layout of the cell list (a CSR counting-sort structure instead of the
 // reference's fixed-capacity DynamicVectorOfVectors columns):
 //   start[c] .. start[c+1]   slots of cell c (c = 0-based column-major linear index)
-//   perm[slot]               point index of the slot (ascending inside a cell)
+//   perm[slot]               point index of the slot (inside a cell: ascending first
+//                            coordinate, ties by point index)
 //   cell_of_slot[slot]       linear cell index of the slot
 //   pos[slot * PS]           the point's coordinates, cell-sorted (3D padded to 4 values)
 // Incremental update! keeps this "main" structure from the last full build and holds the

@@ -6,11 +6,12 @@
 //
 // Here the candidates come from the cell-sorted coordinate copy: since cells are numbered
 // column-major, the three cells (x-1, x, x+1) of one row of the stencil are one contiguous
-// slot range, so a query walks 3^(d-1) contiguous ranges.  Query threads are taken in
-// cell-sorted order (when x is y), so the lanes of a warp share their rows and the
-// candidate loads are broadcast / L1 hits.  Candidates are visited in the reference's order
-// (CartesianIndices over the 3^d cells, first dimension fastest; inside a cell by point
-// index), so every sum is accumulated in a fixed, reproducible order.
+// slot range, so a query walks 3^(d-1) contiguous ranges (each clipped to the query's reach,
+// see TravArgs).  Query threads are taken in cell-sorted order (when x is y), so the lanes
+// of a warp share their rows and most candidate loads are L1 hits.  Rows are visited in the
+// reference's order (CartesianIndices over the 3^d cells, first dimension fastest), a row's
+// candidates in slot order (inside a cell by first coordinate), so every sum is accumulated
+// in a fixed, reproducible order.
 //
 // The distance test restates the reference bit for bit: pos_diff = xi - yj in T,
 // d2 = ((pd1*pd1 + pd2*pd2) + pd3*pd3) without contraction, and with a periodic box,

@@ -50,7 +50,8 @@ def test_struct_layout_matches_header(L, tmp_path):
                "pn_nbody_params": L.pn_nbody_params,
                "pn_potential_params": L.pn_potential_params,
                "pn_wcsph_params": L.pn_wcsph_params,
-               "pn_adjoint_params": L.pn_adjoint_params}
+               "pn_adjoint_params": L.pn_adjoint_params,
+               "pn_batch_schedule": L.pn_batch_schedule}
     lines = ['#include <stdio.h>', '#include <stddef.h>', f'#include "{HEADER}"', "int main(){"]
     for name, cls in structs.items():
         lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
