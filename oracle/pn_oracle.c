@@ -70,3 +70,52 @@ static inline double pno_wendland_dw(int d, double h, double r) {
 #include "pn_oracle_body.h"
 #undef T
 #undef S
+
+/* Float64 coordinates, Float32 search radius (pn_oracle.h). full_grid.jl:48-82: the padding
+ * `1001 // 1000 * search_radius` is Float32 (the Rational converts to the radius' type),
+ * subtracted from the Float64 corners in Float64; the grid size is
+ * ceil((max - min) / search_radius) in Float64.  nhs_grid.jl:112-124 with a Float32
+ * PeriodicBox: n_cells = floor((size + 10eps()) / r) in Float64, cell_size = size / n_cells
+ * in Float32. */
+int pno_grid_create_mixed(int32_t ndims, float radius, const double* min_corner,
+                          const double* max_corner, const float* periodic_min,
+                          const float* periodic_max, int32_t max_ppc, pno_grid* g) {
+  memset(g, 0, sizeof(*g));
+  if (ndims < 1 || ndims > 3) return PNO_ERR_INVALID_ARG;
+  g->ndims = ndims;
+  g->dtype = 1;
+  g->mixed = 1;
+  g->max_ppc = max_ppc;
+  g->radius = (double)radius;
+  const float pad = (float)((float)1001 / (float)1000) * radius;
+  for (int k = 0; k < ndims; ++k) {
+    g->min_pad[k] = min_corner[k] - (double)pad;
+    g->max_pad[k] = max_corner[k] + (double)pad;
+    g->n_cells[k] = -1;
+    g->cell_size[k] = (double)radius;
+  }
+  g->n_total = 1;
+  if ((double)radius < 2.220446049250313e-16) {
+    g->is_template = 1;
+    g->n_total = 0;
+  } else {
+    for (int k = 0; k < ndims; ++k) {
+      g->n[k] = (int64_t)ceil((g->max_pad[k] - g->min_pad[k]) / (double)radius);
+      g->n_total *= g->n[k];
+    }
+  }
+  if (periodic_min != NULL && !g->is_template) {
+    g->periodic = 1;
+    for (int k = 0; k < ndims; ++k) {
+      g->box_min[k] = (double)periodic_min[k];
+      g->box_max[k] = (double)periodic_max[k];
+      const float size = periodic_max[k] - periodic_min[k];
+      g->box_size[k] = (double)size;
+      const double nc = floor(((double)size + 10.0 * 2.220446049250313e-16) / (double)radius);
+      g->n_cells[k] = (int64_t)nc;
+      g->cell_size[k] = (double)(size / (float)g->n_cells[k]);
+      if (g->n_cells[k] < 3) return PNO_ERR_INVALID_ARG;
+    }
+  }
+  return PNO_OK;
+}

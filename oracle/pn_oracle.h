@@ -56,7 +56,7 @@ typedef struct {
   double box_min[3], box_max[3], box_size[3];
   double radius;
   int32_t is_template;     /* search_radius < eps(): empty template cell list        */
-  int32_t pad_;
+  int32_t mixed;           /* Float64 coordinates with a Float32 search radius        */
 } pno_grid;
 
 /* Pair-function parameters (all in FP64; the oracle evaluates pair functions in FP64). */
@@ -75,6 +75,15 @@ typedef struct {
   const double* vel;    /* per-point velocity, d components per point             */
   double lambda_pot;    /* loss weight of the n-body energy                       */
 } pno_params;
+
+/* GridNeighborhoodSearch with Float64 coordinates (and cell-list corners) and a Float32
+ * search radius (docs/literate/src/tut_gpu_usage.jl:38-50): cells in Float64 with the
+ * Float32 padding and cell size; pos_diff = Float32(xi - yj), d2, the periodic correction
+ * and the test in Float32 (nhs_grid.jl:547-555, neighborhood_search.jl:428-436).  The
+ * other functions take the Float64 (_f64) entry points with this grid. */
+int pno_grid_create_mixed(int32_t ndims, float radius, const double* min_corner,
+                          const double* max_corner, const float* periodic_min,
+                          const float* periodic_max, int32_t max_ppc, pno_grid* g);
 
 #define PNO_DECL(T, S)                                                                     \
   int64_t pno_floor_to_int_##S(T x);                                                       \

@@ -33,7 +33,7 @@ class Grid(C.Structure):
         ("n_total", C.c_int64), ("min_pad", C.c_double * 3), ("max_pad", C.c_double * 3),
         ("cell_size", C.c_double * 3), ("box_min", C.c_double * 3),
         ("box_max", C.c_double * 3), ("box_size", C.c_double * 3), ("radius", C.c_double),
-        ("is_template", C.c_int32), ("pad_", C.c_int32),
+        ("is_template", C.c_int32), ("mixed", C.c_int32),
     ]
 
 
@@ -104,6 +104,25 @@ def grid_create(ndims, radius, min_corner, max_corner, periodic_box=None, max_pp
             int(max_ppc), C.byref(g))
     if st != PNO_OK:
         raise OracleError(st, "grid_create")
+    return g
+
+
+def grid_create_mixed(ndims, radius, min_corner, max_corner, periodic_box=None, max_ppc=100):
+    """Float64 coordinates with a Float32 search radius (pno_grid_create_mixed); the grid is
+    then used with the Float64 functions."""
+    mn = np.ascontiguousarray(min_corner, dtype=np.float64)
+    mx = np.ascontiguousarray(max_corner, dtype=np.float64)
+    pmn = pmx = None
+    if periodic_box is not None:
+        pmn = np.ascontiguousarray(periodic_box[0], dtype=np.float32)
+        pmx = np.ascontiguousarray(periodic_box[1], dtype=np.float32)
+    fn = lib().pno_grid_create_mixed
+    fn.argtypes = [C.c_int32, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                   C.c_int32, C.POINTER(Grid)]
+    st = fn(ndims, float(np.float32(radius)), _ptr(mn), _ptr(mx), _ptr(pmn), _ptr(pmx),
+            int(max_ppc), C.byref(g := Grid()))
+    if st != PNO_OK:
+        raise OracleError(st, "grid_create_mixed")
     return g
 
 

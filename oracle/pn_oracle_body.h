@@ -179,16 +179,46 @@ int FN(pno_build_parallel_)(const pno_grid* g, const T* y, int64_t n_y, int32_t*
   return status;
 }
 
+/* r^2 in the search radius' type: Float32 for a mixed grid. */
+static inline T FN(r2_)(const pno_grid* g) {
+  const T r = (T)g->radius;
+  if (g->mixed) {
+    const float rf = (float)g->radius;
+    return (T)(float)(rf * rf);
+  }
+  return (T)(r * r);
+}
+
 /* neighborhood_search.jl:547-555 (via nhs_grid.jl:547-553) and :428-436:
  * pos_diff = xi - yj in T; d2 = dot(pos_diff, pos_diff); with a periodic box and
  * d2 > r^2, pos_diff -= size .* round.(pos_diff ./ size) and d2 is recomputed. */
 static inline T FN(pair_d2_)(const pno_grid* g, const T* xi, const T* yj, T* pd) {
   const int d = g->ndims;
+  if (g->mixed) {
+    /* pos_diff = convert.(Float32, xi - yj): the difference in Float64, then rounded */
+    float pf[3];
+    for (int k = 0; k < d; ++k) pf[k] = (float)((double)xi[k] - (double)yj[k]);
+    float d2f = pf[0] * pf[0];
+    for (int k = 1; k < d; ++k) d2f = d2f + pf[k] * pf[k];
+    const float rf = (float)g->radius;
+    if (g->periodic && d2f > rf * rf) {
+      for (int k = 0; k < d; ++k) {
+        const float sz = (float)g->box_size[k];
+        const float q = pf[k] / sz;
+        const float rq = rintf(q);
+        const float sh = sz * rq;
+        pf[k] = pf[k] - sh;
+      }
+      d2f = pf[0] * pf[0];
+      for (int k = 1; k < d; ++k) d2f = d2f + pf[k] * pf[k];
+    }
+    for (int k = 0; k < d; ++k) pd[k] = (T)pf[k];
+    return (T)d2f;
+  }
   for (int k = 0; k < d; ++k) pd[k] = (T)(xi[k] - yj[k]);
   T d2 = (T)(pd[0] * pd[0]);
   for (int k = 1; k < d; ++k) d2 = (T)(d2 + (T)(pd[k] * pd[k]));
-  const T r = (T)g->radius;
-  const T r2 = (T)(r * r);
+  const T r2 = FN(r2_)(g);
   if (g->periodic && d2 > r2) {
     for (int k = 0; k < d; ++k) {
       T sz = (T)g->box_size[k];
@@ -307,8 +337,7 @@ int FN(pno_foreach_)(const pno_grid* g, const int32_t* cells, const int32_t* len
                      const int32_t* points, int64_t n_points, int32_t f,
                      const pno_params* p, void* out, double* abs_out, int32_t n_threads) {
   const int d = g->ndims;
-  const T r = (T)g->radius;
-  const T r2 = (T)(r * r);
+  const T r2 = FN(r2_)(g);
   const int64_t m = points ? n_points : n_x;
   int status = PNO_OK;
   (void)n_y;
@@ -362,8 +391,7 @@ int FN(pno_neighbor_lists_)(const pno_grid* g, const int32_t* cells, const int32
                             const int64_t* offsets, int32_t* counts, int32_t* nbrs,
                             int32_t n_threads) {
   const int d = g->ndims;
-  const T r = (T)g->radius;
-  const T r2 = (T)(r * r);
+  const T r2 = FN(r2_)(g);
   int status = PNO_OK;
   (void)n_y;
 #pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(dynamic, 64)
@@ -396,8 +424,7 @@ int FN(pno_trivial_lists_)(const pno_grid* g, const T* x, int64_t n_x, const T* 
                            int64_t n_y, const int64_t* offsets, int32_t* counts,
                            int32_t* nbrs, int32_t n_threads) {
   const int d = g->ndims;
-  const T r = (T)g->radius;
-  const T r2 = (T)(r * r);
+  const T r2 = FN(r2_)(g);
 #pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(dynamic, 16)
   for (int64_t i = 0; i < n_x; ++i) {
     int64_t cnt = 0;
@@ -469,8 +496,7 @@ int FN(pno_loss_grad_)(const pno_grid* g, const int32_t* cells, const int32_t* l
                        const T* x, int64_t n, const pno_params* p, double* rho,
                        double* loss, double* grad, int32_t n_threads) {
   const int d = g->ndims;
-  const T r = (T)g->radius;
-  const T r2 = (T)(r * r);
+  const T r2 = FN(r2_)(g);
   double lsum = 0.0, esum = 0.0;
   int status = PNO_OK;
 #pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(dynamic, 64) \
@@ -538,8 +564,7 @@ int FN(pno_loss_fd_)(const pno_grid* g, const int32_t* cells, const int32_t* len
                      const T* x, int64_t n, const pno_params* p, const double* rho,
                      const int64_t* which, int64_t n_which, double step, double* fd) {
   const int d = g->ndims;
-  const T r = (T)g->radius;
-  const T r2 = (T)(r * r);
+  const T r2 = FN(r2_)(g);
   (void)n;
 #pragma omp parallel for schedule(dynamic, 4)
   for (int64_t w = 0; w < n_which; ++w) {

@@ -210,3 +210,42 @@ def test_grid_equals_trivial(O, pkg, shape, seed):
     isum = O.foreach(g, cl, coords, coords, O.F_INDEX_SUM)
     expect = np.array([int((tnb[toff[i]:toff[i + 1]] + 1).sum()) for i in range(coords.shape[0])])
     assert np.array_equal(isum, expect)
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_mixed_precision_grid_equals_trivial(O, periodic):
+    """Float64 coordinates with a Float32 search radius (docs/literate/src/tut_gpu_usage.jl:45-50):
+    the grid's lists equal brute force under the same Float32 distance test, plain and periodic."""
+    rng = np.random.default_rng(11)
+    r = np.float32(0.9)
+    lo, hi = np.zeros(3), np.array([6.0, 5.0, 7.3])
+    y = rng.uniform(lo, hi, size=(3000, 3))
+    if periodic:
+        g = O.grid_create_mixed(3, r, lo, hi, periodic_box=(lo, hi))
+    else:
+        g = O.grid_create_mixed(3, r, lo - r, hi + r)
+    assert g.mixed == 1 and g.dtype == 1
+    cl = O.build(g, y)
+    toff, tnb = O.trivial_lists(g, y, y)
+    off, nb = O.neighbor_lists(g, cl, y, y)
+    assert np.array_equal(off, toff)
+    for i in range(len(y)):
+        assert np.array_equal(np.sort(nb[off[i]:off[i + 1]]), tnb[toff[i]:toff[i + 1]])
+
+
+def test_mixed_precision_distance_in_float32(O):
+    """The distance test of a mixed search rounds the Float64 difference to Float32 first:
+    a pair 1e-12 beyond the radius in Float64 is a neighbour, one Float32 step beyond is not."""
+    r = np.float32(1.7)
+    rd = float(r)
+    step = float(np.nextafter(r, np.float32(np.inf)))
+    y = np.array([[0.0, 0.0], [rd + 1e-12, 0.0], [step, 0.0]])
+    g = O.grid_create_mixed(2, r, [-3.0, -3.0], [5.0, 3.0])
+    cl = O.build(g, y)
+    off, nb = O.neighbor_lists(g, cl, y, y)
+    rows = [sorted(nb[off[i]:off[i + 1]].tolist()) for i in range(3)]
+    assert rows == [[0, 1], [0, 1, 2], [1, 2]]
+    # the same points with the Float64 radius: the first pair is outside
+    g64 = O.grid_create(2, rd, [-3.0, -3.0], [5.0, 3.0])
+    off, nb = O.neighbor_lists(g64, O.build(g64, y), y, y)
+    assert sorted(nb[off[0]:off[1]].tolist()) == [0]
