@@ -57,6 +57,16 @@ typedef enum {
 
 typedef enum { PN_FLOAT32 = 0, PN_FLOAT64 = 1 } pn_dtype;
 
+/* pn_config.flags.  PN_FLAG_FLOAT32_SEARCH: Float64 coordinates (dtype PN_FLOAT64) with a
+ * Float32 search radius and PeriodicBox -- the reference's mixed precision
+ * (docs/literate/src/tut_gpu_usage.jl:38-50): cells are computed in Float64, but pos_diff is
+ * the Float64 difference converted to Float32, and d^2, the periodic correction and the test
+ * d^2 <= r^2 are Float32 (neighborhood_search.jl:402-410).  The pair functions' arrays
+ * (masses, density, pressure, velocity, accel, energy, ...) are then Float32, the type of
+ * pos_diff and distance.  Not taken by pn_count_neighbors_noalloc or pn_batch_create; the
+ * pair cache is not used. */
+#define PN_FLAG_FLOAT32_SEARCH 1
+
 /* nhs_grid.jl:135-192 update strategies available for a FullGridCellList. */
 typedef enum {
   PN_PARALLEL_UPDATE = 0,             /* full rebuild (the FullGridCellList default)       */
@@ -94,7 +104,7 @@ typedef struct {
   int64_t n_points;            /* expected number of points in y (pre-sizes scratch)       */
   int32_t max_points_per_cell; /* > 0: error like the reference when a cell exceeds it;
                                   0: no limit (the CSR cell list has no fixed capacity)     */
-  int32_t flags;               /* reserved, must be 0                                       */
+  int32_t flags;               /* 0 or PN_FLAG_FLOAT32_SEARCH                               */
 } pn_config;
 
 /* Geometry as computed by the constructors (for tests and for the Julia binding's

@@ -115,7 +115,11 @@ class PeriodicBox:
 class FullGridCellList:
     """FullGridCellList(; min_corner, max_corner, search_radius, max_points_per_cell)
     (full_grid.jl:48-82).  `min_corner`/`max_corner` hold the padded corners like the
-    reference; `max_points_per_cell = 0` removes the per-cell limit."""
+    reference; `max_points_per_cell = 0` removes the per-cell limit.
+
+    The corners are Float32 only when they and the search radius are (Julia's promotion of
+    `min_corner .- 1001 // 1000 * search_radius`); Float64 corners with a Float32 radius
+    give the mixed-precision search (Float64 coordinates, Float32 distances)."""
 
     def __init__(self, *, min_corner, max_corner, search_radius=0.0, max_points_per_cell=100):
         mn = _vec(min_corner, np.float64)
@@ -127,17 +131,16 @@ class FullGridCellList:
                                 "check your `min_corner` and `max_corner`")
         if mn.size > 3:
             raise ArgumentError("this GPU FullGridCellList supports 1 to 3 dimensions")
-        T = _eltype(search_radius) if not isinstance(search_radius, numbers.Integral) else np.float64
-        if _eltype(min_corner) == np.float32 and T == np.float32:
-            T = np.float32
+        R = _eltype(search_radius) if not isinstance(search_radius, numbers.Integral) else np.float64
+        T = np.float32 if _eltype(min_corner) == np.float32 and R == np.float32 else np.float64
         self.eltype = T
         self.ndims = mn.size
         self._min = mn.astype(T)
         self._max = mx.astype(T)
         self.search_radius = search_radius
         self.max_points_per_cell = int(max_points_per_cell)
-        r = T(search_radius)
-        pad = T(T(1001) / T(1000)) * r
+        r = R(search_radius)
+        pad = T(R(R(1001) / R(1000)) * r)
         self.min_corner = (self._min - pad).astype(T)
         self.max_corner = (self._max + pad).astype(T)
 
@@ -184,7 +187,11 @@ class GridNeighborhoodSearch:
     of each query's stencil rows are neighbours (a start and a 128-bit mask per row, 20 bytes
     x 3^(d-1) per point), and the sweeps that follow until the next initialize/update visit
     exactly those.  Queries the cache cannot describe keep the cell stencil, so results do
-    not depend on it."""
+    not depend on it.
+
+    A Float32 search radius over a Float64 cell list is the reference's mixed precision
+    (docs/literate/src/tut_gpu_usage.jl:38-50): coordinates are Float64 (`coord_eltype`),
+    pos_diff and distance Float32 (`eltype`), and so are the pair functions' arrays."""
 
     def __init__(self, ndims, *, search_radius=0.0, n_points=0, periodic_box=None,
                  cell_list=None, update_strategy=None, pair_cache=0):
@@ -212,6 +219,8 @@ class GridNeighborhoodSearch:
                                 "same element type")
         self.ndims = int(ndims)
         self.eltype = T
+        self.mixed = T == np.float32 and cell_list.eltype == np.float64
+        self.coord_eltype = np.float64 if self.mixed else T
         self.search_radius = T(search_radius)
         self.n_points = int(n_points)
         self.periodic_box = periodic_box
@@ -219,11 +228,13 @@ class GridNeighborhoodSearch:
         self.update_strategy = update_strategy
         cfg = _lib.pn_config()
         cfg.ndims = self.ndims
-        cfg.dtype = _lib.PN_FLOAT32 if T == np.float32 else _lib.PN_FLOAT64
+        C_ = self.coord_eltype
+        cfg.dtype = _lib.PN_FLOAT32 if C_ == np.float32 else _lib.PN_FLOAT64
+        cfg.flags = _lib.PN_FLAG_FLOAT32_SEARCH if self.mixed else 0
         cfg.search_radius = float(self.search_radius)
         for k in range(self.ndims):
-            cfg.min_corner[k] = float(T(cell_list._min[k]))
-            cfg.max_corner[k] = float(T(cell_list._max[k]))
+            cfg.min_corner[k] = float(C_(cell_list._min[k]))
+            cfg.max_corner[k] = float(C_(cell_list._max[k]))
         if periodic_box is not None:
             cfg.periodic = 1
             for k in range(self.ndims):
@@ -310,9 +321,9 @@ def _coords(nhs: GridNeighborhoodSearch, a, name: str):
         raise ArgumentError(f"`{name}` must be a CUDA tensor of shape (d, N)")
     if a.dim() != 2 or a.shape[0] != nhs.ndims:
         raise ArgumentError(f"`{name}` must have shape ({nhs.ndims}, N), got {tuple(a.shape)}")
-    want = torch.float32 if nhs.eltype == np.float32 else torch.float64
+    want = torch.float32 if nhs.coord_eltype == np.float32 else torch.float64
     if a.dtype != want:
-        raise ArgumentError(f"`{name}` must have dtype {want} like the search radius")
+        raise ArgumentError(f"`{name}` must have dtype {want} like the cell list")
     if a.shape[1] > 0 and a.stride() != (1, nhs.ndims):
         a = a.t().contiguous().t()
     return a
@@ -371,7 +382,8 @@ def copy_neighborhood_search(nhs, search_radius, n_points):
         return nhs._copy(search_radius, n_points)
     cl = nhs.cell_list
     T = _eltype(search_radius)
-    new_cl = FullGridCellList(min_corner=cl._min.astype(T), max_corner=cl._max.astype(T),
+    CT = np.result_type(cl.eltype, T)  # a Float64 cell list stays Float64
+    new_cl = FullGridCellList(min_corner=cl._min.astype(CT), max_corner=cl._max.astype(CT),
                               search_radius=T(search_radius),
                               max_points_per_cell=cl.max_points_per_cell)
     return GridNeighborhoodSearch(nhs.ndims, search_radius=T(search_radius), n_points=n_points,
@@ -636,7 +648,7 @@ def neighbor_lists(x, y, nhs: GridNeighborhoodSearch, *, points=None, sort=True)
 def cell_coords(coords, nhs: GridNeighborhoodSearch):
     """cell_coords(x, nhs) (nhs_grid.jl:622-638): the 1-based (periodic) cell of a point."""
     torch = _torch()
-    x = torch.as_tensor(np.asarray(coords, dtype=nhs.eltype).reshape(1, -1), device="cuda")
+    x = torch.as_tensor(np.asarray(coords, dtype=nhs.coord_eltype).reshape(1, -1), device="cuda")
     out = torch.empty(nhs.ndims, dtype=torch.int64, device="cuda")
     rc = lib().pn_cell_coords(nhs._h, _ptr(x), 1, _ptr(out), _stream())
     _finish(nhs, rc, True, "cell_coords")

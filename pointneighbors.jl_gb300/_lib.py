@@ -27,6 +27,7 @@ PN_ERR_SCRATCH_LIMIT = 11
 PN_NOALLOC_SCRATCH_BYTES = 4 * 1024 * 1024
 
 PN_FLOAT32, PN_FLOAT64 = 0, 1
+PN_FLAG_FLOAT32_SEARCH = 1
 PN_PARALLEL_UPDATE, PN_PARALLEL_INCREMENTAL_UPDATE = 0, 1
 
 PN_F_COUNT = 0

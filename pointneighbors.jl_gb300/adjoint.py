@@ -13,7 +13,7 @@ from __future__ import annotations
 
 import torch
 
-from . import AdjointLossBackward, AdjointLossForward, foreach_point_neighbor, update
+from . import AdjointLossBackward, AdjointLossForward, _tdtype, foreach_point_neighbor, update
 
 
 class _AdjointLoss(torch.autograd.Function):
@@ -21,8 +21,9 @@ class _AdjointLoss(torch.autograd.Function):
     def forward(ctx, x, nhs, mass, h, cutoff, lambda_pot):
         n = x.shape[1]
         update(nhs, x, x, check=False)
-        density = torch.empty(n, dtype=x.dtype, device=x.device)
-        terms = torch.empty(n, dtype=x.dtype, device=x.device)
+        vt = _tdtype(nhs)  # the pair arithmetic's type (Float32 in a mixed search)
+        density = torch.empty(n, dtype=vt, device=x.device)
+        terms = torch.empty(n, dtype=vt, device=x.device)
         loss = torch.empty(1, dtype=torch.float64, device=x.device)
         f = AdjointLossForward(density=density, terms=terms, loss=loss, mass=mass, h=h,
                                cutoff=cutoff, lambda_pot=lambda_pot)
@@ -42,12 +43,12 @@ class _AdjointLoss(torch.autograd.Function):
         (density,) = ctx.saved_tensors
         y = nhs._y_keep
         n, d = y.shape[1], y.shape[0]
-        grad = torch.empty(n * d, dtype=y.dtype, device=y.device)
+        grad = torch.empty(n * d, dtype=_tdtype(nhs), device=y.device)
         scale = g_out.detach().to(torch.float64).reshape(1).contiguous()
         f = AdjointLossBackward(density=density, grad=grad, grad_scale=scale,
                                 reuse_state=False, **ctx.consts)
         foreach_point_neighbor(f, y, y, nhs, check=True)
-        return grad.view(n, d).t(), None, None, None, None, None
+        return grad.view(n, d).t().to(y.dtype), None, None, None, None, None
 
 
 def adjoint_loss(x, nhs, *, mass=1.0, h=1.5, cutoff=3.0, lambda_pot=0.01):

@@ -65,7 +65,7 @@ class BatchedNeighborhoodSearch:
             raise ArgumentError("a batch needs at least one search")
         for s in searches:
             if not isinstance(s, GridNeighborhoodSearch) or s.ndims != 3 or \
-                    s.eltype != np.float32 or s.periodic_box is not None:
+                    s.coord_eltype != np.float32 or s.periodic_box is not None:
                 raise ArgumentError("the batched form takes 3D Float32 searches without a "
                                     "periodic box")
         n = len(searches)

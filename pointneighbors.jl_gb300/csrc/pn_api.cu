@@ -7,6 +7,10 @@
 //   GridNeighborhoodSearch (nhs_grid.jl:77-129): with a PeriodicBox,
 //     n_cells = floor(Int, (size + 10 eps()) / r) in Float64, cell_size = size / n_cells in T,
 //     at least 3 cells per dimension.
+// With PN_FLAG_FLOAT32_SEARCH (Float64 coordinates, Float32 search radius) the corners are
+// Float64 padded by the Float32 value Float32(1001 // 1000) * r, the cell count divides the
+// Float64 extent by the widened radius, and the PeriodicBox is Float32 like the radius
+// (nhs_grid.jl:107-110): its size and cell size are Float32 values.
 // This file is compiled with -ffp-contract=off for the host compiler as well, so these T
 // expressions are rounded exactly like Julia's.
 #include <algorithm>
@@ -100,12 +104,13 @@ int ensure_qcount(pn_search* s, int64_t n) {
   return PN_OK;
 }
 
-template <typename T>
+// T: the coordinates' type (corners, cells); R: the search radius's (and PeriodicBox's) type.
+template <typename T, typename R>
 static int geometry(pn_search* s) {
-  const pn_config& c = s->cfg;
+  pn_config& c = s->cfg;
   const int d = c.ndims;
-  const T r = (T)c.search_radius;
-  const T pad = (T)((T)1001 / (T)1000) * r;  // `1001 // 1000 * search_radius`
+  const R r = (R)c.search_radius;
+  const R pad = (R)((R)1001 / (R)1000) * r;  // `1001 // 1000 * search_radius`
   s->radius = (double)r;
   s->is_template = (double)r < 2.220446049250313e-16 ? 1 : 0;  // search_radius < eps()
   int64_t total = 1;
@@ -118,12 +123,12 @@ static int geometry(pn_search* s) {
   }
   for (int k = 0; k < d; ++k) {
     const T mn = (T)c.min_corner[k], mx = (T)c.max_corner[k];
-    const T mnp = (T)(mn - pad), mxp = (T)(mx + pad);
+    const T mnp = (T)(mn - (T)pad), mxp = (T)(mx + (T)pad);
     s->min_pad[k] = (double)mnp;
     s->max_pad[k] = (double)mxp;
     s->cell_size[k] = (double)r;
     if (!s->is_template) {
-      const T q = (T)((T)(mxp - mnp) / r);
+      const T q = (T)((T)(mxp - mnp) / (T)r);
       if (!(q >= (T)1) || !(q < (T)2147483647.0)) return PN_ERR_INVALID_ARG;
       s->grid_size[k] = (int64_t)std::ceil((double)q);
       total *= s->grid_size[k];
@@ -135,13 +140,15 @@ static int geometry(pn_search* s) {
   if (c.periodic && !s->is_template) {
     s->periodic = 1;
     for (int k = 0; k < d; ++k) {
-      const T size = (T)((T)c.periodic_max[k] - (T)c.periodic_min[k]);
+      c.periodic_min[k] = (double)(R)c.periodic_min[k];  // the box is in R
+      c.periodic_max[k] = (double)(R)c.periodic_max[k];
+      const R size = (R)((R)c.periodic_max[k] - (R)c.periodic_min[k]);
       s->box_size[k] = (double)size;
       const double nc = std::floor(((double)size + 10.0 * 2.220446049250313e-16) / (double)r);
       if (!(nc >= 3.0)) return PN_ERR_INVALID_ARG;  // "needs at least 3 cells"
       if (nc > 1e9) return PN_ERR_INVALID_ARG;
       s->n_cells[k] = (int64_t)nc;
-      s->cell_size[k] = (double)(T)(size / (T)s->n_cells[k]);
+      s->cell_size[k] = (double)(R)(size / (R)s->n_cells[k]);
       // The periodic cells 2..n_cells+1 (and the stencil's wrap-around neighbours) must be
       // cells of the padded grid; the reference's tests always build the cell list over the
       // periodic box, which gives n_cells + 3 <= grid_size.
@@ -149,6 +156,14 @@ static int geometry(pn_search* s) {
     }
   }
   return PN_OK;
+}
+
+static int geometry_for(pn_search* s) {
+  if (s->cfg.flags & ~PN_FLAG_FLOAT32_SEARCH) return PN_ERR_INVALID_ARG;
+  s->mixed = (s->cfg.flags & PN_FLAG_FLOAT32_SEARCH) ? 1 : 0;
+  if (s->mixed && s->dtype != PN_FLOAT64) return PN_ERR_INVALID_ARG;
+  if (s->mixed) return geometry<double, float>(s);
+  return s->dtype == PN_FLOAT64 ? geometry<double, double>(s) : geometry<float, float>(s);
 }
 
 static int create(const pn_config* cfg, pn_search** out) {
@@ -166,7 +181,7 @@ static int create(const pn_config* cfg, pn_search** out) {
   s->cfg = *cfg;
   s->ndims = cfg->ndims;
   s->dtype = cfg->dtype;
-  int rc = cfg->dtype == PN_FLOAT64 ? geometry<double>(s) : geometry<float>(s);
+  int rc = geometry_for(s);
   if (rc != PN_OK) {
     delete s;
     return rc;
@@ -390,7 +405,7 @@ int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out) {
   tmp.cfg = *cfg;
   tmp.ndims = cfg->ndims;
   tmp.dtype = cfg->dtype;
-  int rc = cfg->dtype == PN_FLOAT64 ? geometry<double>(&tmp) : geometry<float>(&tmp);
+  int rc = geometry_for(&tmp);
   if (rc != PN_OK) return rc;
   return pn_get_grid_info(&tmp, out);
 }

@@ -410,8 +410,8 @@ int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_cl
   int64_t np = 0, nc = 0;
   for (int32_t c = 0; c < n_clouds; ++c) {
     const pn_config& cf = cfgs[c];
-    if (cf.ndims != 3 || cf.dtype != PN_FLOAT32 || cf.periodic || n_points[c] < 0 ||
-        !(cf.search_radius > 0.0)) {
+    if (cf.ndims != 3 || cf.dtype != PN_FLOAT32 || cf.flags != 0 || cf.periodic ||
+        n_points[c] < 0 || !(cf.search_radius > 0.0)) {
       delete b;
       return PN_ERR_INVALID_ARG;
     }

@@ -26,6 +26,7 @@ struct pn_search {
   pn_config cfg;
   // geometry (values exact in T, stored as double)
   int32_t ndims, dtype, periodic, is_template;
+  int32_t mixed;        // PN_FLAG_FLOAT32_SEARCH: Float64 coordinates, Float32 pair arithmetic
   int64_t grid_size[3], n_cells[3];
   double min_pad[3], max_pad[3], cell_size[3], box_size[3];
   double radius;
@@ -155,5 +156,16 @@ int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, 
 template <typename T>
 int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* nb,
                const int64_t* grp, int32_t cap, int32_t* len, cudaStream_t st);
+
+// pn_traverse_mixed.cu: the same three for a search with PN_FLAG_FLOAT32_SEARCH (Float64
+// coordinates, Float32 pair functions); foreach<double> and friends forward to them.
+int foreach_mixed(pn_search* s, int32_t functor, const double* x, int64_t n_x, const double* y,
+                  int64_t n_y, const int32_t* points, int64_t n_points, const void* params,
+                  cudaStream_t st, const ListsRef* lists);
+int lists_count_mixed(pn_search* s, const double* x, int64_t n_x, const double* y, int64_t n_y,
+                      int32_t* len, int32_t* by_slot, int64_t* n_rows, cudaStream_t st);
+int lists_emit_mixed(pn_search* s, const double* x, int64_t n_x, const double* y, int64_t n_y,
+                     int32_t* nb, const int64_t* grp, int32_t cap, int32_t* len,
+                     cudaStream_t st);
 
 }  // namespace pn

@@ -257,6 +257,7 @@ extern "C" int pn_count_neighbors_noalloc(const pn_config* cfg, const void* x, i
   using namespace pn;
   if (!cfg || n < 0 || (n > 0 && (!x || !counts))) return PN_ERR_INVALID_ARG;
   if (!(cfg->search_radius >= 0.0) || cfg->max_points_per_cell < 0) return PN_ERR_INVALID_ARG;
+  if (cfg->flags != 0) return PN_ERR_INVALID_ARG;  // one element type only
   pn_grid_info gi;
   int rc = pn_compute_geometry(cfg, &gi);  // host only: the geometry pn_create computes
   if (rc != PN_OK) return rc;

@@ -709,6 +709,88 @@ __device__ __forceinline__ T pair_geom(const GridDev<T>& g, const T* xi, const T
 }
 
 
+// ------------------------------------------------------------------ mixed precision
+// Float64 coordinates with a Float32 search radius (PN_FLAG_FLOAT32_SEARCH): the reference
+// converts pos_diff = xi - yj (computed in Float64) to Float32, then computes d2, the
+// periodic correction and the test d2 <= r^2 in Float32 (neighborhood_search.jl:402-410,
+// :428-436), and the pair function sees the Float32 pos_diff and distance.
+// The traversal runs in Float64 with a radius widened past the rounding of that Float32
+// arithmetic, so its candidates hold every such neighbour; Mixed<D, F> redoes the Float32
+// geometry and test for each candidate and hands the accepted ones to the Float32 pair
+// function F.
+struct MixedGeom {
+  float r2;            // fl32(r * r)
+  float box[3];        // PeriodicBox size (Float32)
+  int32_t per;         // periodic box present (the traversal's PER)
+  const double* pos;   // cell-sorted coordinates (a candidate's Float64 values)
+  const float* state;  // 3D force / adjoint sweeps: F's aux is state[4 js + 3], else null
+};
+template <class PF>
+struct MixedParams {
+  PF f;
+  MixedGeom m;
+};
+
+template <int D, class F>
+struct Mixed {
+  static constexpr bool kCountOnly = false;  // every candidate is re-tested in Float32
+  static constexpr bool kInline = F::kInline;
+  using Params = MixedParams<typename F::Params>;  // the same type for every D
+  using Acc = typename F::Acc;
+  static __device__ __forceinline__ Query<float, D> narrow(const Query<double, D>& q) {
+    Query<float, D> r;
+    r.i = q.i;
+    r.q = q.q;
+    r.k = q.k;
+#pragma unroll
+    for (int k = 0; k < D; ++k) r.x[k] = __double2float_rn(q.x[k]);
+    return r;
+  }
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
+  static __device__ __forceinline__ void fail(const Params& p, const Query<double, D>& q) {
+    F::fail(p.f, narrow(q));
+  }
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<double, D>& q) {
+    F::init(a, p.f, narrow(q));
+  }
+  // pd: the traversal's Float64 pos_diff, the plain difference unless a periodic image was
+  // taken -- with a periodic box the difference is recomputed from the candidate.
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<double, D>& q,
+                                              int32_t js, const double* pd, double, double) {
+    float pf[D];
+    if (p.m.per) {
+      double yj[D];
+      load_pos<double, D>(p.m.pos, js, yj);
+#pragma unroll
+      for (int k = 0; k < D; ++k) pf[k] = __double2float_rn(xsub(q.x[k], yj[k]));
+    } else {
+#pragma unroll
+      for (int k = 0; k < D; ++k) pf[k] = __double2float_rn(pd[k]);
+    }
+    float d2 = d2_exact<float, D>(pf);
+    if (p.m.per && d2 > p.m.r2) {
+#pragma unroll
+      for (int k = 0; k < D; ++k)
+        pf[k] = xsub(pf[k], xmul(p.m.box[k], xrint(xdiv(pf[k], p.m.box[k]))));
+      d2 = d2_exact<float, D>(pf);
+    }
+    if (!(d2 <= p.m.r2)) return;
+    const float aux = p.m.state != nullptr ? __ldg(&p.m.state[4 * (int64_t)js + 3]) : 0.0f;
+    F::pair(a, p.f, narrow(q), js, pf, d2, aux);
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<double, D>& q) {
+    F::finish(a, p.f, narrow(q));
+  }
+};
+
+// Mixed<D, F<float, D>> as a pair-function template of the traversal's (T, D).
+template <template <typename, int> class F>
+struct MixedOf {
+  template <typename T, int D>
+  using type = Mixed<D, F<float, D>>;
+};
+
+
 // ------------------------------------------------------------------ candidate scan
 // Candidates are classified without branches.  The exact path (classify, kExact) gives
 // `hit` when the FMA form of d2 is clearly inside r^2 and `slow` when the exact form must

@@ -1,10 +1,12 @@
-// pn_traverse_impl.cuh -- host dispatch of foreach_point_neighbor for one element type;
-// included by pn_traverse_f32.cu and pn_traverse_f64.cu.
+// pn_traverse_impl.cuh -- host dispatch of foreach_point_neighbor for one coordinate type T
+// and pair-arithmetic type V (V = T, or Float32 with Float64 coordinates); included by
+// pn_traverse_f32.cu, pn_traverse_f64.cu and pn_traverse_mixed.cu.
 #pragma once
 
 #include <algorithm>
 #include <cmath>
 #include <limits>
+#include <type_traits>
 
 #include "pn_traverse.cuh"
 
@@ -15,10 +17,11 @@ static __global__ void k_check_capacity(const int64_t* total, int64_t capacity, 
   if (*total > capacity) set_error(err, PN_ERR_CAPACITY);
 }
 
-// Sorted WCSPH state from user arrays (original order) for a standalone FORCE call.
-template <typename T, int D>
+// Sorted WCSPH state from user arrays (original order) for a standalone FORCE call
+// (coordinates in TP, state in T).
+template <typename TP, typename T, int D>
 __global__ void __launch_bounds__(256)
-k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int32_t n_slots_max,
+k_gather_state(const int32_t* __restrict__ perm, const TP* __restrict__ pos, int32_t n_slots_max,
                const int32_t* __restrict__ n_slots, const T* __restrict__ density,
                const T* __restrict__ pressure, const T* __restrict__ velocity,
                T* __restrict__ pa, T* __restrict__ pb) {
@@ -29,8 +32,8 @@ k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int3
     store4(pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
     return;
   }
-  T x[D];
-  load_pos<T, D>(pos, k, x);
+  TP x[D];
+  load_pos<TP, D>(pos, k, x);
   const T rho = density[i];
   V4<T> va{(T)0, (T)0, (T)0, pressure[i] / (rho * rho)};
   V4<T> vb{(T)0, (T)0, (T)0, rho};
@@ -38,7 +41,7 @@ k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int3
   T* xb = &vb.x;
 #pragma unroll
   for (int d = 0; d < D; ++d) {
-    xa[d] = x[d];
+    xa[d] = (T)x[d];
     xb[d] = velocity[(int64_t)i * D + d];
   }
   store4(pa, k, va);
@@ -46,9 +49,9 @@ k_gather_state(const int32_t* __restrict__ perm, const T* __restrict__ pos, int3
 }
 
 // Adjoint state (x, g = 2 (rho - 1)) in slot order from a density array (original order).
-template <typename T, int D>
+template <typename TP, typename T, int D>
 __global__ void __launch_bounds__(256)
-k_gather_adjoint(const int32_t* __restrict__ perm, const T* __restrict__ pos,
+k_gather_adjoint(const int32_t* __restrict__ perm, const TP* __restrict__ pos,
                  int32_t n_slots_max, const int32_t* __restrict__ n_slots,
                  const T* __restrict__ density, T* __restrict__ pa) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -58,12 +61,12 @@ k_gather_adjoint(const int32_t* __restrict__ perm, const T* __restrict__ pos,
     store4(pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
     return;
   }
-  T x[D];
-  load_pos<T, D>(pos, k, x);
+  TP x[D];
+  load_pos<TP, D>(pos, k, x);
   V4<T> va{(T)0, (T)0, (T)0, (T)2 * (density[i] - (T)1)};
   T* xa = &va.x;
 #pragma unroll
-  for (int d = 0; d < D; ++d) xa[d] = x[d];
+  for (int d = 0; d < D; ++d) xa[d] = (T)x[d];
   store4(pa, k, va);
 }
 
@@ -236,10 +239,62 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
   return a;
 }
 
-template <typename T>
-int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
-            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st,
-            const ListsRef* lists) {
+// ------------------------------------------------------------------ mixed precision
+// The Float64 traversal of a Float32 search: its radius is widened past the rounding of the
+// reference's Float32 arithmetic.  The Float32 d2 of a pair is within 6 units of 2^-24 of
+// the exact squared distance of the Float64 points, plus, after a periodic correction,
+// 2^-24 |pos_diff| per component (the Float32 difference is rounded before the box is
+// subtracted; |pos_diff| is at most the grid's extent).  The margins below exceed both, so
+// every pair the Float32 test accepts is a candidate; Mixed<D, F> decides.
+static MixedGeom mixed_geom(const pn_search* s, TravArgs<double>* a) {
+  MixedGeom m{};
+  const float r = (float)s->radius;
+  m.r2 = r * r;
+  double rs = (double)r * (1.0 + 1e-5);
+  for (int k = 0; k < s->ndims; ++k) {
+    m.box[k] = (float)s->box_size[k];
+    if (s->periodic) rs += 4.0 * std::ldexp(1.0, -24) * (s->max_pad[k] - s->min_pad[k]);
+  }
+  m.per = s->periodic;
+  m.pos = static_cast<const double*>(s->d_pos);
+  m.state = nullptr;
+  a->g.r = rs;
+  a->g.r2 = rs * rs * (1.0 + 1e-9);
+  const double u = std::numeric_limits<double>::epsilon() / 2;
+  a->r2_lo = a->g.r2 * (1.0 - 32.0 * u);
+  a->r2_hi = a->g.r2 * (1.0 + 32.0 * u);
+  return m;
+}
+
+// Launch pair function F: F<T, D> itself, or, with Float32 pair arithmetic over Float64
+// coordinates, Mixed<D, F<float, D>> with the geometry m.
+template <typename T, typename V, template <typename, int> class F>
+static int launch_pair(const pn_search* s, const TravArgs<T>& a, const typename F<V, 1>::Params& p,
+                       const MixedGeom& m, bool sorted, int64_t n_launch, cudaStream_t st) {
+  if constexpr (std::is_same<T, V>::value) {
+    (void)m;
+    return launch_trav<T, F>(s, a, p, sorted, n_launch, st);
+  } else {
+    const MixedParams<typename F<V, 1>::Params> mp{p, m};
+    return launch_trav<T, MixedOf<F>::template type>(s, a, mp, sorted, n_launch, st);
+  }
+}
+
+// In 3D the WCSPH / adjoint state (x, y, z, aux) has the coordinates' layout: the force and
+// backward sweeps read their candidates from it and get aux with the same load.  Over
+// Float64 coordinates the candidates stay the coordinates and Mixed loads aux.
+template <typename T, typename V>
+static void use_state(const pn_search* s, TravArgs<T>& a, MixedGeom& m, const V* state) {
+  if (s->ndims != 3) return;
+  if constexpr (std::is_same<T, V>::value) a.pos = state;
+  else m.state = state;
+}
+
+template <typename T, typename V>
+static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y,
+                     int64_t n_y, const int32_t* points, int64_t n_points, const void* params,
+                     cudaStream_t st, const ListsRef* lists) {
+  constexpr bool kMixed = !std::is_same<T, V>::value;
   if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
   if (n_y != s->n_y || n_x < 0 || (points == nullptr && n_points != 0 && n_points != n_x))
     return PN_ERR_INVALID_ARG;
@@ -248,6 +303,8 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
                       s->full_binned;
   const int64_t n_q = points ? n_points : n_x;
   TravArgs<T> a = trav_args<T>(s, x, n_x, points, n_q);
+  MixedGeom m{};
+  if constexpr (kMixed) m = mixed_geom(s, &a);
   if (lists != nullptr) {
     // rows are slots (lists built with x is y) or the points of x
     if (lists->by_slot) {
@@ -264,7 +321,7 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   const int64_t n_launch = sorted ? n_sorted : n_q;
   // the pair cache: walked while valid, built by a density / adjoint-forward sweep
-  const bool cache_on = lists == nullptr && sorted && s->pc_cap > 0;
+  const bool cache_on = !kMixed && lists == nullptr && sorted && s->pc_cap > 0;
   auto use_cache = [&]() {
     a.pc_b0 = s->d_pc_b0;
     a.pc_mask = reinterpret_cast<const ulonglong2*>(s->d_pc_mask);
@@ -278,13 +335,13 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
   switch (functor) {
     case PN_F_COUNT: {
       const auto* u = static_cast<const pn_count_params*>(params);
-      CountParams<T> p{u->counts, 0};
-      return launch_trav<T, FCount>(s, a, p, sorted, n_launch, st);
+      CountParams<V> p{u->counts, 0};
+      return launch_pair<T, V, FCount>(s, a, p, m, sorted, n_launch, st);
     }
     case PN_F_INDEX_SUM: {
       const auto* u = static_cast<const pn_index_sum_params*>(params);
-      IndexSumParams<T> p{u->sums, s->d_perm};
-      return launch_trav<T, FIndexSum>(s, a, p, sorted, n_launch, st);
+      IndexSumParams<V> p{u->sums, s->d_perm};
+      return launch_pair<T, V, FIndexSum>(s, a, p, m, sorted, n_launch, st);
     }
     case PN_F_NEIGHBOR_LIST: {
       const auto* u = static_cast<const pn_neighbor_list_params*>(params);
@@ -295,8 +352,8 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         if (rc != PN_OK) return rc;
         counts = s->d_qcount;
       }
-      CountParams<T> pc{counts, 1};
-      int rc = launch_trav<T, FCount>(s, a, pc, sorted, n_launch, st);
+      CountParams<V> pc{counts, 1};
+      int rc = launch_pair<T, V, FCount>(s, a, pc, m, sorted, n_launch, st);
       if (rc != PN_OK) return rc;
       rc = scan64(s, counts, n_q, u->offsets, st);
       if (rc != PN_OK) return rc;
@@ -304,57 +361,58 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       // offsets[n_q]); with one, rows are written only if they all fit.
       if (u->neighbors == nullptr || u->capacity <= 0) return cuda_status(cudaGetLastError());
       k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err); count_launch();
-      EmitParams<T> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
-      rc = launch_trav<T, FEmit>(s, a, pe, sorted, n_launch, st);
+      EmitParams<V> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
+      rc = launch_pair<T, V, FEmit>(s, a, pe, m, sorted, n_launch, st);
       if (rc != PN_OK) return rc;
       if (u->sort_rows) rc = sort_rows(s, u->offsets, n_q, u->neighbors, u->capacity, st);
       return rc;
     }
     case PN_F_NBODY_ACCEL: {
       const auto* u = static_cast<const pn_nbody_params*>(params);
-      const T eps_t = std::numeric_limits<T>::epsilon();
-      NBodyParams<T> p{static_cast<const T*>(u->masses), s->d_perm, (T)u->G, std::sqrt(eps_t),
-                       static_cast<T*>(u->accel)};
-      return launch_trav<T, FNBody>(s, a, p, sorted, n_launch, st);
+      const V eps_v = std::numeric_limits<V>::epsilon();
+      NBodyParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->G, std::sqrt(eps_v),
+                       static_cast<V*>(u->accel)};
+      return launch_pair<T, V, FNBody>(s, a, p, m, sorted, n_launch, st);
     }
     case PN_F_POTENTIAL: {
       const auto* u = static_cast<const pn_potential_params*>(params);
       if ((const void*)x != (const void*)y) return PN_ERR_INVALID_ARG;
-      PotentialParams<T> p{static_cast<const T*>(u->masses), s->d_perm, (T)u->cutoff,
-                           (T)(1.0 / u->cutoff), static_cast<T*>(u->energy)};
-      return launch_trav<T, FPotential>(s, a, p, sorted, n_launch, st);
+      PotentialParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->cutoff,
+                           (V)(1.0 / u->cutoff), static_cast<V*>(u->energy)};
+      return launch_pair<T, V, FPotential>(s, a, p, m, sorted, n_launch, st);
     }
     case PN_F_WCSPH_DENSITY:
     case PN_F_WCSPH_STEP: {
       const auto* u = static_cast<const pn_wcsph_params*>(params);
       const bool step = functor == PN_F_WCSPH_STEP;
       if (step && !sorted) return PN_ERR_INVALID_ARG;
-      DensityParams<T> p{sph_const<T>(s, u), static_cast<T*>(u->density),
-                         static_cast<T*>(u->pressure), static_cast<const T*>(u->velocity),
+      DensityParams<V> p{sph_const<V>(s, u), static_cast<V*>(u->density),
+                         static_cast<V*>(u->pressure), static_cast<const V*>(u->velocity),
                          nullptr, nullptr};
       if (sorted && u->velocity != nullptr) {
-        p.pa = static_cast<T*>(s->d_pa);
-        p.pb = static_cast<T*>(s->d_pb);
+        p.pa = static_cast<V*>(s->d_pa);
+        p.pb = static_cast<V*>(s->d_pb);
       }
-      int rc;
-      if (cache_on && !s->pc_valid) {
-        MaskPairParams<DensityParams<T>> pp{p, {}};
-        rc = pc_prepare(s, n_sorted, &pp.m, st);
-        if (rc == PN_OK) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
-        if (rc == PN_OK) {
-          s->pc_valid = true;
-          use_cache();
+      int rc = PN_OK;
+      bool done = false;
+      if constexpr (!kMixed) {
+        if (cache_on && !s->pc_valid) {
+          MaskPairParams<DensityParams<T>> pp{p, {}};
+          rc = pc_prepare(s, n_sorted, &pp.m, st);
+          if (rc == PN_OK) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
+          if (rc == PN_OK) {
+            s->pc_valid = true;
+            use_cache();
+          }
+          done = true;
         }
-      } else {
-        rc = launch_trav<T, FDensity>(s, a, p, sorted, n_launch, st);
       }
+      if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st);
       if (rc != PN_OK || !step) return rc;
-      ForceParams<T> pf{p.c, static_cast<const T*>(s->d_pa), static_cast<const T*>(s->d_pb),
-                        static_cast<T*>(u->accel)};
-      // In 3D the state (x, y, z, p/rho^2) has the coordinates' layout: the force sweep
-      // reads its candidates from it and gets p/rho^2 with the same load.
-      if (s->ndims == 3) a.pos = pf.pa;
-      return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
+      ForceParams<V> pf{p.c, static_cast<const V*>(s->d_pa), static_cast<const V*>(s->d_pb),
+                        static_cast<V*>(u->accel)};
+      use_state(s, a, m, pf.pa);
+      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st);
     }
     case PN_F_WCSPH_FORCE: {
       const auto* u = static_cast<const pn_wcsph_params*>(params);
@@ -362,21 +420,22 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       const int b = div_up(n_sorted, 256);
       const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
       const T* pos = static_cast<const T*>(s->d_pos);
-      T* pa = static_cast<T*>(s->d_pa);
-      T* pb = static_cast<T*>(s->d_pb);
-      const T* dn = static_cast<const T*>(u->density);
-      const T* pr = static_cast<const T*>(u->pressure);
-      const T* ve = static_cast<const T*>(u->velocity);
+      V* pa = static_cast<V*>(s->d_pa);
+      V* pb = static_cast<V*>(s->d_pb);
+      const V* dn = static_cast<const V*>(u->density);
+      const V* pr = static_cast<const V*>(u->pressure);
+      const V* ve = static_cast<const V*>(u->velocity);
       if (b > 0 && !u->reuse_state) {
+        const int32_t ns = (int32_t)n_sorted;
         switch (s->ndims) {
-          case 1: k_gather_state<T, 1><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
-          case 2: k_gather_state<T, 2><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
-          default: k_gather_state<T, 3><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
+          case 1: k_gather_state<T, V, 1><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
+          case 2: k_gather_state<T, V, 2><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
+          default: k_gather_state<T, V, 3><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
         }
       }
-      ForceParams<T> pf{sph_const<T>(s, u), pa, pb, static_cast<T*>(u->accel)};
-      if (s->ndims == 3) a.pos = pa;
-      return launch_trav<T, FForce>(s, a, pf, sorted, n_launch, st);
+      ForceParams<V> pf{sph_const<V>(s, u), pa, pb, static_cast<V*>(u->accel)};
+      use_state(s, a, m, pf.pa);
+      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st);
     }
     case PN_F_ADJOINT_FORWARD:
     case PN_F_ADJOINT_BACKWARD: {
@@ -386,28 +445,32 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
       w.mass = u->mass;
       w.h = u->h;
       w.c0 = w.rho0 = w.gamma_exp = 1.0;
-      AdjointParams<T> p{};
-      p.c = sph_const<T>(s, &w);
-      p.cutoff = (T)u->cutoff;
-      p.inv_cutoff = (T)(1.0 / u->cutoff);
-      p.lambda = (T)u->lambda_pot;
-      p.pa = static_cast<T*>(s->d_pa);
+      AdjointParams<V> p{};
+      p.c = sph_const<V>(s, &w);
+      p.cutoff = (V)u->cutoff;
+      p.inv_cutoff = (V)(1.0 / u->cutoff);
+      p.lambda = (V)u->lambda_pot;
+      p.pa = static_cast<V*>(s->d_pa);
       if (functor == PN_F_ADJOINT_FORWARD) {
         if (!u->density || !u->terms || !u->loss) return PN_ERR_INVALID_ARG;
         int rc = ensure_sum_part(s);
         if (rc != PN_OK) return rc;
-        p.density = static_cast<T*>(u->density);
-        p.terms = static_cast<T*>(u->terms);
-        if (cache_on && !s->pc_valid) {
-          MaskPairParams<AdjointParams<T>> pp{p, {}};
-          rc = pc_prepare(s, n_sorted, &pp.m, st);
-          if (rc == PN_OK) rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
-          if (rc == PN_OK) s->pc_valid = true;
-        } else {
-          rc = launch_trav<T, FAdjointForward>(s, a, p, sorted, n_launch, st);
+        p.density = static_cast<V*>(u->density);
+        p.terms = static_cast<V*>(u->terms);
+        bool done = false;
+        if constexpr (!kMixed) {
+          if (cache_on && !s->pc_valid) {
+            MaskPairParams<AdjointParams<T>> pp{p, {}};
+            rc = pc_prepare(s, n_sorted, &pp.m, st);
+            if (rc == PN_OK)
+              rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
+            if (rc == PN_OK) s->pc_valid = true;
+            done = true;
+          }
         }
+        if (!done) rc = launch_pair<T, V, FAdjointForward>(s, a, p, m, sorted, n_launch, st);
         if (rc != PN_OK) return rc;
-        k_sum_partials<T><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
+        k_sum_partials<V><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
         k_sum_final<<<1, 256, 0, st>>>(s->d_sum_part, SUM_BLOCKS, u->loss); count_launch();
         return cuda_status(cudaGetLastError());
       }
@@ -416,52 +479,87 @@ int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, 
         const int b = div_up(n_sorted, 256);
         const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
         const T* pos = static_cast<const T*>(s->d_pos);
-        const T* dn = static_cast<const T*>(u->density);
+        const V* dn = static_cast<const V*>(u->density);
+        const int32_t ns = (int32_t)n_sorted;
         if (b > 0) {
           switch (s->ndims) {
-            case 1: k_gather_adjoint<T, 1><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, p.pa); count_launch(); break;
-            case 2: k_gather_adjoint<T, 2><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, p.pa); count_launch(); break;
-            default: k_gather_adjoint<T, 3><<<b, 256, 0, st>>>(s->d_perm, pos, (int32_t)n_sorted, n_slots, dn, p.pa); count_launch(); break;
+            case 1: k_gather_adjoint<T, V, 1><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, p.pa); count_launch(); break;
+            case 2: k_gather_adjoint<T, V, 2><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, p.pa); count_launch(); break;
+            default: k_gather_adjoint<T, V, 3><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, p.pa); count_launch(); break;
           }
         }
       }
-      p.grad = static_cast<T*>(u->grad);
+      p.grad = static_cast<V*>(u->grad);
       p.scale = u->grad_scale;
-      if (s->ndims == 3) a.pos = p.pa;
-      return launch_trav<T, FAdjointBackward>(s, a, p, sorted, n_launch, st);
+      use_state(s, a, m, static_cast<const V*>(p.pa));
+      return launch_pair<T, V, FAdjointBackward>(s, a, p, m, sorted, n_launch, st);
     }
     default:
       return PN_ERR_UNSUPPORTED_FUNCTOR;
   }
 }
 
-// ------------------------------------------------------------------ precomputed lists
 template <typename T>
-int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* len,
-                int32_t* by_slot, int64_t* n_rows, cudaStream_t st) {
+int foreach(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y, int64_t n_y,
+            const int32_t* points, int64_t n_points, const void* params, cudaStream_t st,
+            const ListsRef* lists) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (s->mixed)
+      return foreach_mixed(s, functor, x, n_x, y, n_y, points, n_points, params, st, lists);
+  }
+  return foreach_t<T, T>(s, functor, x, n_x, y, n_y, points, n_points, params, st, lists);
+}
+
+// ------------------------------------------------------------------ precomputed lists
+template <typename T, typename V>
+static int lists_count_t(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y,
+                         int32_t* len, int32_t* by_slot, int64_t* n_rows, cudaStream_t st) {
   if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
   if (n_y != s->n_y || n_x < 0) return PN_ERR_INVALID_ARG;
   const bool sorted = (const void*)x == (const void*)y && n_x == n_y && s->full_binned;
   TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
+  MixedGeom m{};
+  if constexpr (!std::is_same<T, V>::value) m = mixed_geom(s, &a);
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   *by_slot = sorted ? 1 : 0;
   *n_rows = sorted ? n_sorted : n_x;
   if (sorted) cudaMemsetAsync(len, 0, sizeof(int32_t) * n_sorted, st);  // vacated slots
-  CountParams<T> p{len, sorted ? 2 : 1};
-  return launch_trav<T, FCount>(s, a, p, sorted, *n_rows, st);
+  CountParams<V> p{len, sorted ? 2 : 1};
+  return launch_pair<T, V, FCount>(s, a, p, m, sorted, *n_rows, st);
+}
+
+template <typename T, typename V>
+static int lists_emit_t(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y,
+                        int32_t* nb, const int64_t* grp, int32_t cap, int32_t* len,
+                        cudaStream_t st) {
+  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
+  if (n_y != s->n_y || n_x < 0) return PN_ERR_INVALID_ARG;
+  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && s->full_binned;
+  TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
+  MixedGeom m{};
+  if constexpr (!std::is_same<T, V>::value) m = mixed_geom(s, &a);
+  const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
+  if (len != nullptr && sorted) cudaMemsetAsync(len, 0, sizeof(int32_t) * n_sorted, st);
+  EmitListParams<V> p{nb, grp, sorted ? 1 : 0, (cap + 3) & ~3, cap, len, s->d_err};
+  return launch_pair<T, V, FEmitList>(s, a, p, m, sorted, sorted ? n_sorted : n_x, st);
+}
+
+template <typename T>
+int lists_count(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* len,
+                int32_t* by_slot, int64_t* n_rows, cudaStream_t st) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (s->mixed) return lists_count_mixed(s, x, n_x, y, n_y, len, by_slot, n_rows, st);
+  }
+  return lists_count_t<T, T>(s, x, n_x, y, n_y, len, by_slot, n_rows, st);
 }
 
 template <typename T>
 int lists_emit(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y, int32_t* nb,
                const int64_t* grp, int32_t cap, int32_t* len, cudaStream_t st) {
-  if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
-  if (n_y != s->n_y || n_x < 0) return PN_ERR_INVALID_ARG;
-  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && s->full_binned;
-  TravArgs<T> a = trav_args<T>(s, x, n_x, nullptr, n_x);
-  const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
-  if (len != nullptr && sorted) cudaMemsetAsync(len, 0, sizeof(int32_t) * n_sorted, st);
-  EmitListParams<T> p{nb, grp, sorted ? 1 : 0, (cap + 3) & ~3, cap, len, s->d_err};
-  return launch_trav<T, FEmitList>(s, a, p, sorted, sorted ? n_sorted : n_x, st);
+  if constexpr (std::is_same<T, double>::value) {
+    if (s->mixed) return lists_emit_mixed(s, x, n_x, y, n_y, nb, grp, cap, len, st);
+  }
+  return lists_emit_t<T, T>(s, x, n_x, y, n_y, nb, grp, cap, len, st);
 }
 
 }  // namespace pn

@@ -45,6 +45,8 @@ class PrecomputedNeighborhoodSearch:
                 raise ArgumentError("`NDIMS` must be 1, 2, or 3")
         self.ndims = int(ndims)
         self.eltype = grid.eltype
+        self.coord_eltype = grid.coord_eltype
+        self.mixed = grid.mixed
         self.search_radius = grid.search_radius
         self.n_points = int(n_points)
         self.periodic_box = grid.periodic_box

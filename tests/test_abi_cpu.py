@@ -117,6 +117,66 @@ def test_geometry_equals_oracle(L, O, g):
         assert gi.n_cells[k] == og.n_cells[k]
 
 
+MIXED_GEOMS = [
+    (3, 0.9, [0.0, 0.0, 0.0], [6.0, 5.0, 7.3], None),
+    (3, 0.9, [0.0, 0.0, 0.0], [6.0, 5.0, 7.3], ([0.0, 0.0, 0.0], [6.0, 5.0, 7.3])),
+    (2, 0.1, [-0.1, -0.2], [0.205, 0.43], ([-0.1, -0.2], [0.205, 0.43])),
+    (2, 1.7, [-3.0, -3.0], [5.0, 3.0], None),
+]
+
+
+@pytest.mark.parametrize("g", MIXED_GEOMS)
+def test_mixed_geometry_equals_oracle(L, O, g):
+    """Float64 corners with a Float32 radius and PeriodicBox (PN_FLAG_FLOAT32_SEARCH)."""
+    ndims, r, mn, mx, box = g
+    r32 = np.float32(r)
+    cfg = L.pn_config()
+    cfg.ndims = ndims
+    cfg.dtype = L.PN_FLOAT64
+    cfg.flags = L.PN_FLAG_FLOAT32_SEARCH
+    cfg.search_radius = float(r32)
+    lo, hi = (np.array(mn) - r, np.array(mx) + r) if box is None else (np.array(mn), np.array(mx))
+    for k in range(ndims):
+        cfg.min_corner[k], cfg.max_corner[k] = lo[k], hi[k]
+    if box is not None:
+        cfg.periodic = 1
+        for k in range(ndims):
+            cfg.periodic_min[k] = float(np.float32(box[0][k]))
+            cfg.periodic_max[k] = float(np.float32(box[1][k]))
+    gi = L.pn_grid_info()
+    assert L.load().pn_compute_geometry(C.byref(cfg), C.byref(gi)) == 0
+    pb = None if box is None else (np.array(box[0]), np.array(box[1]))
+    og = O.grid_create_mixed(ndims, r32, lo, hi, periodic_box=pb)
+    for k in range(ndims):
+        assert gi.grid_size[k] == og.n[k]
+        assert gi.min_corner[k] == og.min_pad[k]
+        assert gi.max_corner[k] == og.max_pad[k]
+        assert gi.cell_size[k] == og.cell_size[k]
+        assert gi.n_cells[k] == og.n_cells[k]
+    assert gi.search_radius == float(r32)
+    # the flag needs Float64 coordinates; unknown flags are rejected
+    cfg.dtype = L.PN_FLOAT32
+    assert L.load().pn_compute_geometry(C.byref(cfg), C.byref(gi)) == L.PN_ERR_INVALID_ARG
+    cfg.dtype = L.PN_FLOAT64
+    cfg.flags = 2
+    assert L.load().pn_compute_geometry(C.byref(cfg), C.byref(gi)) == L.PN_ERR_INVALID_ARG
+
+
+def test_mixed_cell_list_corners(pkg):
+    """FullGridCellList(Float64 corners, Float32 radius): Float64 corners padded by the
+    Float32 value Float32(1001 // 1000) * r (full_grid.jl:65-67); the search is mixed."""
+    P = pkg
+    r = np.float32(0.3)
+    cl = P.FullGridCellList(min_corner=[0.1, 0.2], max_corner=[1.0, 2.0], search_radius=r)
+    pad = float(np.float32(np.float32(1001) / np.float32(1000)) * r)
+    assert cl.eltype == np.float64
+    assert list(cl.min_corner) == [0.1 - pad, 0.2 - pad]
+    assert list(cl.max_corner) == [1.0 + pad, 2.0 + pad]
+    cl32 = P.FullGridCellList(min_corner=np.zeros(2, np.float32), max_corner=np.ones(2, np.float32),
+                              search_radius=r)
+    assert cl32.eltype == np.float32
+
+
 def test_geometry_known_values(L):
     # test/cell_lists/full_grid.jl:28-29
     rc, gi = _geometry(L, 3, np.float64, 1.0, [0.0] * 3, [10.0] * 3)

@@ -101,7 +101,7 @@ def test_adjoint_loss_autograd(P, O):
     L = P.adjoint_loss(xg, nhs, **CONSTS)
     (3.0 * L).backward()
     _, _, _, _, oloss, _, ogr = _oracle(O, x, lo, hi, np.float64)
-    assert abs(float(L) - oloss) <= 1e-12 * abs(oloss)
+    assert abs(float(L.detach()) - oloss) <= 1e-12 * abs(oloss)
     got = xg.grad.T.cpu().numpy()
     assert np.abs(got - 3.0 * ogr).max() <= 1e-10 * np.abs(3.0 * ogr).max()
     # a search re-binned elsewhere between forward and backward is re-binned at the
