@@ -39,6 +39,26 @@ static inline int64_t pno_mod(int64_t x, int64_t n) {
   return r;
 }
 
+/* spatial_hashing.jl:142-156 spatial_hash (Ihmsen et al.): Int64 products and xor, which
+ * wrap around like Julia's, then mod(h, list_size); returned 0-based. */
+int64_t pno_spatial_hash(const int64_t* cell, int32_t ndims, int64_t list_size) {
+  uint64_t h = (uint64_t)cell[0] * 73856093u;
+  if (ndims >= 2) h ^= (uint64_t)cell[1] * 19349663u;
+  if (ndims >= 3) h ^= (uint64_t)cell[2] * 83492791u;
+  return pno_mod((int64_t)h, list_size);
+}
+
+/* spatial_hashing.jl:171-184 coordinates_flattened: coordinate k, reinterpreted as UInt32,
+ * at bits 32k of a UInt128. */
+int pno_coordinates_flattened(const int64_t* cell, int32_t ndims, uint32_t* out) {
+  out[0] = out[1] = out[2] = out[3] = 0;
+  for (int k = 0; k < ndims; ++k) {
+    if (cell[k] < INT32_MIN || cell[k] > INT32_MAX) return PNO_ERR_OUT_OF_DOMAIN;
+    out[k] = (uint32_t)(int32_t)cell[k];
+  }
+  return PNO_OK;
+}
+
 /* Wendland C2 kernel with support 2h: W = sigma_d (1 - q/2)^4 (2q + 1), q = r/h. */
 static inline double pno_wendland_sigma(int d, double h) {
   if (d == 3) return 21.0 / (16.0 * M_PI * h * h * h);

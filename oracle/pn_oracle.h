@@ -57,6 +57,7 @@ typedef struct {
   double radius;
   int32_t is_template;     /* search_radius < eps(): empty template cell list        */
   int32_t mixed;           /* Float64 coordinates with a Float32 search radius        */
+  int64_t list_size;       /* SpatialHashingCellList: number of hash lists (0: none)  */
 } pno_grid;
 
 /* Pair-function parameters (all in FP64; the oracle evaluates pair functions in FP64). */
@@ -84,6 +85,14 @@ typedef struct {
 int pno_grid_create_mixed(int32_t ndims, float radius, const double* min_corner,
                           const double* max_corner, const float* periodic_min,
                           const float* periodic_max, int32_t max_ppc, pno_grid* g);
+
+/* SpatialHashingCellList helpers (cell_lists/spatial_hashing.jl:142-162): the 0-based
+ * hash list of a cell, and its coordinates flattened to 128 bits as four 32-bit words
+ * (word k = the k-th coordinate as UInt32, word 3 = 0).  coordinates_flattened returns
+ * PNO_ERR_OUT_OF_DOMAIN where the reference throws InexactError (a coordinate outside
+ * Int32). */
+int64_t pno_spatial_hash(const int64_t* cell, int32_t ndims, int64_t list_size);
+int pno_coordinates_flattened(const int64_t* cell, int32_t ndims, uint32_t* out);
 
 #define PNO_DECL(T, S)                                                                     \
   int64_t pno_floor_to_int_##S(T x);                                                       \
@@ -118,7 +127,18 @@ int pno_grid_create_mixed(int32_t ndims, float radius, const double* min_corner,
                         double* loss, double* grad, int32_t n_threads);                    \
   int pno_loss_fd_##S(const pno_grid* g, const int32_t* cells, const int32_t* lengths,     \
                       const T* x, int64_t n, const pno_params* p, const double* rho,       \
-                      const int64_t* which, int64_t n_which, double step, double* fd);
+                      const int64_t* which, int64_t n_which, double step, double* fd);    \
+  int pno_grid_create_hash_##S(int32_t ndims, T radius, const T* periodic_min,             \
+                               const T* periodic_max, int64_t list_size, int32_t max_ppc,  \
+                               pno_grid* g);                                               \
+  int pno_hash_build_##S(const pno_grid* g, const T* y, int64_t n_y, int32_t* cells,       \
+                         int32_t* lengths, uint32_t* coords, uint8_t* collisions,          \
+                         int32_t atomic);                                                  \
+  int pno_hash_neighbor_lists_##S(const pno_grid* g, const int32_t* cells,                 \
+                                  const int32_t* lengths, const uint32_t* coords,          \
+                                  const uint8_t* collisions, const T* x, int64_t n_x,      \
+                                  const T* y, int64_t n_y, const int64_t* offsets,         \
+                                  int32_t* counts, int32_t* nbrs, int32_t n_threads);
 
 PNO_DECL(float, f32)
 PNO_DECL(double, f64)

@@ -33,7 +33,7 @@ class Grid(C.Structure):
         ("n_total", C.c_int64), ("min_pad", C.c_double * 3), ("max_pad", C.c_double * 3),
         ("cell_size", C.c_double * 3), ("box_min", C.c_double * 3),
         ("box_max", C.c_double * 3), ("box_size", C.c_double * 3), ("radius", C.c_double),
-        ("is_template", C.c_int32), ("mixed", C.c_int32),
+        ("is_template", C.c_int32), ("mixed", C.c_int32), ("list_size", C.c_int64),
     ]
 
 
@@ -346,3 +346,98 @@ def loss_fd(g: Grid, cl: CellList, x, params: Params, rho, which, step=1e-6):
     fn(C.byref(g), _ptr(cl.cells), _ptr(cl.lengths), _ptr(xa), xa.shape[0],
        C.byref(params), _ptr(ra), _ptr(wa), wa.size, float(step), _ptr(fd))
     return fd
+
+
+# ---------------------------------------------------------------- SpatialHashingCellList
+
+
+def spatial_hash(cell, list_size: int) -> int:
+    """spatial_hash(cell, list_size) - 1 (0-based)."""
+    c = (C.c_int64 * 3)(*[int(v) for v in cell], *([0] * (3 - len(cell))))
+    fn = lib().pno_spatial_hash
+    fn.restype = C.c_int64
+    fn.argtypes = [C.c_void_p, C.c_int32, C.c_int64]
+    return int(fn(c, len(cell), int(list_size)))
+
+
+def coordinates_flattened(cell) -> int:
+    """coordinates_flattened(cell) as a Python int (raises OracleError where the reference
+    throws InexactError)."""
+    c = (C.c_int64 * 3)(*[max(min(int(v), 2**63 - 1), -2**63) for v in cell],
+                        *([0] * (3 - len(cell))))
+    out = (C.c_uint32 * 4)()
+    fn = lib().pno_coordinates_flattened
+    fn.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
+    st = fn(c, len(cell), out)
+    if st != PNO_OK:
+        raise OracleError(st, "coordinates_flattened")
+    return sum(int(out[k]) << (32 * k) for k in range(4))
+
+
+def grid_create_hash(ndims, radius, list_size, periodic_box=None, max_ppc=100,
+                     dtype=np.float64) -> Grid:
+    """GridNeighborhoodSearch over SpatialHashingCellList{ndims}(; list_size,
+    max_points_per_cell)."""
+    dt = np.dtype(dtype)
+    g = Grid()
+    pmn = pmx = None
+    if periodic_box is not None:
+        pmn = np.ascontiguousarray(periodic_box[0], dtype=dt)
+        pmx = np.ascontiguousarray(periodic_box[1], dtype=dt)
+    fn = _f(dt, "grid_create_hash")
+    ctyp = C.c_float if dt == np.float32 else C.c_double
+    fn.argtypes = [C.c_int32, ctyp, C.c_void_p, C.c_void_p, C.c_int64, C.c_int32,
+                   C.POINTER(Grid)]
+    st = fn(ndims, float(dt.type(radius)), _ptr(pmn), _ptr(pmx), int(list_size), int(max_ppc),
+            C.byref(g))
+    if st != PNO_OK:
+        raise OracleError(st, "grid_create_hash")
+    return g
+
+
+class HashCellList:
+    """The reference's SpatialHashingCellList: list_size lists (DynamicVectorOfVectors),
+    the flattened coordinates stored per list and the collision flags."""
+
+    def __init__(self, g: Grid):
+        self.g = g
+        self.cells = np.zeros(g.list_size * g.max_ppc, dtype=np.int32)
+        self.lengths = np.zeros(g.list_size, dtype=np.int32)
+        self.coords = np.zeros(4 * g.list_size, dtype=np.uint32)
+        self.collisions = np.zeros(g.list_size, dtype=np.uint8)
+
+    def __getitem__(self, cell):
+        """cell_list[cell]: the points of the cell's hash list (0-based)."""
+        h = spatial_hash(cell, self.g.list_size)
+        return self.cells[h * self.g.max_ppc: h * self.g.max_ppc + self.lengths[h]]
+
+
+def hash_build(g: Grid, y, atomic: bool = True) -> HashCellList:
+    """initialize! with push_cell_atomic! (ParallelUpdate, atomic=True) or push_cell!
+    (SerialUpdate), in point order."""
+    dt = np.float32 if g.dtype == 0 else np.float64
+    ya = np.ascontiguousarray(y, dtype=dt).reshape(-1, g.ndims)
+    hl = HashCellList(g)
+    fn = _f(dt, "hash_build")
+    fn.argtypes = [C.POINTER(Grid), C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_void_p, C.c_int32]
+    st = fn(C.byref(g), _ptr(ya), ya.shape[0], _ptr(hl.cells), _ptr(hl.lengths),
+            _ptr(hl.coords), _ptr(hl.collisions), 1 if atomic else 0)
+    if st != PNO_OK:
+        raise OracleError(st, "hash_build")
+    return hl
+
+
+def hash_neighbor_lists(g: Grid, hl: HashCellList, x, y, n_threads: int = 0):
+    """CSR (offsets[n_x+1], nbrs) in the reference's traversal order."""
+    dt = np.float32 if g.dtype == 0 else np.float64
+    xa = np.ascontiguousarray(x, dtype=dt).reshape(-1, g.ndims)
+    ya = np.ascontiguousarray(y, dtype=dt).reshape(-1, g.ndims)
+    fn = _f(dt, "hash_neighbor_lists")
+    fn.argtypes = [C.POINTER(Grid), C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p,
+                   C.c_void_p, C.c_int32]
+    head = (C.byref(g), _ptr(hl.cells), _ptr(hl.lengths), _ptr(hl.coords),
+            _ptr(hl.collisions), _ptr(xa), xa.shape[0], _ptr(ya), ya.shape[0])
+    return _lists("hash_neighbor_lists", head, g, xa.shape[0], n_threads)
+

@@ -609,4 +609,124 @@ int FN(pno_loss_fd_)(const pno_grid* g, const int32_t* cells, const int32_t* len
   return PNO_OK;
 }
 
+/* ---------------------------------------------------------------- SpatialHashingCellList */
+
+/* GridNeighborhoodSearch over SpatialHashingCellList{d}(; list_size, max_points_per_cell)
+ * (spatial_hashing.jl:79-89, nhs_grid.jl:77-129): the cell size is r, or the PeriodicBox's
+ * size / n_cells as for the full grid; a point's cell is floor.(x ./ cell_size)
+ * (nhs_grid.jl:636-638), wrapped to 2:n_cells+1 with a periodic box. */
+int FN(pno_grid_create_hash_)(int32_t ndims, T radius, const T* periodic_min,
+                              const T* periodic_max, int64_t list_size, int32_t max_ppc,
+                              pno_grid* g) {
+  const T zero[3] = {(T)0, (T)0, (T)0};
+  if (list_size < 1) return PNO_ERR_INVALID_ARG;
+  const int st = FN(pno_grid_create_)(ndims, radius, periodic_min ? periodic_min : zero,
+                                      periodic_max ? periodic_max : zero, periodic_min,
+                                      periodic_max, max_ppc, g);
+  if (st != PNO_OK) return st;
+  g->list_size = list_size;
+  g->n_total = list_size;
+  return PNO_OK;
+}
+
+/* initialize_grid! into a SpatialHashingCellList (nhs_grid.jl:227-281), serially in point
+ * order.  `cells` holds list_size lists of max_ppc entries (the DynamicVectorOfVectors
+ * backend), `coords` the flattened coordinates stored for each list (4 words; all zero is
+ * typemin(UInt128), unused) and `collisions` the collision flags.  atomic == 0 restates
+ * push_cell! (spatial_hashing.jl:91-107, SerialUpdate): the first cell pushed into a list
+ * sets its coordinates, another cell marks a collision.  atomic != 0 restates
+ * push_cell_atomic! (:109-126, used by the default ParallelUpdate): there the stored
+ * UInt128 is compared with a tuple, which is never equal, so the coordinates stay unused
+ * and every push of a cell whose flattened coordinates are not zero marks a collision. */
+int FN(pno_hash_build_)(const pno_grid* g, const T* y, int64_t n_y, int32_t* cells,
+                        int32_t* lengths, uint32_t* coords, uint8_t* collisions,
+                        int32_t atomic) {
+  const int64_t L = g->list_size;
+  const int d = g->ndims;
+  for (int64_t h = 0; h < L; ++h) {
+    lengths[h] = 0;
+    coords[4 * h] = coords[4 * h + 1] = coords[4 * h + 2] = coords[4 * h + 3] = 0;
+    collisions[h] = 0;
+  }
+  if (g->is_template) return PNO_OK;
+  for (int64_t i = 0; i < n_y; ++i) {
+    int64_t c[3] = {0, 0, 0};
+    FN(pno_cell_coords_dict_)(g, y + i * d, c);
+    const int64_t h = pno_spatial_hash(c, d, L);
+    if (lengths[h] + 1 > g->max_ppc) return PNO_ERR_CELL_FULL;
+    cells[h * g->max_ppc + lengths[h]] = (int32_t)i;
+    lengths[h] += 1;
+    uint32_t flat[4];
+    if (pno_coordinates_flattened(c, d, flat) != PNO_OK) return PNO_ERR_OUT_OF_DOMAIN;
+    uint32_t* cw = coords + 4 * h;
+    const int unused = !cw[0] && !cw[1] && !cw[2] && !cw[3];
+    const int same = cw[0] == flat[0] && cw[1] == flat[1] && cw[2] == flat[2] &&
+                     cw[3] == flat[3];
+    if (atomic) {
+      if (!same) collisions[h] = 1;
+    } else if (unused) {
+      for (int k = 0; k < 4; ++k) cw[k] = flat[k];
+    } else if (!same) {
+      collisions[h] = 1;
+    }
+  }
+  return PNO_OK;
+}
+
+/* Neighbour lists over a SpatialHashingCellList: nhs_grid.jl:519-575 with its collision
+ * handling (:479-513).  For each of the 3^d cells (CartesianIndices order) the cell's list
+ * is visited; when the list has a collision flag, or stored coordinates other than the
+ * cell's (check_cell_collision), each accepted point's own cell is compared with the
+ * visited cell (check_collision) and a point of another cell is skipped. */
+int FN(pno_hash_neighbor_lists_)(const pno_grid* g, const int32_t* cells,
+                                 const int32_t* lengths, const uint32_t* coords,
+                                 const uint8_t* collisions, const T* x, int64_t n_x,
+                                 const T* y, int64_t n_y, const int64_t* offsets,
+                                 int32_t* counts, int32_t* nbrs, int32_t n_threads) {
+  const int d = g->ndims;
+  const T r2 = FN(r2_)(g);
+  int status = PNO_OK;
+  (void)n_y;
+#pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(dynamic, 64)
+  for (int64_t i = 0; i < n_x; ++i) {
+    const T* xi = x + i * d;
+    int64_t ci[3] = {0, 0, 0};
+    FN(pno_cell_coords_dict_)(g, xi, ci);
+    int64_t cnt = 0;
+    int bad = 0;
+    const int o3n = d >= 3 ? 1 : 0, o2n = d >= 2 ? 1 : 0;
+    for (int o3 = -o3n; o3 <= o3n; ++o3)
+      for (int o2 = -o2n; o2 <= o2n; ++o2)
+        for (int o1 = -1; o1 <= 1; ++o1) {
+          int64_t nc[3] = {pno_wadd(ci[0], o1), d >= 2 ? pno_wadd(ci[1], o2) : 0,
+                           d >= 3 ? pno_wadd(ci[2], o3) : 0};
+          FN(periodic_wrap_)(g, nc);
+          const int64_t h = pno_spatial_hash(nc, d, g->list_size);
+          uint32_t flat[4];
+          if (pno_coordinates_flattened(nc, d, flat) != PNO_OK) {
+            bad = 1;
+            continue;
+          }
+          const uint32_t* cw = coords + 4 * h;
+          const int cell_collision = collisions[h] || cw[0] != flat[0] || cw[1] != flat[1] ||
+                                     cw[2] != flat[2] || cw[3] != flat[3];
+          for (int32_t a = 0; a < lengths[h]; ++a) {
+            const int64_t j = cells[h * g->max_ppc + a];
+            T pd[3];
+            if (!(FN(pair_d2_)(g, xi, y + j * d, pd) <= r2)) continue;
+            if (cell_collision) {
+              int64_t cj[3] = {0, 0, 0};
+              FN(pno_cell_coords_dict_)(g, y + j * d, cj);
+              if (cj[0] != nc[0] || cj[1] != nc[1] || cj[2] != nc[2]) continue;
+            }
+            if (offsets) nbrs[offsets[i] + cnt] = (int32_t)j;
+            ++cnt;
+          }
+        }
+    if (bad) status = PNO_ERR_OUT_OF_DOMAIN;
+    counts[i] = (int32_t)cnt;
+  }
+  return status;
+}
+
 #undef FN

@@ -180,6 +180,37 @@ def main():
         "message": "cell list is full. Use a larger `max_points_per_cell`.",
     }
 
+    # test/cell_lists/spatial_hashing.jl:2-67 -- hash collisions, with an empty and with a
+    # non-empty colliding cell (list_size = n_points), r = 0.1 + 10 eps().
+    cases["spatial_hashing_collisions"] = {
+        "source": "test/cell_lists/spatial_hashing.jl:2-67",
+        "radius": 0.1 + 10 * 2.220446049250313e-16,  # Float64 arithmetic, like Julia's
+        "cases": [
+            {"coords": [[-0.05, 0.05]], "list_size": 1,
+             "colliding_cells": [[-1, 0], [-2, -1]], "cell_points": [1],
+             "neighbors": [[1]]},
+            {"coords": [[-0.05, 0.05], [-0.15, -0.05]], "list_size": 2,
+             "colliding_cells": [[-1, 0], [-2, -1]], "cell_points": [1, 2],
+             "neighbors": [[1], [2]]},
+        ],
+    }
+
+    # test/cell_lists/spatial_hashing.jl:69-121 -- coordinates_flattened.
+    cases["coordinates_flattened"] = {
+        "source": "test/cell_lists/spatial_hashing.jl:69-121",
+        "values": [
+            {"cell": [1], "flat": str(1)},
+            {"cell": [-1], "flat": str(2**32 - 1)},
+            {"cell": [0], "flat": "0"},
+            {"cell": [-1, 1], "flat": str(2**32 - 1 + 2**32)},
+            {"cell": [1, 0, -1], "flat": str(1 + (2**32 - 1) * 2**64)},
+            {"cell": [2**31 - 1], "flat": str(2**31 - 1)},
+            {"cell": [-2**31], "flat": str(2**31)},
+            {"cell": [-2**31, 2**31 - 1, 0], "flat": str(2**31 + (2**31 - 1) * 2**32)},
+        ],
+        "inexact": [[2**31], [-2**31 - 1]],
+    }
+
     out = os.path.join(HERE, "reference_known_answers.json")
     with open(out, "w") as f:
         json.dump(cases, f, indent=1)

@@ -249,3 +249,65 @@ def test_mixed_precision_distance_in_float32(O):
     g64 = O.grid_create(2, rd, [-3.0, -3.0], [5.0, 3.0])
     off, nb = O.neighbor_lists(g64, O.build(g64, y), y, y)
     assert sorted(nb[off[0]:off[1]].tolist()) == [0]
+
+
+def test_spatial_hashing_collisions(O, golden):
+    """test/cell_lists/spatial_hashing.jl:2-67: colliding cells share a list, and the
+    traversal's collision checks keep each point to its own cell."""
+    c = golden["spatial_hashing_collisions"]
+    for case in c["cases"]:
+        y = np.array(case["coords"])
+        ls = case["list_size"]
+        g = O.grid_create_hash(2, c["radius"], ls)
+        for atomic in (True, False):
+            hl = O.hash_build(g, y, atomic=atomic)
+            a, b = case["colliding_cells"]
+            assert O.spatial_hash(a, ls) == O.spatial_hash(b, ls)
+            assert sorted((hl[tuple(a)] + 1).tolist()) == case["cell_points"]
+            assert sorted((hl[tuple(b)] + 1).tolist()) == case["cell_points"]
+            off, nb = O.hash_neighbor_lists(g, hl, y, y)
+            rows = [(nb[off[i]:off[i + 1]] + 1).tolist() for i in range(len(y))]
+            assert rows == case["neighbors"]
+
+
+def test_coordinates_flattened(O, golden):
+    c = golden["coordinates_flattened"]
+    for v in c["values"]:
+        assert O.coordinates_flattened(v["cell"]) == int(v["flat"])
+    for cell in c["inexact"]:
+        with pytest.raises(O.OracleError):
+            O.coordinates_flattened(cell)
+
+
+@pytest.mark.parametrize("shape", CLOUDS)
+def test_spatial_hashing_equals_trivial(O, pkg, shape):
+    """test/neighborhood_search.jl:186-469 with SpatialHashingCellList(list_size = 2n): the
+    lists equal brute force, for both push semantics and, on the smaller clouds, for a
+    list_size of 7 (every list shared by many cells)."""
+    W = pkg.workloads
+    r = 2.5
+    coords = W.reference_test_cloud(shape, r, seed=2)
+    d = len(shape)
+    mn = coords.min(axis=0) - r
+    mx = coords.max(axis=0) + r
+    toff, tnb = O.trivial_lists(O.grid_create(d, r, mn, mx), coords, coords)
+    for ls in ((2 * len(coords), 7) if len(coords) < 10000 else (2 * len(coords),)):
+        g = O.grid_create_hash(d, r, ls, max_ppc=len(coords))
+        for atomic in (True, False):
+            off, nb = O.hash_neighbor_lists(g, O.hash_build(g, coords, atomic=atomic),
+                                            coords, coords)
+            assert np.array_equal(off, toff)
+            for i in range(coords.shape[0]):
+                assert np.array_equal(np.sort(nb[off[i]:off[i + 1]]), tnb[toff[i]:toff[i + 1]])
+
+
+def test_spatial_hashing_periodic_neighbors(O, golden):
+    """test/neighborhood_search.jl:72-160 with SpatialHashingCellList(list_size = 2n)."""
+    c = golden["periodic_neighbors"]
+    for s in c["setups"]:
+        y = np.array(s["coords"])
+        g = O.grid_create_hash(y.shape[1], c["radius"], 2 * len(y),
+                               periodic_box=(np.array(s["box_min"]), np.array(s["box_max"])))
+        off, nb = O.hash_neighbor_lists(g, O.hash_build(g, y), y, y)
+        for i, exp in enumerate(c["expected"]):
+            assert sorted((nb[off[i]:off[i + 1]] + 1).tolist()) == exp, s["name"]
