@@ -119,6 +119,7 @@ typedef struct {
   double search_radius;
   int64_t n_binned;            /* points in the cell list after the last initialize/update */
   int64_t n_overflow;          /* points held in the incremental-update overflow lists     */
+  int64_t list_size;           /* SpatialHashingCellList lists (0: FullGridCellList)       */
 } pn_grid_info;
 
 typedef struct { int32_t* counts; } pn_count_params;       /* out int32[n_queries]         */
@@ -205,8 +206,22 @@ typedef struct {
  * integer-like radius is not representable here; periodic boxes with < 3 cells. */
 int pn_create(const pn_config* cfg, pn_search** out);
 
+/* GridNeighborhoodSearch{NDIMS}(; search_radius, n_points, periodic_box,
+ *   cell_list = SpatialHashingCellList{NDIMS}(; list_size, max_points_per_cell))
+ * (spatial_hashing.jl:79-89, nhs_grid.jl:77-129): an unbounded domain whose cells
+ * floor.(x ./ cell_size) (nhs_grid.jl:636-638; wrapped to 2:n_cells+1 with a periodic box)
+ * are hashed into list_size lists (spatial_hash, spatial_hashing.jl:142-156).  cfg's corners
+ * are not used; update_strategy must be PN_PARALLEL_UPDATE (update! rebuilds);
+ * max_points_per_cell > 0 limits each hash list ("cell list is full").  A cell coordinate
+ * must leave its neighbours inside Int32 (the reference's InexactError), and NaN
+ * coordinates are rejected: both PN_ERR_OUT_OF_DOMAIN.  The lists hold each cell's points
+ * as a separate run, so the traversal visits exactly the points of the 3^d cells -- the
+ * result of the reference's collision checks (nhs_grid.jl:479-513). */
+int pn_create_spatial_hashing(const pn_config* cfg, int64_t list_size, pn_search** out);
+
 /* copy_neighborhood_search(nhs, search_radius, n_points) (nhs_grid.jl:640-649,
- * full_grid.jl:179-185): same corners, periodic box, strategy and cell capacity. */
+ * full_grid.jl:179-185, spatial_hashing.jl:133-141): same corners or list size, periodic
+ * box, strategy and cell capacity. */
 int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
                    pn_search** out);
 

@@ -31,7 +31,8 @@ from . import _lib, build, workloads  # noqa: F401
 lib = _lib.load
 
 __all__ = [
-    "GridNeighborhoodSearch", "FullGridCellList", "PeriodicBox", "ParallelUpdate",
+    "GridNeighborhoodSearch", "FullGridCellList", "SpatialHashingCellList", "spatial_hash",
+    "PeriodicBox", "ParallelUpdate",
     "ParallelIncrementalUpdate", "initialize", "update", "foreach_point_neighbor",
     "requires_update", "copy_neighborhood_search", "cell_coords", "eachneighbor",
     "neighbor_lists", "CountNeighbors", "NeighborIndexSum", "NBodyAcceleration",
@@ -145,6 +146,34 @@ class FullGridCellList:
         self.max_corner = (self._max + pad).astype(T)
 
 
+class SpatialHashingCellList:
+    """SpatialHashingCellList{ndims}(; list_size, max_points_per_cell = 100)
+    (spatial_hashing.jl:79-89): the cells of an unbounded domain hashed into `list_size`
+    lists (about twice the number of points is the reference's advice).
+    `max_points_per_cell` limits each list; 0 removes the limit."""
+
+    def __init__(self, ndims, *, list_size, max_points_per_cell=100):
+        if isinstance(list_size, bool) or not isinstance(list_size, numbers.Integral) or \
+                list_size < 1:
+            raise ArgumentError("`list_size` must be a positive integer")
+        if int(ndims) not in (1, 2, 3):
+            raise ArgumentError("this GPU SpatialHashingCellList supports 1 to 3 dimensions")
+        self.ndims = int(ndims)
+        self.list_size = int(list_size)
+        self.max_points_per_cell = int(max_points_per_cell)
+
+
+def spatial_hash(cell, list_size: int) -> int:
+    """spatial_hash(cell, list_size) - 1 (spatial_hashing.jl:142-156): the 0-based list of
+    a cell, with Julia's wrapping Int64 products and xor and mod(h, list_size)."""
+    h = 0
+    for c, k in zip(cell, (73856093, 19349663, 83492791)):
+        h ^= (int(c) * k) & 0xFFFFFFFFFFFFFFFF
+    if h >= 1 << 63:
+        h -= 1 << 64
+    return h % int(list_size)
+
+
 class ParallelUpdate:
     """Full rebuild on update (the FullGridCellList default, nhs_grid.jl:135-144)."""
 
@@ -196,19 +225,23 @@ class GridNeighborhoodSearch:
     def __init__(self, ndims, *, search_radius=0.0, n_points=0, periodic_box=None,
                  cell_list=None, update_strategy=None, pair_cache=0):
         if cell_list is None:
-            raise ArgumentError("a FullGridCellList is required: the GPU search has no "
-                                "DictionaryCellList")
-        if not isinstance(cell_list, FullGridCellList):
-            raise ArgumentError("only FullGridCellList is supported")
+            raise ArgumentError("a FullGridCellList or SpatialHashingCellList is required: "
+                                "the GPU search has no DictionaryCellList")
+        if not isinstance(cell_list, (FullGridCellList, SpatialHashingCellList)):
+            raise ArgumentError("only FullGridCellList and SpatialHashingCellList are "
+                                "supported")
+        hashing = isinstance(cell_list, SpatialHashingCellList)
         if cell_list.ndims != ndims:
             raise ArgumentError(f"a {ndims}D cell list is required for a "
                                 f"GridNeighborhoodSearch{{{ndims}}}")
         if update_strategy is None:
             update_strategy = ParallelUpdate()
-        elif type(update_strategy) not in _STRATEGIES:
+        elif type(update_strategy) not in _STRATEGIES or \
+                (hashing and not isinstance(update_strategy, ParallelUpdate)):
+            options = "(ParallelUpdate,)" if hashing else \
+                "(ParallelUpdate, ParallelIncrementalUpdate)"
             raise ArgumentError(f"{update_strategy} is not a valid update strategy for this "
-                                "cell list. Available options are (ParallelUpdate, "
-                                "ParallelIncrementalUpdate)")
+                                f"cell list. Available options are {options}")
         if isinstance(search_radius, numbers.Integral) or isinstance(search_radius, bool):
             raise ArgumentError("`search_radius` cannot be an integer type, since computed "
                                 "distances will be converted to this type")
@@ -219,7 +252,7 @@ class GridNeighborhoodSearch:
                                 "same element type")
         self.ndims = int(ndims)
         self.eltype = T
-        self.mixed = T == np.float32 and cell_list.eltype == np.float64
+        self.mixed = not hashing and T == np.float32 and cell_list.eltype == np.float64
         self.coord_eltype = np.float64 if self.mixed else T
         self.search_radius = T(search_radius)
         self.n_points = int(n_points)
@@ -232,9 +265,10 @@ class GridNeighborhoodSearch:
         cfg.dtype = _lib.PN_FLOAT32 if C_ == np.float32 else _lib.PN_FLOAT64
         cfg.flags = _lib.PN_FLAG_FLOAT32_SEARCH if self.mixed else 0
         cfg.search_radius = float(self.search_radius)
-        for k in range(self.ndims):
-            cfg.min_corner[k] = float(C_(cell_list._min[k]))
-            cfg.max_corner[k] = float(C_(cell_list._max[k]))
+        if not hashing:
+            for k in range(self.ndims):
+                cfg.min_corner[k] = float(C_(cell_list._min[k]))
+                cfg.max_corner[k] = float(C_(cell_list._max[k]))
         if periodic_box is not None:
             cfg.periodic = 1
             for k in range(self.ndims):
@@ -245,7 +279,10 @@ class GridNeighborhoodSearch:
         cfg.max_points_per_cell = cell_list.max_points_per_cell
         self._cfg = cfg
         h = C.c_void_p()
-        rc = lib().pn_create(C.byref(cfg), C.byref(h))
+        if hashing:
+            rc = lib().pn_create_spatial_hashing(C.byref(cfg), cell_list.list_size, C.byref(h))
+        else:
+            rc = lib().pn_create(C.byref(cfg), C.byref(h))
         if rc != _lib.PN_OK:
             if rc == _lib.PN_ERR_INVALID_ARG and periodic_box is not None:
                 raise ArgumentError("the `GridNeighborhoodSearch` needs at least 3 cells in "
@@ -289,7 +326,7 @@ class GridNeighborhoodSearch:
             "grid_size": tuple(gi.grid_size[:d]), "n_cells": tuple(gi.n_cells[:d]),
             "min_corner": tuple(gi.min_corner[:d]), "max_corner": tuple(gi.max_corner[:d]),
             "cell_size": tuple(gi.cell_size[:d]), "search_radius": gi.search_radius,
-            "n_binned": gi.n_binned, "n_overflow": gi.n_overflow,
+            "n_binned": gi.n_binned, "n_overflow": gi.n_overflow, "list_size": gi.list_size,
             "periodic": bool(gi.periodic), "is_template": bool(gi.is_template),
         }
 
@@ -382,10 +419,14 @@ def copy_neighborhood_search(nhs, search_radius, n_points):
         return nhs._copy(search_radius, n_points)
     cl = nhs.cell_list
     T = _eltype(search_radius)
-    CT = np.result_type(cl.eltype, T)  # a Float64 cell list stays Float64
-    new_cl = FullGridCellList(min_corner=cl._min.astype(CT), max_corner=cl._max.astype(CT),
-                              search_radius=T(search_radius),
-                              max_points_per_cell=cl.max_points_per_cell)
+    if isinstance(cl, SpatialHashingCellList):  # spatial_hashing.jl:133-141
+        new_cl = SpatialHashingCellList(cl.ndims, list_size=cl.list_size,
+                                        max_points_per_cell=cl.max_points_per_cell)
+    else:
+        CT = np.result_type(cl.eltype, T)  # a Float64 cell list stays Float64
+        new_cl = FullGridCellList(min_corner=cl._min.astype(CT), max_corner=cl._max.astype(CT),
+                                  search_radius=T(search_radius),
+                                  max_points_per_cell=cl.max_points_per_cell)
     return GridNeighborhoodSearch(nhs.ndims, search_radius=T(search_radius), n_points=n_points,
                                   periodic_box=nhs.periodic_box, cell_list=new_cl,
                                   update_strategy=nhs.update_strategy)
@@ -656,10 +697,11 @@ def cell_coords(coords, nhs: GridNeighborhoodSearch):
 
 
 def export_cells(nhs: GridNeighborhoodSearch):
-    """(counts[prod(grid_size)], points) with each cell's points ascending (0-based)."""
+    """(counts[prod(grid_size)], points) with each cell's points ascending (0-based); for a
+    SpatialHashingCellList, per hash list (counts[list_size])."""
     torch = _torch()
     gi = nhs.grid_info()
-    n_total = int(np.prod(gi["grid_size"]))
+    n_total = gi["list_size"] or int(np.prod(gi["grid_size"]))
     counts = torch.empty(n_total, dtype=torch.int32, device="cuda")
     pts = torch.empty(max(int(gi["n_binned"]), 1), dtype=torch.int32, device="cuda")
     rc = lib().pn_export_cells(nhs._h, _ptr(counts), _ptr(pts), _stream())
@@ -678,6 +720,19 @@ def eachneighbor(coords, nhs: GridNeighborhoodSearch):
     starts = np.concatenate([[0], np.cumsum(counts)])
     d = nhs.ndims
     out = []
+    if gi["list_size"] > 0:
+        # SpatialHashingCellList: each cell's whole hash list, like points_in_cell
+        rng = [range(-1, 2) if k < d else range(0, 1) for k in range(3)]
+        for o3 in rng[2]:
+            for o2 in rng[1]:
+                for o1 in rng[0]:
+                    cc = [c[0] + o1, c[1] + o2 if d > 1 else 0, c[2] + o3 if d > 2 else 0]
+                    if nhs.periodic_box is not None:
+                        for k in range(d):
+                            cc[k] = (cc[k] - 2) % gi["n_cells"][k] + 2
+                    h = spatial_hash(cc[:d], gi["list_size"])
+                    out.extend(pts[starts[h]:starts[h + 1]].tolist())
+        return np.asarray(out, dtype=np.int64)
     rng = [range(-1, 2) if k < d else range(0, 1) for k in range(3)]
     for o3 in rng[2]:
         for o2 in rng[1]:

@@ -60,6 +60,7 @@ class pn_grid_info(C.Structure):
         ("is_template", C.c_int32), ("grid_size", I3), ("n_cells", I3),
         ("min_corner", D3), ("max_corner", D3), ("cell_size", D3),
         ("search_radius", C.c_double), ("n_binned", C.c_int64), ("n_overflow", C.c_int64),
+        ("list_size", C.c_int64),
     ]
 
 
@@ -113,6 +114,7 @@ _SIGNATURES = {
     "pn_abi_version": (C.c_int, []),
     "pn_launch_count": (C.c_ulonglong, []),
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),
+    "pn_create_spatial_hashing": (C.c_int, [C.POINTER(pn_config), C.c_int64, C.POINTER(_P)]),
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),
     "pn_destroy": (C.c_int, [_P]),
     "pn_set_rebuild_fraction": (C.c_int, [_P, C.c_double]),

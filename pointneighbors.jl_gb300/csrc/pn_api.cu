@@ -158,15 +158,57 @@ static int geometry(pn_search* s) {
   return PN_OK;
 }
 
+// GridNeighborhoodSearch over a SpatialHashingCellList: no corners; the cell size is r, or
+// the periodic one as above (nhs_grid.jl:102-124); n_total = list_size hash lists.
+template <typename R>
+static int geometry_hash(pn_search* s) {
+  pn_config& c = s->cfg;
+  const int d = c.ndims;
+  const R r = (R)c.search_radius;
+  s->radius = (double)r;
+  s->is_template = (double)r < 2.220446049250313e-16 ? 1 : 0;
+  if (s->list_size < 1 || s->list_size > (int64_t)INT32_MAX - 1) return PN_ERR_INVALID_ARG;
+  for (int k = 0; k < 3; ++k) {
+    s->grid_size[k] = 1;
+    s->n_cells[k] = -1;
+    s->min_pad[k] = s->max_pad[k] = 0.0;
+    s->cell_size[k] = k < d ? (double)r : 1.0;
+    s->box_size[k] = 0.0;
+  }
+  s->n_total = s->is_template ? 0 : (int32_t)s->list_size;
+  s->periodic = 0;
+  if (c.periodic && !s->is_template) {
+    s->periodic = 1;
+    for (int k = 0; k < d; ++k) {
+      c.periodic_min[k] = (double)(R)c.periodic_min[k];
+      c.periodic_max[k] = (double)(R)c.periodic_max[k];
+      const R size = (R)((R)c.periodic_max[k] - (R)c.periodic_min[k]);
+      s->box_size[k] = (double)size;
+      const double nc = std::floor(((double)size + 10.0 * 2.220446049250313e-16) / (double)r);
+      if (!(nc >= 3.0)) return PN_ERR_INVALID_ARG;  // "needs at least 3 cells"
+      if (nc > 1e9) return PN_ERR_INVALID_ARG;
+      s->n_cells[k] = (int64_t)nc;
+      s->cell_size[k] = (double)(R)(size / (R)s->n_cells[k]);
+    }
+  }
+  return PN_OK;
+}
+
 static int geometry_for(pn_search* s) {
   if (s->cfg.flags & ~PN_FLAG_FLOAT32_SEARCH) return PN_ERR_INVALID_ARG;
   s->mixed = (s->cfg.flags & PN_FLAG_FLOAT32_SEARCH) ? 1 : 0;
   if (s->mixed && s->dtype != PN_FLOAT64) return PN_ERR_INVALID_ARG;
+  if (s->hashed) {
+    if (s->cfg.update_strategy != PN_PARALLEL_UPDATE) return PN_ERR_INVALID_ARG;
+    return (s->mixed || s->dtype == PN_FLOAT32) ? geometry_hash<float>(s)
+                                                : geometry_hash<double>(s);
+  }
   if (s->mixed) return geometry<double, float>(s);
   return s->dtype == PN_FLOAT64 ? geometry<double, double>(s) : geometry<float, float>(s);
 }
 
-static int create(const pn_config* cfg, pn_search** out) {
+// list_size > 0: a SpatialHashingCellList with that many lists, else a FullGridCellList.
+static int create(const pn_config* cfg, int64_t list_size, pn_search** out) {
   if (!cfg || !out) return PN_ERR_INVALID_ARG;
   *out = nullptr;
   if (cfg->ndims < 1 || cfg->ndims > 3) return PN_ERR_INVALID_ARG;
@@ -181,6 +223,8 @@ static int create(const pn_config* cfg, pn_search** out) {
   s->cfg = *cfg;
   s->ndims = cfg->ndims;
   s->dtype = cfg->dtype;
+  s->hashed = list_size > 0 ? 1 : 0;
+  s->list_size = list_size > 0 ? list_size : 0;
   int rc = geometry_for(s);
   if (rc != PN_OK) {
     delete s;
@@ -201,6 +245,7 @@ static int create(const pn_config* cfg, pn_search** out) {
          cudaMalloc(&s->d_ovf_start, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
          cudaMalloc(&s->d_ovf_n, sizeof(int32_t) * 4) == cudaSuccess &&
          cudaMalloc(&s->d_scan_state, sizeof(unsigned long long) * (s->scan_tiles + 1)) == cudaSuccess;
+    if (ok && s->hashed) ok = cudaMalloc(&s->d_hbucket, sizeof(int32_t) * (nt + 1)) == cudaSuccess;
     if (ok && cfg->n_points > 0) ok = ensure_capacity(s, cfg->n_points) == PN_OK;
   }
   if (!ok) {
@@ -228,7 +273,12 @@ int pn_abi_version(void) { return PN_ABI_VERSION; }
 
 unsigned long long pn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
-int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, out); }
+int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, 0, out); }
+
+int pn_create_spatial_hashing(const pn_config* cfg, int64_t list_size, pn_search** out) {
+  if (list_size < 1) return PN_ERR_INVALID_ARG;
+  return create(cfg, list_size, out);
+}
 
 int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
                    pn_search** out) {
@@ -236,7 +286,7 @@ int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points
   pn_config c = tmpl->cfg;
   c.search_radius = search_radius;
   c.n_points = n_points;
-  const int rc = create(&c, out);
+  const int rc = create(&c, tmpl->list_size, out);
   if (rc == PN_OK) (*out)->rebuild_fraction = tmpl->rebuild_fraction;
   return rc;
 }
@@ -260,7 +310,8 @@ int pn_destroy(pn_search* s) {
   void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
                   s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_b0,
-                  s->d_pc_mask};
+                  s->d_pc_mask,    s->d_hkey_t,     s->d_hkey_tmp,  s->d_hkey,
+                  s->d_hcellidx,   s->d_hcell,      s->d_hbucket,   s->d_hscan_state};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->h_ovf_n) cudaFreeHost(s->h_ovf_n);
@@ -279,9 +330,15 @@ int pn_initialize(pn_search* s, const void* y, int64_t n_y, const int32_t* eachi
     s->initialized = false;
     return record(s, PN_OK, st);
   }
-  int rc = s->dtype == PN_FLOAT64
-               ? build<double>(s, (const double*)y, n_y, eachindex_y, n_eachindex_y, st)
-               : build<float>(s, (const float*)y, n_y, eachindex_y, n_eachindex_y, st);
+  int rc;
+  if (s->hashed)
+    rc = s->dtype == PN_FLOAT64
+             ? build_hash<double>(s, (const double*)y, n_y, eachindex_y, n_eachindex_y, st)
+             : build_hash<float>(s, (const float*)y, n_y, eachindex_y, n_eachindex_y, st);
+  else
+    rc = s->dtype == PN_FLOAT64
+             ? build<double>(s, (const double*)y, n_y, eachindex_y, n_eachindex_y, st)
+             : build<float>(s, (const float*)y, n_y, eachindex_y, n_eachindex_y, st);
   if (rc == PN_OK) {
     s->initialized = true;
     s->full_binned = eachindex_y == nullptr;
@@ -391,6 +448,7 @@ int pn_get_grid_info(const pn_search* s, pn_grid_info* out) {
     out->cell_size[k] = s->cell_size[k];
   }
   out->search_radius = s->radius;
+  out->list_size = s->list_size;
   out->n_binned = s->n_binned;
   // the mover count of the last update, once its asynchronous read-back has landed
   out->n_overflow = (s->ovf_pending && cudaEventQuery(s->ev_ovf) == cudaSuccess)
@@ -405,6 +463,8 @@ int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out) {
   tmp.cfg = *cfg;
   tmp.ndims = cfg->ndims;
   tmp.dtype = cfg->dtype;
+  tmp.hashed = 0;
+  tmp.list_size = 0;
   int rc = geometry_for(&tmp);
   if (rc != PN_OK) return rc;
   return pn_get_grid_info(&tmp, out);

@@ -467,6 +467,238 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   return cuda_status(cudaGetLastError());
 }
 
+// ---------------------------------------------------------------- SpatialHashingCellList
+// The same counting sort with the hash list as the bucket (spatial_hashing.jl:91-126 pushes
+// into the hash lists).  Inside a list the points are ranked by cell, then by first
+// coordinate and index, so that each cell is a contiguous, x-sorted run; a scan of the
+// run heads numbers the cells, which become the entries (x, y, z, first slot) that the
+// traversal matches against the cells of a stencil.  The reference instead stores one
+// coordinate tuple and a collision flag per list and compares each point's cell while
+// traversing (nhs_grid.jl:479-513); both visit exactly the points of the stencil's cells.
+template <typename T, int D, bool PER>
+__global__ void __launch_bounds__(BIN_THREADS)
+k_hash_bin(const GridDev<T> g, int64_t list_size, const T* __restrict__ y, int64_t n_y,
+           const int32_t* __restrict__ idx, int32_t m, int32_t* __restrict__ bucket_of,
+           int4* __restrict__ key_of, int32_t* __restrict__ slot_of,
+           int32_t* __restrict__ counts, int32_t* __restrict__ err) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = base + threadIdx.x;
+    int32_t bucket = -1;
+    int32_t c[3] = {0, 0, 0};
+    if (t < m) {
+      const int64_t i = idx ? (int64_t)idx[t] : t;
+      if (i < 0 || i >= n_y) {
+        set_error(err, PN_ERR_INVALID_ARG);
+      } else {
+        bool ok = true;
+#pragma unroll
+        for (int k = 0; k < D; ++k) ok &= hash_cell_1d(g, PER, k, y[i * D + k], c[k]);
+        if (ok) bucket = spatial_hash<D>(c, list_size);
+        else set_error(err, PN_ERR_OUT_OF_DOMAIN);
+      }
+    }
+    const unsigned valid = __ballot_sync(0xffffffffu, bucket >= 0);
+    if (bucket >= 0) {
+      const unsigned peers = __match_any_sync(valid, bucket);
+      const int leader = __ffs(peers) - 1;
+      int32_t b = 0;
+      if (lane == leader) b = atomicAdd(&counts[bucket], __popc(peers));
+      b = __shfl_sync(peers, b, leader);
+      slot_of[t] = b + __popc(peers & lanemask_lt());
+    }
+    if (t < m) {
+      bucket_of[t] = bucket;
+      key_of[t] = make_int4(c[0], c[1], c[2], 0);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256)
+k_hash_scatter(const int32_t* __restrict__ bucket_of, const int32_t* __restrict__ slot_of,
+               const int4* __restrict__ key_of, const int32_t* __restrict__ idx, int32_t m,
+               const int32_t* __restrict__ start, int32_t* __restrict__ tmp_perm,
+               int32_t* __restrict__ bucket_of_slot, int4* __restrict__ key_tmp) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const int32_t b = bucket_of[t];
+  if (b < 0) return;
+  const int32_t p = start[b] + slot_of[t];
+  tmp_perm[p] = idx ? idx[t] : (int32_t)t;
+  bucket_of_slot[p] = b;
+  key_tmp[p] = key_of[t];
+}
+
+__device__ __forceinline__ bool key_less(int4 a, int4 b) {
+  if (a.x != b.x) return a.x < b.x;
+  if (a.y != b.y) return a.y < b.y;
+  return a.z < b.z;
+}
+__device__ __forceinline__ bool key_eq(int4 a, int4 b) {
+  return a.x == b.x && a.y == b.y && a.z == b.z;
+}
+
+// Rank each slot inside its list by (cell, first coordinate, point index): a total order
+// (NaN coordinates are not binned), so every slot gets a distinct destination.
+template <typename T, int D>
+__global__ void __launch_bounds__(256)
+k_hash_finalize(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ bucket_of_slot,
+                const int4* __restrict__ key_tmp, const int32_t* __restrict__ start,
+                int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
+                T* __restrict__ pos, int4* __restrict__ key) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= start[n_total]) return;
+  const int32_t b = bucket_of_slot[k];
+  const int32_t s = start[b], e = start[b + 1];
+  const int32_t v = tmp_perm[k];
+  const int4 kv = key_tmp[k];
+  const T xv = y[(int64_t)v * D];
+  int32_t rank = 0;
+  for (int32_t q = s; q < e; ++q) {
+    const int32_t u = __ldg(&tmp_perm[q]);
+    const int4 ku = __ldg(&key_tmp[q]);
+    const T xu = __ldg(&y[(int64_t)u * D]);
+    rank += key_less(ku, kv) || (key_eq(ku, kv) && ((xu < xv) || (xu == xv && u < v)));
+  }
+  const int32_t dst = s + rank;
+  perm[dst] = v;
+  key[dst] = kv;
+  T p[D];
+#pragma unroll
+  for (int d = 0; d < D; ++d) p[d] = y[(int64_t)v * D + d];
+  store_pos<T, D>(pos, dst, p);
+}
+
+// head[k] = 1 where slot k starts a cell's run (slots [n, m) hold 0 for the scan).
+__global__ void __launch_bounds__(256)
+k_hash_heads(const int32_t* __restrict__ bucket_of_slot, const int4* __restrict__ key,
+             const int32_t* __restrict__ n_slots, int32_t m, int32_t* __restrict__ head) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const int32_t n = *n_slots;
+  int32_t h = 0;
+  if (k < n)
+    h = (k == 0 || bucket_of_slot[k] != bucket_of_slot[k - 1] || !key_eq(key[k], key[k - 1]))
+            ? 1 : 0;
+  head[k] = h;
+}
+
+// The cell entries (a sentinel entry after the last closes its run) and each list's first
+// entry.
+__global__ void __launch_bounds__(256)
+k_hash_cells(const int32_t* __restrict__ head, const int32_t* __restrict__ cellidx,
+             const int4* __restrict__ key, const int32_t* __restrict__ n_slots, int32_t m,
+             int4* __restrict__ hcell) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t n = *n_slots;
+  if (k < n && head[k]) {
+    const int4 c = key[k];
+    hcell[cellidx[k]] = make_int4(c.x, c.y, c.z, (int32_t)k);
+  }
+  if (k == 0) hcell[cellidx[m]] = make_int4(0, 0, 0, n);
+}
+
+__global__ void __launch_bounds__(256)
+k_hash_buckets(const int32_t* __restrict__ start, const int32_t* __restrict__ cellidx,
+               int32_t n_lists, int32_t* __restrict__ hbucket) {
+  const int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (b <= n_lists) hbucket[b] = cellidx[start[b]];
+}
+
+static int ensure_hash_capacity(pn_search* s, int64_t n) {
+  if (n <= s->hash_cap && s->d_hkey) return PN_OK;
+  void* ptrs[] = {s->d_hkey_t, s->d_hkey_tmp, s->d_hkey, s->d_hcellidx, s->d_hcell,
+                  s->d_hscan_state};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  s->d_hkey_t = s->d_hkey_tmp = s->d_hkey = s->d_hcell = nullptr;
+  s->d_hcellidx = nullptr;
+  s->d_hscan_state = nullptr;
+  s->hash_cap = 0;
+  const int64_t cap = std::max<int64_t>(s->cap, n);
+  bool ok = cudaMalloc(&s->d_hkey_t, sizeof(int4) * cap) == cudaSuccess &&
+            cudaMalloc(&s->d_hkey_tmp, sizeof(int4) * cap) == cudaSuccess &&
+            cudaMalloc(&s->d_hkey, sizeof(int4) * (cap + 1)) == cudaSuccess &&
+            cudaMalloc(&s->d_hcellidx, sizeof(int32_t) * (cap + 1)) == cudaSuccess &&
+            cudaMalloc(&s->d_hcell, sizeof(int4) * (cap + 1)) == cudaSuccess &&
+            cudaMalloc(&s->d_hscan_state,
+                       sizeof(unsigned long long) * (scan_tile_count(cap) + 1)) == cudaSuccess;
+  if (!ok) {
+    cudaGetLastError();
+    return PN_ERR_OUT_OF_MEMORY;
+  }
+  s->hash_cap = cap;
+  return PN_OK;
+}
+
+template <typename T>
+int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_idx,
+               cudaStream_t st) {
+  const int64_t m = idx ? n_idx : n_y;
+  int rc = ensure_capacity(s, std::max(m, n_y));
+  if (rc == PN_OK) rc = ensure_hash_capacity(s, s->cap);
+  if (rc != PN_OK) return rc;
+  const int32_t nl = s->n_total;
+  cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * nl, st);
+  if (m > 0) {
+    const GridDev<T> g = make_grid<T>(s);
+    const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
+    const bool per = s->periodic != 0;
+#define PN_HASH_BIN(DD, PP)                                                                 \
+  k_hash_bin<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(g, s->list_size, y, n_y, idx,       \
+                                                        (int32_t)m, s->d_cell_of, s->d_hkey_t, \
+                                                        s->d_slot_of, s->d_counts, s->d_err)
+    switch (s->ndims * 2 + (per ? 1 : 0)) {
+      case 2: PN_HASH_BIN(1, false); break;
+      case 3: PN_HASH_BIN(1, true); break;
+      case 4: PN_HASH_BIN(2, false); break;
+      case 5: PN_HASH_BIN(2, true); break;
+      case 6: PN_HASH_BIN(3, false); break;
+      default: PN_HASH_BIN(3, true); break;
+    }
+#undef PN_HASH_BIN
+    count_launch();
+  }
+  scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
+  if (m > 0) {
+    const int b = div_up(m, 256);
+    k_hash_scatter<<<b, 256, 0, st>>>(s->d_cell_of, s->d_slot_of, s->d_hkey_t, idx, (int32_t)m,
+                                      s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
+                                      s->d_hkey_tmp); count_launch();
+    T* pos = static_cast<T*>(s->d_pos);
+    switch (s->ndims) {
+      case 1: k_hash_finalize<T, 1><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey); break;
+      case 2: k_hash_finalize<T, 2><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey); break;
+      default: k_hash_finalize<T, 3><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey); break;
+    }
+    count_launch();
+    // the heads go into d_slot_of (free again after the scatter), their scan into hcellidx
+    k_hash_heads<<<b, 256, 0, st>>>(s->d_cell_of_slot, s->d_hkey, s->d_start + nl, (int32_t)m,
+                                    s->d_slot_of); count_launch();
+    scan_counts(s->d_slot_of, (int32_t)m, s->d_hcellidx, s->d_hscan_state,
+                scan_tile_count(m), s->d_err, st);
+    k_hash_cells<<<b, 256, 0, st>>>(s->d_slot_of, s->d_hcellidx, s->d_hkey, s->d_start + nl,
+                                    (int32_t)m, s->d_hcell); count_launch();
+    k_hash_buckets<<<div_up((int64_t)nl + 1, 256), 256, 0, st>>>(s->d_start, s->d_hcellidx, nl,
+                                                                 s->d_hbucket); count_launch();
+  } else {
+    cudaMemsetAsync(s->d_hbucket, 0, sizeof(int32_t) * ((int64_t)nl + 1), st);
+  }
+  s->n_binned = m;
+  s->pc_valid = false;
+  s->ovf_active = false;
+  s->main_perm_valid = false;
+  s->n_ovf = 0;
+  s->updates_since_build = 0;
+  return cuda_status(cudaGetLastError());
+}
+
+template int build_hash<float>(pn_search*, const float*, int64_t, const int32_t*, int64_t,
+                               cudaStream_t);
+template int build_hash<double>(pn_search*, const double*, int64_t, const int32_t*, int64_t,
+                                cudaStream_t);
+
 // ---------------------------------------------------------------- pieces of the batched build
 // (pn_batch.cu bins the points of many clouds itself, then reuses these on the
 // concatenated cell and slot arrays.)

@@ -27,6 +27,8 @@ struct pn_search {
   // geometry (values exact in T, stored as double)
   int32_t ndims, dtype, periodic, is_template;
   int32_t mixed;        // PN_FLAG_FLOAT32_SEARCH: Float64 coordinates, Float32 pair arithmetic
+  int32_t hashed;       // SpatialHashingCellList (n_total = list_size hash lists)
+  int64_t list_size;
   int64_t grid_size[3], n_cells[3];
   double min_pad[3], max_pad[3], cell_size[3], box_size[3];
   double radius;
@@ -83,6 +85,19 @@ struct pn_search {
   int64_t pc_mask_cap = 0;
   int64_t pc_rows = 0;
 
+  // SpatialHashingCellList: the slots of a hash list are sorted by cell, then by first
+  // coordinate; every distinct cell is an entry (x, y, z, first slot) of hcell, and the
+  // entries of list h are hcell[hbucket[h] .. hbucket[h + 1]) (a sentinel entry closes the
+  // last run)
+  int4* d_hkey_t = nullptr;         // [cap] cell of the t-th binned point (w unused)
+  int4* d_hkey_tmp = nullptr;       // [cap] cells in scatter order
+  int4* d_hkey = nullptr;           // [cap] cell of each slot
+  int32_t* d_hcellidx = nullptr;    // [cap + 1] scan of the cell heads
+  int4* d_hcell = nullptr;          // [cap + 1] cell entries
+  int32_t* d_hbucket = nullptr;     // [list_size + 1]
+  unsigned long long* d_hscan_state = nullptr;
+  int64_t hash_cap = 0;
+
   // state
   bool initialized = false;
   bool full_binned = false;   // every point of y is binned (no eachindex_y subset)
@@ -111,6 +126,9 @@ int cuda_status(cudaError_t e);
 template <typename T>
 int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_idx,
           cudaStream_t st);
+template <typename T>
+int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_idx,
+               cudaStream_t st);
 template <typename T>
 int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st);
 template <typename T>

@@ -64,8 +64,8 @@ template <typename T>
 struct GridDev {
   int32_t n[3];        // padded FullGridCellList size per dimension
   int32_t ncell[3];    // periodic cells per dimension (0 when not periodic)
-  int32_t n_total;     // prod(n)
-  int32_t pad_;
+  int32_t n_total;     // prod(n), or the hash lists of a SpatialHashingCellList
+  int32_t hashed;      // SpatialHashingCellList: cells floor(x / cell_size), no offset
   T min_pad[3];        // padded min corner (cell (1,1,1) starts here)
   T cell_size[3];
   T box_min[3], box_max[3];  // periodic box corners
@@ -82,7 +82,7 @@ __device__ __forceinline__ void cell_coords_exact(const GridDev<T>& g, bool peri
 #pragma unroll
   for (int k = 0; k < D; ++k) {
     const T q = xdiv(xsub(x[k], g.min_pad[k]), g.cell_size[k]);
-    int64_t ck = wadd(floor_to_int(q), 1);
+    int64_t ck = wadd(floor_to_int(q), g.hashed ? 0 : 1);
     if (periodic) ck = wadd(jl_mod(wsub(ck, 2), (int64_t)g.ncell[k]), 2);
     c[k] = ck;
   }
@@ -118,6 +118,34 @@ __device__ __forceinline__ bool cell_coord_1d(const GridDev<T>& g, bool periodic
   return c <= g.n[k] - 1;
 }
 
+// SpatialHashingCellList cell coordinate (nhs_grid.jl:636-638): floor(x / cell_size), with
+// a periodic box mod(c - 2, n_cells) + 2.  False when the cell or one of its neighbours
+// would leave Int32 (the reference's InexactError in coordinates_flattened) or x is NaN.
+template <typename T>
+__device__ __forceinline__ bool hash_cell_1d(const GridDev<T>& g, bool periodic, int k, T xk,
+                                             int32_t& c) {
+  const T q = xdiv(xk, g.cell_size[k]);
+  if (!periodic) {
+    const double fl = (double)xfloor(q);
+    const bool ok = fl >= -2147483647.0 && fl <= 2147483646.0;  // false for NaN
+    c = ok ? (int32_t)fl : 0;
+    return ok;
+  }
+  c = (int32_t)(jl_mod(wsub(floor_to_int(q), 2), (int64_t)g.ncell[k]) + 2);
+  return !(xk != xk);
+}
+
+// spatial_hash (spatial_hashing.jl:142-156, Ihmsen et al.): Int64 products and xor that
+// wrap around like Julia's, then mod(h, list_size); 0-based.
+template <int D>
+__device__ __forceinline__ int32_t spatial_hash(const int32_t* c, int64_t list_size) {
+  uint64_t h = (uint64_t)(int64_t)c[0] * 73856093ull;
+  if (D >= 2) h ^= (uint64_t)(int64_t)c[1] * 19349663ull;
+  if (D >= 3) h ^= (uint64_t)(int64_t)c[2] * 83492791ull;
+  int64_t m = (int64_t)h % list_size;
+  return (int32_t)(m < 0 ? m + list_size : m);
+}
+
 // A point outside the periodic box [min, max) (the periodic traversal then checks every
 // candidate for a periodic image; inside the box it can skip that check in the interior).
 template <typename T>
@@ -151,6 +179,7 @@ template <typename T>
 inline GridDev<T> make_grid(const pn_search* s) {
   GridDev<T> g{};
   g.n_total = s->n_total;
+  g.hashed = s->hashed;
   for (int k = 0; k < 3; ++k) {
     const bool used = k < s->ndims;
     g.n[k] = used ? (int32_t)s->grid_size[k] : 1;

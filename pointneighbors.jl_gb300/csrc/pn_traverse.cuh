@@ -67,6 +67,13 @@ struct TravArgs {
   const ulonglong2* pc_mask;
   int64_t pc_stride;
   const int32_t* pc_any_fallback;  // device flag: some query was marked for the fallback
+  // SpatialHashingCellList (or null): list h's cells are the entries hash_cell[hash_list[h]
+  // .. hash_list[h + 1]), each (x, y, z, first slot), a cell's run ending at the next
+  // entry's first slot; hash_key[slot] is the slot's own cell
+  const int32_t* hash_list;
+  const int4* hash_cell;
+  const int4* hash_key;
+  int64_t hash_size;
 };
 
 template <typename T, int D>
@@ -1157,6 +1164,113 @@ k_trav_list(const TravArgs<T> a, const typename F::Params p) {
     for (int d = 0; d < D; ++d) q.x[d] = (T)0;
   }
   traverse_query<T, D, PER, F>(a, p, q, c, valid);
+}
+
+// ================================================================== spatial hashing
+// The run of cell cc: its hash list's entries are searched for the cell (one entry unless
+// cells collide in the list); an empty run when the cell has no points.
+template <int D>
+__device__ __forceinline__ void hash_run(const int32_t* __restrict__ list,
+                                         const int4* __restrict__ cell, int64_t size,
+                                         const int32_t* cc, int32_t& b, int32_t& e) {
+  const int32_t h = spatial_hash<D>(cc, size);
+  const int32_t e1 = __ldg(&list[h + 1]);
+  b = e = 0;
+  for (int32_t k = __ldg(&list[h]); k < e1; ++k) {
+    const int4 c = __ldg(&cell[k]);
+    if (c.x == cc[0] && (D < 2 || c.y == cc[1]) && (D < 3 || c.z == cc[2])) {
+      b = c.w;
+      e = __ldg(&cell[k + 1]).w;
+      return;
+    }
+  }
+}
+
+// One query over a SpatialHashingCellList: the 3^d cells in the reference's
+// CartesianIndices order, each cell's run in slot order.  Cells need not line up with a
+// periodic box's faces here, so with one every candidate is checked for its image.
+template <typename T, int D, bool PER, class F>
+__device__ __forceinline__ void traverse_query_hash(const TravArgs<T>& a,
+                                                    const typename F::Params& p,
+                                                    Query<T, D>& q, const int32_t* c,
+                                                    bool valid) {
+  typename F::Acc acc;
+  if (!valid) return;
+  F::init(acc, p, q);
+  constexpr int OZ = D == 3 ? 1 : 0;
+  constexpr int OY = D >= 2 ? 1 : 0;
+#pragma unroll 1
+  for (int oz = -OZ; oz <= OZ; ++oz) {
+#pragma unroll 1
+    for (int oy = -OY; oy <= OY; ++oy) {
+#pragma unroll 1
+      for (int ox = -1; ox <= 1; ++ox) {
+        int32_t cc[3] = {c[0] + ox, c[1] + oy, c[2] + oz};
+        if (PER) {
+#pragma unroll
+          for (int k = 0; k < D; ++k) cc[k] = pwrap(cc[k], a.g.ncell[k]);
+        }
+        int32_t b, e;
+        hash_run<D>(a.hash_list, a.hash_cell, a.hash_size, cc, b, e);
+        scan_any<T, D, PER, F>(a, p, acc, q, PER, b, e);
+      }
+    }
+  }
+  F::finish(acc, p, q);
+}
+
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_trav_hash_sorted(const TravArgs<T> a, const typename F::Params p) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t n_slots = a.start[a.g.n_total];
+  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
+  Query<T, D> q;
+  const bool valid = k < n_slots;
+  q.i = valid ? a.perm[k] : -1;
+  q.q = q.i;
+  q.k = (int32_t)k;
+  int32_t c[3] = {0, 0, 0};
+  if (valid) {
+    load_pos<T, D>(a.pos, k, q.x);
+    const int4 key = __ldg(&a.hash_key[k]);
+    c[0] = key.x;
+    c[1] = key.y;
+    c[2] = key.z;
+  }
+  traverse_query_hash<T, D, PER, F>(a, p, q, c, valid);
+}
+
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_trav_hash_list(const TravArgs<T> a, const typename F::Params p) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if ((int64_t)blockIdx.x * blockDim.x >= a.n_q) return;  // whole block idle
+  Query<T, D> q;
+  bool valid = t < a.n_q;
+  q.i = valid ? (a.qlist ? a.qlist[t] : (int32_t)t) : -1;
+  q.q = (int32_t)t;
+  q.k = -1;
+  int32_t c[3] = {0, 0, 0};
+  if (valid && (q.i < 0 || q.i >= a.n_x)) {
+    set_error(a.err, PN_ERR_INVALID_ARG);
+    F::fail(p, q);
+    valid = false;
+  }
+  if (valid) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      q.x[k] = a.x[(int64_t)q.i * D + k];
+      ok &= hash_cell_1d(a.g, PER, k, q.x[k], c[k]);
+    }
+    if (!ok) {
+      set_error(a.err, PN_ERR_OUT_OF_DOMAIN);
+      F::fail(p, q);
+      valid = false;
+    }
+  }
+  traverse_query_hash<T, D, PER, F>(a, p, q, c, valid);
 }
 
 // ================================================================== precomputed lists

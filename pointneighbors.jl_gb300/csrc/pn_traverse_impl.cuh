@@ -150,6 +150,14 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
       else                                                                              \
         k_lists_query<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);      \
       count_launch();                                                                   \
+    } else if (a.hash_cell != nullptr) {                                                \
+      if constexpr (!has_row_hook<F<T, DD>>::value) {                                   \
+        if (sorted)                                                                     \
+          k_trav_hash_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p); \
+        else                                                                            \
+          k_trav_hash_list<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p); \
+        count_launch();                                                                 \
+      }                                                                                 \
     } else if (sorted) {                                                                \
       k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
       count_launch();                                                                   \
@@ -225,6 +233,12 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
   a.err = s->d_err;
   a.outside = s->d_err + 1;
   a.unsorted = s->d_err + 3;
+  if (s->hashed) {
+    a.hash_list = s->d_hbucket;
+    a.hash_cell = s->d_hcell;
+    a.hash_key = s->d_hkey;
+    a.hash_size = s->list_size;
+  }
   for (int k = 0; k < 3; ++k)
     a.clip_m[k] = (T)(16.0 * (double)std::numeric_limits<T>::epsilon() *
                       (std::fabs(s->min_pad[k]) + std::fabs(s->max_pad[k]) + s->cell_size[k]));
@@ -321,7 +335,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
   const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   const int64_t n_launch = sorted ? n_sorted : n_q;
   // the pair cache: walked while valid, built by a density / adjoint-forward sweep
-  const bool cache_on = !kMixed && lists == nullptr && sorted && s->pc_cap > 0;
+  const bool cache_on = !kMixed && !s->hashed && lists == nullptr && sorted && s->pc_cap > 0;
   auto use_cache = [&]() {
     a.pc_b0 = s->d_pc_b0;
     a.pc_mask = reinterpret_cast<const ulonglong2*>(s->d_pc_mask);
