@@ -65,6 +65,10 @@ def parse():
     ap.add_argument("--pair-cache", type=int, default=1,
                     help="1: the grid search's pair cache (the density sweep records each "
                          "query's neighbours for the force sweep); 0: off")
+    ap.add_argument("--cell-list", default="full_grid", choices=["full_grid", "spatial_hashing"],
+                    help="wcsph workload: FullGridCellList [-1, n_side+1]^3 (incremental "
+                         "update, pair cache) or SpatialHashingCellList(list_size = 2n) "
+                         "(ParallelUpdate rebuild, no pair cache)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",
@@ -184,11 +188,19 @@ def run_gpu(args, rank, world, local):
     x1 = (x0.astype(np.float64) + dx).astype(dt)
     n = len(x0)
     r = dt(3.0)
-    cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt), max_corner=np.full(3, n_side + 1.0, dt),
-                            search_radius=r, max_points_per_cell=0)
-    nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
-                                   update_strategy=P.ParallelIncrementalUpdate(),
-                                   pair_cache=args.pair_cache)
+    hashing = args.cell_list == "spatial_hashing"
+    if hashing:
+        args.pair_cache = 0  # the pair cache follows the full grid's stencil rows
+        cl = P.SpatialHashingCellList(3, list_size=2 * n, max_points_per_cell=0)
+        nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                       update_strategy=P.ParallelUpdate())
+    else:
+        cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt),
+                                max_corner=np.full(3, n_side + 1.0, dt),
+                                search_radius=r, max_points_per_cell=0)
+        nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                       update_strategy=P.ParallelIncrementalUpdate(),
+                                       pair_cache=args.pair_cache)
     x0d = torch.as_tensor(x0, device="cuda").T
     vd = torch.as_tensor(v, device="cuda").reshape(-1)
     rho = torch.zeros(n, dtype=tdt, device="cuda")
@@ -360,16 +372,21 @@ def run_gpu(args, rank, world, local):
     t_force = statistics.median(frc) / 1e3
     alg = FORCE_BYTES_PER_POINT[args.dtype] * n
     achieved = alg / t_force / 1e9
+    tkey = (args.dtype, args.pair_cache > 0)
     roofline = {"bound": "hbm",
-                "kernel": ("k_masks_sorted<FForce> (force sweep over the pair cache)"
+                "kernel": ("k_trav_hash_sorted<FForce> (force sweep over the hash lists)"
+                           if hashing else
+                           "k_masks_sorted<FForce> (force sweep over the pair cache)"
                            if args.pair_cache > 0 else "k_trav_sorted<FForce> (force sweep)"),
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak,
-                "traffic": (FORCE_TRAFFIC_BYTES_PER_POINT[(args.dtype, args.pair_cache > 0)] * n
-                            if (args.dtype, args.pair_cache > 0) in FORCE_TRAFFIC_BYTES_PER_POINT
+                "traffic": (FORCE_TRAFFIC_BYTES_PER_POINT[tkey] * n
+                            if tkey in FORCE_TRAFFIC_BYTES_PER_POINT and not hashing
                             else None),
                 "algorithmic_bytes_per_launch": alg,
-                "note": ("force over the pair cache's hit masks and density + masks: "
+                "note": ("the hashed traversal: 27 cell runs per query, each found "
+                         "through its hash list" if hashing else
+                         "force over the pair cache's hit masks and density + masks: "
                          "issue-bound (ncu issue slots 76 % / 87 %, DRAM 5 %)"
                          if args.pair_cache > 0 else
                          "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
@@ -385,8 +402,13 @@ def run_gpu(args, rank, world, local):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == np.float32 else "f64",
         "data": "synthetic (seeded perturbed lattice, numpy PCG64)",
         "config": {"workload": f"WCSPH step, {n_side}^3 = {n:,} points 3D lattice, spacing 1, "
-                               "U[-0.25,0.25] noise, r=3, FullGridCellList [-1,201]^3, "
-                               "random walk N(0,0.05^2) per step, ParallelIncrementalUpdate",
+                               "U[-0.25,0.25] noise, r=3, " +
+                               (f"SpatialHashingCellList(list_size={2 * n}), ParallelUpdate, "
+                                if hashing else
+                                f"FullGridCellList [-1,{n_side + 1}]^3, "
+                                "ParallelIncrementalUpdate, ") +
+                               "random walk N(0,0.05^2) per step",
+                   "cell_list": args.cell_list,
                    "n_points": n, "search_radius": 3.0,
                    "pairs_per_sweep": pairs_per_sweep,
                    "pair_cache": args.pair_cache,
