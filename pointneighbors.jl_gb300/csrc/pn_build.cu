@@ -477,7 +477,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
 // traversing (nhs_grid.jl:479-513); both visit exactly the points of the stencil's cells.
 template <typename T, int D, bool PER>
 __global__ void __launch_bounds__(BIN_THREADS)
-k_hash_bin(const GridDev<T> g, int64_t list_size, const T* __restrict__ y, int64_t n_y,
+k_hash_bin(const GridDev<T> g, const HashMod hm, const T* __restrict__ y, int64_t n_y,
            const int32_t* __restrict__ idx, int32_t m, int32_t* __restrict__ bucket_of,
            int4* __restrict__ key_of, int32_t* __restrict__ slot_of,
            int32_t* __restrict__ counts, int32_t* __restrict__ err) {
@@ -495,7 +495,7 @@ k_hash_bin(const GridDev<T> g, int64_t list_size, const T* __restrict__ y, int64
         bool ok = true;
 #pragma unroll
         for (int k = 0; k < D; ++k) ok &= hash_cell_1d(g, PER, k, y[i * D + k], c[k]);
-        if (ok) bucket = spatial_hash<D>(c, list_size);
+        if (ok) bucket = spatial_hash<D>(c, hm);
         else set_error(err, PN_ERR_OUT_OF_DOMAIN);
       }
     }
@@ -646,7 +646,7 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
     const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
     const bool per = s->periodic != 0;
 #define PN_HASH_BIN(DD, PP)                                                                 \
-  k_hash_bin<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(g, s->list_size, y, n_y, idx,       \
+  k_hash_bin<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(g, hash_mod(s->list_size), y, n_y, idx, \
                                                         (int32_t)m, s->d_cell_of, s->d_hkey_t, \
                                                         s->d_slot_of, s->d_counts, s->d_err)
     switch (s->ndims * 2 + (per ? 1 : 0)) {

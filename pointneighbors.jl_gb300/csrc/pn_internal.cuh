@@ -135,15 +135,31 @@ __device__ __forceinline__ bool hash_cell_1d(const GridDev<T>& g, bool periodic,
   return !(xk != xk);
 }
 
+// The number of hash lists with its reciprocal magic = floor((2^64 - 1) / size), so that
+// x mod size is one high multiply, one multiply and at most two corrections (the estimate
+// floor(x magic / 2^64) is at most 2 below floor(x / size) for x < 2^64, size < 2^31).
+struct HashMod {
+  int64_t size;
+  uint64_t magic;
+};
+inline HashMod hash_mod(int64_t size) {
+  return HashMod{size, size > 0 ? ~0ull / (uint64_t)size : 0ull};
+}
+
 // spatial_hash (spatial_hashing.jl:142-156, Ihmsen et al.): Int64 products and xor that
-// wrap around like Julia's, then mod(h, list_size); 0-based.
+// wrap around like Julia's, then Julia's mod(h, list_size) (non-negative); 0-based.
 template <int D>
-__device__ __forceinline__ int32_t spatial_hash(const int32_t* c, int64_t list_size) {
+__device__ __forceinline__ int32_t spatial_hash(const int32_t* c, const HashMod& hm) {
   uint64_t h = (uint64_t)(int64_t)c[0] * 73856093ull;
   if (D >= 2) h ^= (uint64_t)(int64_t)c[1] * 19349663ull;
   if (D >= 3) h ^= (uint64_t)(int64_t)c[2] * 83492791ull;
-  int64_t m = (int64_t)h % list_size;
-  return (int32_t)(m < 0 ? m + list_size : m);
+  const bool neg = (int64_t)h < 0;
+  const uint64_t ax = neg ? 0ull - h : h;  // |h|, 2^63 for typemin
+  const uint64_t sz = (uint64_t)hm.size;
+  uint64_t r = ax - __umul64hi(ax, hm.magic) * sz;
+  if (r >= sz) r -= sz;
+  if (r >= sz) r -= sz;
+  return (int32_t)(neg && r != 0 ? sz - r : r);
 }
 
 // A point outside the periodic box [min, max) (the periodic traversal then checks every

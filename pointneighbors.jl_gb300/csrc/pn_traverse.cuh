@@ -73,7 +73,7 @@ struct TravArgs {
   const int32_t* hash_list;
   const int4* hash_cell;
   const int4* hash_key;
-  int64_t hash_size;
+  HashMod hash_mod;
 };
 
 template <typename T, int D>
@@ -948,14 +948,14 @@ __device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F:
           F::pair(acc, p, q, js, pd, d2, (T)0);
         }
       }
-      return;
-    }
-    for (int32_t js = beg; js < end; ++js) {
-      T yj[D], pd[D];
-      load_cand<T, D>(a.pos, js, yj);
-      const T d2 = WRAP ? pair_geom<T, D, true>(a.g, q.x, yj, pd)
-                        : pair_geom<T, D, false>(a.g, q.x, yj, pd);
-      if (d2 <= a.g.r2) F::pair(acc, p, q, js, pd, d2, (T)0);
+    } else {
+      for (int32_t js = beg; js < end; ++js) {
+        T yj[D], pd[D];
+        load_cand<T, D>(a.pos, js, yj);
+        const T d2 = WRAP ? pair_geom<T, D, true>(a.g, q.x, yj, pd)
+                          : pair_geom<T, D, false>(a.g, q.x, yj, pd);
+        if (d2 <= a.g.r2) F::pair(acc, p, q, js, pd, d2, (T)0);
+      }
     }
     return;
   }
@@ -1099,13 +1099,8 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
 // [0, start[n_total]) are the main structure, then the overflow slots up to
 // ovf_start[n_total]; vacated slots (perm < 0) are skipped.
 template <typename T, int D, bool PER, class F>
-__global__ void __launch_bounds__(TRAV_THREADS, 8)
-k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
-  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
-  // the pair cache's fallback launch: nothing to do unless some query was marked
-  if (a.nb_len != nullptr && a.pc_any_fallback != nullptr && *a.pc_any_fallback == 0) return;
+__device__ __forceinline__ void sorted_query(const TravArgs<T>& a, const typename F::Params& p,
+                                             int64_t k, int32_t n_slots) {
   Query<T, D> q;
   bool valid = k < n_slots;
   q.i = valid ? a.perm[k] : -1;
@@ -1126,6 +1121,28 @@ k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
     for (int d = 0; d < D; ++d) q.x[d] = (T)0;
   }
   traverse_query<T, D, PER, F>(a, p, q, c, valid);
+}
+
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
+  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
+  sorted_query<T, D, PER, F>(a, p, k, n_slots);
+}
+
+// The stencil traversal of the queries that a pair cache or precomputed lists could not
+// hold (nb_len < 0), as a grid-stride loop over the slots on one wave of blocks: with the
+// pair cache's flag clear (no such query) every block returns at once.
+template <typename T, int D, bool PER, class F>
+__global__ void __launch_bounds__(TRAV_THREADS, 8)
+k_trav_fallback(const TravArgs<T> a, const typename F::Params p) {
+  if (a.pc_any_fallback != nullptr && *a.pc_any_fallback == 0) return;
+  const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < n_slots;
+       base += (int64_t)gridDim.x * blockDim.x)
+    sorted_query<T, D, PER, F>(a, p, base + threadIdx.x, n_slots);
 }
 
 // List mode: queries are x[:, qlist[q]] (or q) in the given order.  A query whose
@@ -1171,9 +1188,9 @@ k_trav_list(const TravArgs<T> a, const typename F::Params p) {
 // cells collide in the list); an empty run when the cell has no points.
 template <int D>
 __device__ __forceinline__ void hash_run(const int32_t* __restrict__ list,
-                                         const int4* __restrict__ cell, int64_t size,
+                                         const int4* __restrict__ cell, const HashMod& hm,
                                          const int32_t* cc, int32_t& b, int32_t& e) {
-  const int32_t h = spatial_hash<D>(cc, size);
+  const int32_t h = spatial_hash<D>(cc, hm);
   const int32_t e1 = __ldg(&list[h + 1]);
   b = e = 0;
   for (int32_t k = __ldg(&list[h]); k < e1; ++k) {
@@ -1189,6 +1206,9 @@ __device__ __forceinline__ void hash_run(const int32_t* __restrict__ list,
 // One query over a SpatialHashingCellList: the 3^d cells in the reference's
 // CartesianIndices order, each cell's run in slot order.  Cells need not line up with a
 // periodic box's faces here, so with one every candidate is checked for its image.
+// (Skipping the neighbouring cells that lie farther than r from the query saves nothing:
+// the lanes of a warp are queries of one cell at different positions, and some lane
+// nearly always needs each of the 3^d cells.)
 template <typename T, int D, bool PER, class F>
 __device__ __forceinline__ void traverse_query_hash(const TravArgs<T>& a,
                                                     const typename F::Params& p,
@@ -1211,7 +1231,7 @@ __device__ __forceinline__ void traverse_query_hash(const TravArgs<T>& a,
           for (int k = 0; k < D; ++k) cc[k] = pwrap(cc[k], a.g.ncell[k]);
         }
         int32_t b, e;
-        hash_run<D>(a.hash_list, a.hash_cell, a.hash_size, cc, b, e);
+        hash_run<D>(a.hash_list, a.hash_cell, a.hash_mod, cc, b, e);
         scan_any<T, D, PER, F>(a, p, acc, q, PER, b, e);
       }
     }

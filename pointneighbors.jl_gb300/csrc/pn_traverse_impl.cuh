@@ -177,13 +177,23 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
   }
 #undef PN_TRAV_CASE
   if ((a.nb != nullptr || a.pc_mask != nullptr) && a.nb_fallback && sorted) {
-    // queries the pair cache could not hold: the stencil traversal, for those only
+    // queries the pair cache or the lists could not hold: the stencil traversal, for
+    // those only (the full grid's; neither is offered over hash lists)
     TravArgs<T> g = a;
     g.nb = nullptr;
     g.pc_mask = nullptr;
     g.pc_b0 = nullptr;
     g.nb_fallback = 0;
-    return launch_trav<T, F>(s, g, p, sorted, n_launch, st);
+    const int fb = std::min(blocks, 152 * 8);
+    switch (key) {
+      case 2: k_trav_fallback<T, 1, false, F<T, 1>><<<fb, TRAV_THREADS, 0, st>>>(g, p); break;
+      case 3: k_trav_fallback<T, 1, true, F<T, 1>><<<fb, TRAV_THREADS, 0, st>>>(g, p); break;
+      case 4: k_trav_fallback<T, 2, false, F<T, 2>><<<fb, TRAV_THREADS, 0, st>>>(g, p); break;
+      case 5: k_trav_fallback<T, 2, true, F<T, 2>><<<fb, TRAV_THREADS, 0, st>>>(g, p); break;
+      case 6: k_trav_fallback<T, 3, false, F<T, 3>><<<fb, TRAV_THREADS, 0, st>>>(g, p); break;
+      default: k_trav_fallback<T, 3, true, F<T, 3>><<<fb, TRAV_THREADS, 0, st>>>(g, p); break;
+    }
+    count_launch();
   }
   return cuda_status(cudaGetLastError());
 }
@@ -237,7 +247,7 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
     a.hash_list = s->d_hbucket;
     a.hash_cell = s->d_hcell;
     a.hash_key = s->d_hkey;
-    a.hash_size = s->list_size;
+    a.hash_mod = hash_mod(s->list_size);
   }
   for (int k = 0; k < 3; ++k)
     a.clip_m[k] = (T)(16.0 * (double)std::numeric_limits<T>::epsilon() *
@@ -304,48 +314,80 @@ static void use_state(const pn_search* s, TravArgs<T>& a, MixedGeom& m, const V*
   else m.state = state;
 }
 
+// One foreach_point_neighbor call after its checks: the traversal arguments and the launch
+// shape that every pair function uses.
+template <typename T>
+struct TravCall {
+  TravArgs<T> a;
+  MixedGeom m;
+  bool sorted;    // the queries are the cell-sorted slots (x is y, every point binned)
+  bool cache_on;  // the pair cache is walked or built by this call
+  int64_t n_q, n_sorted, n_launch;
+};
+
+// Walk the pair cache (valid since the last density / adjoint-forward sweep).
+template <typename T>
+static void use_pair_cache(const pn_search* s, TravArgs<T>& a) {
+  a.pc_b0 = s->d_pc_b0;
+  a.pc_mask = reinterpret_cast<const ulonglong2*>(s->d_pc_mask);
+  a.pc_stride = s->pc_rows;
+  a.nb_len = s->d_pc_b0;  // row 0: negative marks the stencil fallback
+  a.nb_fallback = 1;
+  a.pc_any_fallback = s->d_err + 4;
+}
+
 template <typename T, typename V>
-static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y,
-                     int64_t n_y, const int32_t* points, int64_t n_points, const void* params,
-                     cudaStream_t st, const ListsRef* lists) {
+static int prepare_call(pn_search* s, const T* x, int64_t n_x, const T* y, int64_t n_y,
+                        const int32_t* points, int64_t n_points, const void* params,
+                        const ListsRef* lists, TravCall<T>& c) {
   constexpr bool kMixed = !std::is_same<T, V>::value;
   if (!s->initialized || s->is_template) return PN_ERR_NOT_INITIALIZED;
   if (n_y != s->n_y || n_x < 0 || (points == nullptr && n_points != 0 && n_points != n_x))
     return PN_ERR_INVALID_ARG;
   if (params == nullptr) return PN_ERR_INVALID_ARG;
-  const bool sorted = (const void*)x == (const void*)y && n_x == n_y && points == nullptr &&
-                      s->full_binned;
-  const int64_t n_q = points ? n_points : n_x;
-  TravArgs<T> a = trav_args<T>(s, x, n_x, points, n_q);
-  MixedGeom m{};
-  if constexpr (kMixed) m = mixed_geom(s, &a);
+  c.sorted = (const void*)x == (const void*)y && n_x == n_y && points == nullptr &&
+             s->full_binned;
+  c.n_q = points ? n_points : n_x;
+  c.a = trav_args<T>(s, x, n_x, points, c.n_q);
+  c.m = MixedGeom{};
+  if constexpr (kMixed) c.m = mixed_geom(s, &c.a);
   if (lists != nullptr) {
     // rows are slots (lists built with x is y) or the points of x
     if (lists->by_slot) {
       if ((const void*)x != (const void*)y || n_x != n_y) return PN_ERR_INVALID_ARG;
-      if (!sorted) a.nb_row_of = lists->row_of;  // a subset of the points
-    } else if (sorted || n_x != lists->n_rows) {
+      if (!c.sorted) c.a.nb_row_of = lists->row_of;  // a subset of the points
+    } else if (c.sorted || n_x != lists->n_rows) {
       return PN_ERR_INVALID_ARG;
     }
-    a.nb = lists->nb;
-    a.nb_grp = lists->grp;
-    a.nb_len = lists->len;
+    c.a.nb = lists->nb;
+    c.a.nb_grp = lists->grp;
+    c.a.nb_len = lists->len;
   }
   // Sorted mode launches one thread per possible slot; the kernel reads the live count.
-  const int64_t n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
-  const int64_t n_launch = sorted ? n_sorted : n_q;
-  // the pair cache: walked while valid, built by a density / adjoint-forward sweep
-  const bool cache_on = !kMixed && !s->hashed && lists == nullptr && sorted && s->pc_cap > 0;
-  auto use_cache = [&]() {
-    a.pc_b0 = s->d_pc_b0;
-    a.pc_mask = reinterpret_cast<const ulonglong2*>(s->d_pc_mask);
-    a.pc_stride = s->pc_rows;
-    a.nb_len = s->d_pc_b0;  // row 0: negative marks the stencil fallback
-    a.nb_fallback = 1;
-    a.pc_any_fallback = s->d_err + 4;
-  };
-  if (cache_on && s->pc_valid) use_cache();
+  c.n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
+  c.n_launch = c.sorted ? c.n_sorted : c.n_q;
+  c.cache_on = !kMixed && !s->hashed && lists == nullptr && c.sorted && s->pc_cap > 0;
+  if (c.cache_on && s->pc_valid) use_pair_cache(s, c.a);
+  return PN_OK;
+}
 
+// The WCSPH and adjoint pair functions; defined in pn_traverse_sph.cuh and compiled in
+// translation units of their own (the kernels of one element type in two halves).
+template <typename T, typename V>
+int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
+                TravCall<T>& c, cudaStream_t st);
+
+template <typename T, typename V>
+static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, const T* y,
+                     int64_t n_y, const int32_t* points, int64_t n_points, const void* params,
+                     cudaStream_t st, const ListsRef* lists) {
+  TravCall<T> c;
+  const int rc0 = prepare_call<T, V>(s, x, n_x, y, n_y, points, n_points, params, lists, c);
+  if (rc0 != PN_OK) return rc0;
+  TravArgs<T>& a = c.a;
+  const MixedGeom& m = c.m;
+  const bool sorted = c.sorted;
+  const int64_t n_q = c.n_q, n_launch = c.n_launch;
   switch (functor) {
     case PN_F_COUNT: {
       const auto* u = static_cast<const pn_count_params*>(params);
@@ -395,121 +437,8 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
                            (V)(1.0 / u->cutoff), static_cast<V*>(u->energy)};
       return launch_pair<T, V, FPotential>(s, a, p, m, sorted, n_launch, st);
     }
-    case PN_F_WCSPH_DENSITY:
-    case PN_F_WCSPH_STEP: {
-      const auto* u = static_cast<const pn_wcsph_params*>(params);
-      const bool step = functor == PN_F_WCSPH_STEP;
-      if (step && !sorted) return PN_ERR_INVALID_ARG;
-      DensityParams<V> p{sph_const<V>(s, u), static_cast<V*>(u->density),
-                         static_cast<V*>(u->pressure), static_cast<const V*>(u->velocity),
-                         nullptr, nullptr};
-      if (sorted && u->velocity != nullptr) {
-        p.pa = static_cast<V*>(s->d_pa);
-        p.pb = static_cast<V*>(s->d_pb);
-      }
-      int rc = PN_OK;
-      bool done = false;
-      if constexpr (!kMixed) {
-        if (cache_on && !s->pc_valid) {
-          MaskPairParams<DensityParams<T>> pp{p, {}};
-          rc = pc_prepare(s, n_sorted, &pp.m, st);
-          if (rc == PN_OK) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
-          if (rc == PN_OK) {
-            s->pc_valid = true;
-            use_cache();
-          }
-          done = true;
-        }
-      }
-      if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st);
-      if (rc != PN_OK || !step) return rc;
-      ForceParams<V> pf{p.c, static_cast<const V*>(s->d_pa), static_cast<const V*>(s->d_pb),
-                        static_cast<V*>(u->accel)};
-      use_state(s, a, m, pf.pa);
-      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st);
-    }
-    case PN_F_WCSPH_FORCE: {
-      const auto* u = static_cast<const pn_wcsph_params*>(params);
-      if (!sorted) return PN_ERR_INVALID_ARG;
-      const int b = div_up(n_sorted, 256);
-      const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
-      const T* pos = static_cast<const T*>(s->d_pos);
-      V* pa = static_cast<V*>(s->d_pa);
-      V* pb = static_cast<V*>(s->d_pb);
-      const V* dn = static_cast<const V*>(u->density);
-      const V* pr = static_cast<const V*>(u->pressure);
-      const V* ve = static_cast<const V*>(u->velocity);
-      if (b > 0 && !u->reuse_state) {
-        const int32_t ns = (int32_t)n_sorted;
-        switch (s->ndims) {
-          case 1: k_gather_state<T, V, 1><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
-          case 2: k_gather_state<T, V, 2><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
-          default: k_gather_state<T, V, 3><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
-        }
-      }
-      ForceParams<V> pf{sph_const<V>(s, u), pa, pb, static_cast<V*>(u->accel)};
-      use_state(s, a, m, pf.pa);
-      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st);
-    }
-    case PN_F_ADJOINT_FORWARD:
-    case PN_F_ADJOINT_BACKWARD: {
-      const auto* u = static_cast<const pn_adjoint_params*>(params);
-      if (!sorted || !(u->cutoff > 0.0) || !(u->h > 0.0)) return PN_ERR_INVALID_ARG;
-      pn_wcsph_params w{};
-      w.mass = u->mass;
-      w.h = u->h;
-      w.c0 = w.rho0 = w.gamma_exp = 1.0;
-      AdjointParams<V> p{};
-      p.c = sph_const<V>(s, &w);
-      p.cutoff = (V)u->cutoff;
-      p.inv_cutoff = (V)(1.0 / u->cutoff);
-      p.lambda = (V)u->lambda_pot;
-      p.pa = static_cast<V*>(s->d_pa);
-      if (functor == PN_F_ADJOINT_FORWARD) {
-        if (!u->density || !u->terms || !u->loss) return PN_ERR_INVALID_ARG;
-        int rc = ensure_sum_part(s);
-        if (rc != PN_OK) return rc;
-        p.density = static_cast<V*>(u->density);
-        p.terms = static_cast<V*>(u->terms);
-        bool done = false;
-        if constexpr (!kMixed) {
-          if (cache_on && !s->pc_valid) {
-            MaskPairParams<AdjointParams<T>> pp{p, {}};
-            rc = pc_prepare(s, n_sorted, &pp.m, st);
-            if (rc == PN_OK)
-              rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
-            if (rc == PN_OK) s->pc_valid = true;
-            done = true;
-          }
-        }
-        if (!done) rc = launch_pair<T, V, FAdjointForward>(s, a, p, m, sorted, n_launch, st);
-        if (rc != PN_OK) return rc;
-        k_sum_partials<V><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
-        k_sum_final<<<1, 256, 0, st>>>(s->d_sum_part, SUM_BLOCKS, u->loss); count_launch();
-        return cuda_status(cudaGetLastError());
-      }
-      if (!u->grad || (!u->reuse_state && !u->density)) return PN_ERR_INVALID_ARG;
-      if (!u->reuse_state) {
-        const int b = div_up(n_sorted, 256);
-        const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
-        const T* pos = static_cast<const T*>(s->d_pos);
-        const V* dn = static_cast<const V*>(u->density);
-        const int32_t ns = (int32_t)n_sorted;
-        if (b > 0) {
-          switch (s->ndims) {
-            case 1: k_gather_adjoint<T, V, 1><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, p.pa); count_launch(); break;
-            case 2: k_gather_adjoint<T, V, 2><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, p.pa); count_launch(); break;
-            default: k_gather_adjoint<T, V, 3><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, p.pa); count_launch(); break;
-          }
-        }
-      }
-      p.grad = static_cast<V*>(u->grad);
-      p.scale = u->grad_scale;
-      use_state(s, a, m, static_cast<const V*>(p.pa));
-      return launch_pair<T, V, FAdjointBackward>(s, a, p, m, sorted, n_launch, st);
-    }
     default:
-      return PN_ERR_UNSUPPORTED_FUNCTOR;
+      return foreach_sph<T, V>(s, functor, n_x, params, c, st);
   }
 }
 
