@@ -190,10 +190,11 @@ def run_gpu(args, rank, world, local):
     r = dt(3.0)
     hashing = args.cell_list == "spatial_hashing"
     if hashing:
-        args.pair_cache = 0  # the pair cache follows the full grid's stencil rows
+        # the occupied cells fit 2n lists: the dense layout, which takes the pair cache
         cl = P.SpatialHashingCellList(3, list_size=2 * n, max_points_per_cell=0)
         nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
-                                       update_strategy=P.ParallelUpdate())
+                                       update_strategy=P.ParallelUpdate(),
+                                       pair_cache=args.pair_cache)
     else:
         cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt),
                                 max_corner=np.full(3, n_side + 1.0, dt),
@@ -374,19 +375,17 @@ def run_gpu(args, rank, world, local):
     achieved = alg / t_force / 1e9
     tkey = (args.dtype, args.pair_cache > 0)
     roofline = {"bound": "hbm",
-                "kernel": ("k_trav_hash_sorted<FForce> (force sweep over the hash lists)"
-                           if hashing else
-                           "k_masks_sorted<FForce> (force sweep over the pair cache)"
+                "kernel": ("k_masks_sorted<FForce> (force sweep over the pair cache)"
                            if args.pair_cache > 0 else "k_trav_sorted<FForce> (force sweep)"),
                 "achieved": achieved, "peak": peak, "peak_kind": peak_kind, "unit": "GB/s",
                 "frac": achieved / peak,
                 "traffic": (FORCE_TRAFFIC_BYTES_PER_POINT[tkey] * n
                             if tkey in FORCE_TRAFFIC_BYTES_PER_POINT and not hashing
                             else None),
+                "layout": (("dense grid over the occupied cells" if nhs.grid_info()["grid_size"][0] > 1
+                            else "hash lists") if hashing else "full grid"),
                 "algorithmic_bytes_per_launch": alg,
-                "note": ("the hashed traversal: 27 cell runs per query, each found "
-                         "through its hash list" if hashing else
-                         "force over the pair cache's hit masks and density + masks: "
+                "note": ("force over the pair cache's hit masks and density + masks: "
                          "issue-bound (ncu issue slots 76 % / 87 %, DRAM 5 %)"
                          if args.pair_cache > 0 else
                          "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "

@@ -245,7 +245,10 @@ static int create(const pn_config* cfg, int64_t list_size, pn_search** out) {
          cudaMalloc(&s->d_ovf_start, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
          cudaMalloc(&s->d_ovf_n, sizeof(int32_t) * 4) == cudaSuccess &&
          cudaMalloc(&s->d_scan_state, sizeof(unsigned long long) * (s->scan_tiles + 1)) == cudaSuccess;
-    if (ok && s->hashed) ok = cudaMalloc(&s->d_hbucket, sizeof(int32_t) * (nt + 1)) == cudaSuccess;
+    if (ok && s->hashed)
+      ok = cudaMalloc(&s->d_hbucket, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
+           cudaMalloc(&s->d_hbbox, sizeof(int32_t) * 6) == cudaSuccess &&
+           cudaMallocHost(&s->h_hbbox, sizeof(int32_t) * 6) == cudaSuccess;
     if (ok && cfg->n_points > 0) ok = ensure_capacity(s, cfg->n_points) == PN_OK;
   }
   if (!ok) {
@@ -311,10 +314,12 @@ int pn_destroy(pn_search* s) {
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
                   s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_b0,
                   s->d_pc_mask,    s->d_hkey_t,     s->d_hkey_tmp,  s->d_hkey,
-                  s->d_hcellidx,   s->d_hcell,      s->d_hbucket,   s->d_hscan_state};
+                  s->d_hcellidx,   s->d_hcell,      s->d_hbucket,   s->d_hscan_state,
+                  s->d_hbbox};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   if (s->h_ovf_n) cudaFreeHost(s->h_ovf_n);
+  if (s->h_hbbox) cudaFreeHost(s->h_hbbox);
   if (s->ev_ovf) cudaEventDestroy(s->ev_ovf);
   delete s;
   return PN_OK;
@@ -483,6 +488,7 @@ int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t 
   if (!s || !counts) return PN_ERR_INVALID_ARG;
   if (!s->initialized) return PN_ERR_NOT_INITIALIZED;
   cudaStream_t st = (cudaStream_t)stream;
+  if (s->hashed) return record(s, export_hash_lists(s, counts, points, st), st);
   return record(s, export_cells(s, counts, points, st), st);
 }
 

@@ -480,7 +480,7 @@ __global__ void __launch_bounds__(BIN_THREADS)
 k_hash_bin(const GridDev<T> g, const HashMod hm, const T* __restrict__ y, int64_t n_y,
            const int32_t* __restrict__ idx, int32_t m, int32_t* __restrict__ bucket_of,
            int4* __restrict__ key_of, int32_t* __restrict__ slot_of,
-           int32_t* __restrict__ counts, int32_t* __restrict__ err) {
+           int32_t* __restrict__ counts, int32_t* __restrict__ bbox, int32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
@@ -507,6 +507,16 @@ k_hash_bin(const GridDev<T> g, const HashMod hm, const T* __restrict__ y, int64_
       if (lane == leader) b = atomicAdd(&counts[bucket], __popc(peers));
       b = __shfl_sync(peers, b, leader);
       slot_of[t] = b + __popc(peers & lanemask_lt());
+      // bounding box of the occupied cells (one atomic per warp and bound)
+#pragma unroll
+      for (int k = 0; k < D; ++k) {
+        const int32_t lo = __reduce_min_sync(valid, c[k]);
+        const int32_t hi = __reduce_max_sync(valid, c[k]);
+        if (lane == __ffs(valid) - 1) {
+          atomicMin(&bbox[k], lo);
+          atomicMax(&bbox[3 + k], hi);
+        }
+      }
     }
     if (t < m) {
       bucket_of[t] = bucket;
@@ -606,6 +616,42 @@ k_hash_buckets(const int32_t* __restrict__ start, const int32_t* __restrict__ ce
   if (b <= n_lists) hbucket[b] = cellidx[start[b]];
 }
 
+__global__ void k_hash_bbox_init(int32_t* bbox) {
+  if (threadIdx.x < 3) bbox[threadIdx.x] = INT32_MAX;
+  else if (threadIdx.x < 6) bbox[threadIdx.x] = INT32_MIN;
+}
+
+// The dense layout: grid index = cell + off (1-based, column-major over n), binned like the
+// full grid's k_bin from the cells found by k_hash_bin.
+template <int D>
+__global__ void __launch_bounds__(BIN_THREADS)
+k_hash_dense_bin(const int32_t* bucket_of, const int4* __restrict__ key_of,
+                 int32_t m, int3 off, int3 n, int32_t* cell_of,  // may be bucket_of itself
+                 int32_t* __restrict__ slot_of, int32_t* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = base + threadIdx.x;
+    int32_t cell = -1;
+    if (t < m && bucket_of[t] >= 0) {
+      const int4 c = key_of[t];
+      cell = c.x + off.x - 1;
+      if (D >= 2) cell += (c.y + off.y - 1) * n.x;
+      if (D == 3) cell += (c.z + off.z - 1) * n.x * n.y;
+    }
+    const unsigned valid = __ballot_sync(0xffffffffu, cell >= 0);
+    if (cell >= 0) {
+      const unsigned peers = __match_any_sync(valid, cell);
+      const int leader = __ffs(peers) - 1;
+      int32_t b = 0;
+      if (lane == leader) b = atomicAdd(&counts[cell], __popc(peers));
+      b = __shfl_sync(peers, b, leader);
+      slot_of[t] = b + __popc(peers & lanemask_lt());
+    }
+    if (t < m) cell_of[t] = cell;
+  }
+}
+
 static int ensure_hash_capacity(pn_search* s, int64_t n) {
   if (n <= s->hash_cap && s->d_hkey) return PN_OK;
   void* ptrs[] = {s->d_hkey_t, s->d_hkey_tmp, s->d_hkey, s->d_hcellidx, s->d_hcell,
@@ -639,16 +685,20 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
   int rc = ensure_capacity(s, std::max(m, n_y));
   if (rc == PN_OK) rc = ensure_hash_capacity(s, s->cap);
   if (rc != PN_OK) return rc;
-  const int32_t nl = s->n_total;
+  const int32_t nl = (int32_t)s->list_size;
+  // 1. cells, hash lists (with the per-list max_points_per_cell check) and the bounding box
+  s->n_total = nl;
+  s->hash_dense = false;
   cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * nl, st);
+  k_hash_bbox_init<<<1, 32, 0, st>>>(s->d_hbbox); count_launch();
   if (m > 0) {
     const GridDev<T> g = make_grid<T>(s);
     const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
     const bool per = s->periodic != 0;
-#define PN_HASH_BIN(DD, PP)                                                                 \
-  k_hash_bin<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(g, hash_mod(s->list_size), y, n_y, idx, \
-                                                        (int32_t)m, s->d_cell_of, s->d_hkey_t, \
-                                                        s->d_slot_of, s->d_counts, s->d_err)
+#define PN_HASH_BIN(DD, PP)                                                                  \
+  k_hash_bin<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(                                     \
+      g, hash_mod(s->list_size), y, n_y, idx, (int32_t)m, s->d_cell_of, s->d_hkey_t,         \
+      s->d_slot_of, s->d_counts, s->d_hbbox, s->d_err)
     switch (s->ndims * 2 + (per ? 1 : 0)) {
       case 2: PN_HASH_BIN(1, false); break;
       case 3: PN_HASH_BIN(1, true); break;
@@ -661,7 +711,57 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
     count_launch();
   }
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
-  if (m > 0) {
+  // 2. the layout: a dense grid over the occupied cells' box when it has at most list_size
+  // cells (read back: one synchronisation, like the reference's update!), else the lists
+  cudaMemcpyAsync(s->h_hbbox, s->d_hbbox, sizeof(int32_t) * 6, cudaMemcpyDeviceToHost, st);
+  if (cudaStreamSynchronize(st) != cudaSuccess) return PN_ERR_CUDA;
+  const int32_t* bb = s->h_hbbox;
+  int64_t dims[3] = {1, 1, 1}, cells = 1;
+  bool dense = m > 0;
+  for (int k = 0; k < s->ndims && dense; ++k) {
+    if (bb[k] > bb[3 + k]) {
+      dense = false;  // nothing binned
+      break;
+    }
+    dims[k] = s->periodic ? s->n_cells[k] + 3 : (int64_t)bb[3 + k] - bb[k] + 5;
+    cells *= dims[k];
+    dense = cells <= (int64_t)nl;
+  }
+  for (int k = 0; k < 3; ++k) {
+    s->grid_size[k] = 1;
+    s->hash_off[k] = 0;
+    s->min_pad[k] = s->max_pad[k] = 0.0;
+  }
+  if (dense) {
+    // grid index = cell + off: the lowest cell at 3, two empty cells of padding on each
+    // side (periodic: the cells 2..n_cells+1 themselves, like the full grid's)
+    for (int k = 0; k < s->ndims; ++k) {
+      s->grid_size[k] = dims[k];
+      s->hash_off[k] = s->periodic ? 0 : 3 - bb[k];
+      s->min_pad[k] = s->periodic ? 0.0 : ((double)bb[k] - 2.0) * s->cell_size[k];
+      s->max_pad[k] = s->periodic ? 0.0 : ((double)bb[3 + k] + 3.0) * s->cell_size[k];
+    }
+    s->n_total = (int32_t)cells;
+    s->hash_dense = true;
+    cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * cells, st);
+    const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
+    const int3 off = make_int3(s->hash_off[0], s->hash_off[1], s->hash_off[2]);
+    const int3 n = make_int3((int32_t)dims[0], (int32_t)dims[1], (int32_t)dims[2]);
+    switch (s->ndims) {
+      case 1: k_hash_dense_bin<1><<<blocks, BIN_THREADS, 0, st>>>(s->d_cell_of, s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      case 2: k_hash_dense_bin<2><<<blocks, BIN_THREADS, 0, st>>>(s->d_cell_of, s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      default: k_hash_dense_bin<3><<<blocks, BIN_THREADS, 0, st>>>(s->d_cell_of, s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+    }
+    count_launch();
+    // (the search's scan state has room for the tiles of list_size >= cells counts)
+    scan_counts(s->d_counts, (int32_t)cells, s->d_start, s->d_scan_state,
+                scan_tile_count(cells), s->d_err, st);
+    k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
+                                              s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
+                                              nullptr); count_launch();
+    launch_finalize<T>(s, y, (int32_t)m, st);
+  } else if (m > 0) {
+    // 3. the lists: each list's points ranked by (cell, x, index), one entry per cell
     const int b = div_up(m, 256);
     k_hash_scatter<<<b, 256, 0, st>>>(s->d_cell_of, s->d_slot_of, s->d_hkey_t, idx, (int32_t)m,
                                       s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
@@ -1038,6 +1138,81 @@ static int export_cells_t(pn_search* s, int32_t* counts, int32_t* points, cudaSt
   }
   cudaFreeAsync(out_start, st);
   return rc != PN_OK ? rc : cuda_status(cudaGetLastError());
+}
+
+// The reference's hash lists of a SpatialHashingCellList (either layout): every binned
+// point's list from its stored coordinates, counts per list, then the points of each list
+// ascending.
+template <typename T, int D, bool PER>
+__global__ void __launch_bounds__(256)
+k_export_hash_count(const GridDev<T> g, const HashMod hm, const T* __restrict__ pos,
+                    const int32_t* __restrict__ perm, const int32_t* __restrict__ n_slots,
+                    int32_t* __restrict__ list_of_slot, int32_t* __restrict__ counts) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *n_slots) return;
+  int32_t h = -1;
+  if (perm[k] >= 0) {
+    int32_t c[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < D; ++d) hash_cell_1d(g, PER, d, pos[k * PS<D>::value + d], c[d]);
+    h = spatial_hash<D>(c, hm);
+    atomicAdd(&counts[h], 1);
+  }
+  list_of_slot[k] = h;
+}
+
+__global__ void __launch_bounds__(256)
+k_export_hash_scatter(const int32_t* __restrict__ list_of_slot, const int32_t* __restrict__ perm,
+                      const int32_t* __restrict__ n_slots, unsigned long long* __restrict__ cursor,
+                      int32_t* __restrict__ points) {
+  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= *n_slots) return;
+  const int32_t h = list_of_slot[k];
+  if (h >= 0) points[atomicAdd(&cursor[h], 1ull)] = perm[k];
+}
+
+template <typename T, int D, bool PER>
+static int export_hash_t(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st) {
+  const int64_t nl = s->list_size;
+  const int32_t* n_slots = s->d_start + s->n_total;
+  const int64_t ns = s->n_binned;
+  cudaMemsetAsync(counts, 0, sizeof(int32_t) * nl, st);
+  const int b = div_up(std::max<int64_t>(ns, 1), 256);
+  k_export_hash_count<T, D, PER><<<b, 256, 0, st>>>(make_grid<T>(s), hash_mod(nl),
+                                                    static_cast<const T*>(s->d_pos), s->d_perm,
+                                                    n_slots, s->d_cell_of, counts); count_launch();
+  int64_t* out_start = nullptr;
+  if (cudaMallocAsync(&out_start, sizeof(int64_t) * (nl + 1), st) != cudaSuccess)
+    return PN_ERR_OUT_OF_MEMORY;
+  int rc = scan64(s, counts, nl, out_start, st);
+  if (rc == PN_OK && points) {
+    k_export_hash_scatter<<<b, 256, 0, st>>>(s->d_cell_of, s->d_perm, n_slots,
+                                             reinterpret_cast<unsigned long long*>(out_start),
+                                             points); count_launch();
+    rc = scan64(s, counts, nl, out_start, st);  // the cursors moved: the starts again
+    if (rc == PN_OK) rc = sort_rows(s, out_start, nl, points, ns, st);
+  }
+  cudaFreeAsync(out_start, st);
+  return rc != PN_OK ? rc : cuda_status(cudaGetLastError());
+}
+
+int export_hash_lists(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st) {
+  const bool per = s->periodic != 0;
+  const int key = (s->ndims - 1) * 2 + (per ? 1 : 0) + (s->dtype == PN_FLOAT64 ? 6 : 0);
+  switch (key) {
+    case 0: return export_hash_t<float, 1, false>(s, counts, points, st);
+    case 1: return export_hash_t<float, 1, true>(s, counts, points, st);
+    case 2: return export_hash_t<float, 2, false>(s, counts, points, st);
+    case 3: return export_hash_t<float, 2, true>(s, counts, points, st);
+    case 4: return export_hash_t<float, 3, false>(s, counts, points, st);
+    case 5: return export_hash_t<float, 3, true>(s, counts, points, st);
+    case 6: return export_hash_t<double, 1, false>(s, counts, points, st);
+    case 7: return export_hash_t<double, 1, true>(s, counts, points, st);
+    case 8: return export_hash_t<double, 2, false>(s, counts, points, st);
+    case 9: return export_hash_t<double, 2, true>(s, counts, points, st);
+    case 10: return export_hash_t<double, 3, false>(s, counts, points, st);
+    default: return export_hash_t<double, 3, true>(s, counts, points, st);
+  }
 }
 
 int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st) {

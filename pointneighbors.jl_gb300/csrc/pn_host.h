@@ -97,6 +97,13 @@ struct pn_search {
   int32_t* d_hbucket = nullptr;     // [list_size + 1]
   unsigned long long* d_hscan_state = nullptr;
   int64_t hash_cap = 0;
+  // When the bounding box of the occupied cells (padded by two cells) has at most list_size
+  // cells, the points are stored in a dense grid over that box instead (space order, the
+  // full grid's traversal); hash_off maps a cell coordinate to its 1-based grid index.
+  bool hash_dense = false;
+  int32_t hash_off[3] = {0, 0, 0};
+  int32_t* d_hbbox = nullptr;       // [6] min and max cell coordinate per dimension
+  int32_t* h_hbbox = nullptr;       // pinned copy
 
   // state
   bool initialized = false;
@@ -134,6 +141,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st);
 template <typename T>
 int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t st);
 int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
+int export_hash_lists(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
 int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st);
 // generic pieces of the build, reused by the batched build (pn_batch.cu)
 void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long long* state,

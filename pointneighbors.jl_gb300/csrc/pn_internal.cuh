@@ -66,6 +66,8 @@ struct GridDev {
   int32_t ncell[3];    // periodic cells per dimension (0 when not periodic)
   int32_t n_total;     // prod(n), or the hash lists of a SpatialHashingCellList
   int32_t hashed;      // SpatialHashingCellList: cells floor(x / cell_size), no offset
+  int32_t cell_off[3]; // SpatialHashingCellList in a dense grid: grid index = cell + cell_off
+  int32_t pad_;
   T min_pad[3];        // padded min corner (cell (1,1,1) starts here)
   T cell_size[3];
   T box_min[3], box_max[3];  // periodic box corners
@@ -81,7 +83,8 @@ __device__ __forceinline__ void cell_coords_exact(const GridDev<T>& g, bool peri
                                                   const T* x, int64_t* c) {
 #pragma unroll
   for (int k = 0; k < D; ++k) {
-    const T q = xdiv(xsub(x[k], g.min_pad[k]), g.cell_size[k]);
+    const T q = g.hashed ? xdiv(x[k], g.cell_size[k])
+                         : xdiv(xsub(x[k], g.min_pad[k]), g.cell_size[k]);
     int64_t ck = wadd(floor_to_int(q), g.hashed ? 0 : 1);
     if (periodic) ck = wadd(jl_mod(wsub(ck, 2), (int64_t)g.ncell[k]), 2);
     c[k] = ck;
@@ -196,6 +199,7 @@ inline GridDev<T> make_grid(const pn_search* s) {
   GridDev<T> g{};
   g.n_total = s->n_total;
   g.hashed = s->hashed;
+  for (int k = 0; k < 3; ++k) g.cell_off[k] = s->hash_off[k];
   for (int k = 0; k < 3; ++k) {
     const bool used = k < s->ndims;
     g.n[k] = used ? (int32_t)s->grid_size[k] : 1;

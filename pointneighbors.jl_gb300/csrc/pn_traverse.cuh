@@ -1052,7 +1052,7 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
   if (clip) {
 #pragma unroll
     for (int k = 1; k < D; ++k) {
-      const T lo = g.min_pad[k] + xfloor((q.x[k] - g.min_pad[k]) / g.cell_size[k]) * g.cell_size[k];
+      const T lo = g.min_pad[k] + (T)(c[k] - 1) * g.cell_size[k];  // the query cell's edge
       below[k] = fmax(q.x[k] - lo - a.clip_m[k], (T)0);
       above[k] = fmax(lo + g.cell_size[k] - q.x[k] - a.clip_m[k], (T)0);
     }
@@ -1163,7 +1163,30 @@ k_trav_list(const TravArgs<T> a, const typename F::Params p) {
     F::fail(p, q);
     valid = false;
   }
-  if (valid) {
+  if (valid && a.g.hashed) {
+    // a SpatialHashingCellList in a dense grid: the query's own cell; one outside the grid's
+    // padding has no neighbours (the domain is unbounded)
+    bool ok = true, inside = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) {
+      q.x[k] = a.x[(int64_t)q.i * D + k];
+      int32_t ch = 0;
+      ok &= hash_cell_1d(a.g, PER, k, q.x[k], ch);
+      const int64_t i = (int64_t)ch + a.g.cell_off[k];
+      inside &= i >= 2 && i <= a.g.n[k] - 1;
+      c[k] = inside ? (int32_t)i : 2;
+    }
+    if (!ok) {
+      set_error(a.err, PN_ERR_OUT_OF_DOMAIN);
+      F::fail(p, q);
+      valid = false;
+    } else if (!inside) {
+      typename F::Acc acc;
+      F::init(acc, p, q);
+      F::finish(acc, p, q);
+      valid = false;
+    }
+  } else if (valid) {
     bool ok = true;
 #pragma unroll
     for (int k = 0; k < D; ++k) {

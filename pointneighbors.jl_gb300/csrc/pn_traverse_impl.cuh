@@ -243,12 +243,14 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
   a.err = s->d_err;
   a.outside = s->d_err + 1;
   a.unsorted = s->d_err + 3;
-  if (s->hashed) {
+  if (s->hashed && !s->hash_dense) {  // the hash lists' traversal
     a.hash_list = s->d_hbucket;
     a.hash_cell = s->d_hcell;
     a.hash_key = s->d_hkey;
     a.hash_mod = hash_mod(s->list_size);
   }
+  // hashed cells need not line up with a periodic box's faces: check every image
+  if (s->hashed) a.outside = nullptr;
   for (int k = 0; k < 3; ++k)
     a.clip_m[k] = (T)(16.0 * (double)std::numeric_limits<T>::epsilon() *
                       (std::fabs(s->min_pad[k]) + std::fabs(s->max_pad[k]) + s->cell_size[k]));
@@ -366,7 +368,8 @@ static int prepare_call(pn_search* s, const T* x, int64_t n_x, const T* y, int64
   // Sorted mode launches one thread per possible slot; the kernel reads the live count.
   c.n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   c.n_launch = c.sorted ? c.n_sorted : c.n_q;
-  c.cache_on = !kMixed && !s->hashed && lists == nullptr && c.sorted && s->pc_cap > 0;
+  c.cache_on = !kMixed && (!s->hashed || s->hash_dense) && lists == nullptr && c.sorted &&
+               s->pc_cap > 0;
   if (c.cache_on && s->pc_valid) use_pair_cache(s, c.a);
   return PN_OK;
 }

@@ -200,3 +200,43 @@ def test_hashing_errors(P):
         P.GridNeighborhoodSearch(2, search_radius=1.0,
                                  cell_list=P.SpatialHashingCellList(2, list_size=10),
                                  update_strategy=P.ParallelIncrementalUpdate())
+
+
+def test_hashing_dense_and_list_layouts_agree(P, O):
+    """The same points in the dense grid layout (list_size above the occupied box's cell
+    count) and in the hash-list layout (below it): identical lists, WCSPH sums within the
+    FP32 bar, and the pair cache (dense layout only) bit-identical to no cache."""
+    W = P.workloads
+    x, v, _ = W.wcsph_cloud(20, seed=12, dtype=np.float32)
+    n = len(x)
+    r = np.float32(3.0)
+    xd = dcoords(x)
+    vd = torch.as_tensor(v, device="cuda").reshape(-1)
+    outs = {}
+    for name, ls, cache in (("dense", 2 * n, False), ("lists", 97, False),
+                            ("dense_cache", 2 * n, True)):
+        cl = P.SpatialHashingCellList(3, list_size=ls, max_points_per_cell=0)
+        nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                       pair_cache=cache)
+        P.initialize(nhs, xd, xd)
+        assert (nhs.grid_info()["grid_size"][0] > 1) == (name != "lists")
+        off, nb = P.neighbor_lists(xd, xd, nhs)
+        rho = torch.zeros(n, device="cuda")
+        prs = torch.zeros(n, device="cuda")
+        acc = torch.zeros(3 * n, device="cuda")
+        for _ in range(2):  # with the cache: the second step walks it
+            P.foreach_point_neighbor(P.WCSPHStep(density=rho, pressure=prs, velocity=vd,
+                                                 accel=acc, **W.WCSPH), xd, xd, nhs)
+        outs[name] = (off.cpu().numpy(), nb.cpu().numpy(), rho.cpu().numpy(),
+                      acc.cpu().numpy())
+    for k in range(2):
+        assert np.array_equal(outs["dense"][k], outs["lists"][k])
+        assert np.array_equal(outs["dense"][k], outs["dense_cache"][k])
+    # density: the same sweep with or without recording the cache; the force over the
+    # cache and the sums of the other layout run in another order
+    assert np.array_equal(outs["dense"][2], outs["dense_cache"][2])
+    for k in (2, 3):
+        ref = outs["dense"][k].astype(np.float64)
+        scale = np.abs(ref).max()
+        assert np.max(np.abs(outs["lists"][k] - ref)) <= 1e-5 * scale
+        assert np.max(np.abs(outs["dense_cache"][k] - ref)) <= 1e-5 * scale
