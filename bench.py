@@ -69,6 +69,9 @@ def parse():
                     help="wcsph workload: FullGridCellList [-1, n_side+1]^3 (incremental "
                          "update, pair cache) or SpatialHashingCellList(list_size = 2n) "
                          "(ParallelUpdate rebuild, no pair cache)")
+    ap.add_argument("--list-size", type=int, default=0,
+                    help="SpatialHashingCellList lists (default 2n); fewer lists than the "
+                         "occupied cells' box has cells select the hash-list layout")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",
@@ -191,7 +194,8 @@ def run_gpu(args, rank, world, local):
     hashing = args.cell_list == "spatial_hashing"
     if hashing:
         # the occupied cells fit 2n lists: the dense layout, which takes the pair cache
-        cl = P.SpatialHashingCellList(3, list_size=2 * n, max_points_per_cell=0)
+        cl = P.SpatialHashingCellList(3, list_size=args.list_size or 2 * n,
+                                      max_points_per_cell=0)
         nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
                                        update_strategy=P.ParallelUpdate(),
                                        pair_cache=args.pair_cache)
@@ -402,7 +406,8 @@ def run_gpu(args, rank, world, local):
         "data": "synthetic (seeded perturbed lattice, numpy PCG64)",
         "config": {"workload": f"WCSPH step, {n_side}^3 = {n:,} points 3D lattice, spacing 1, "
                                "U[-0.25,0.25] noise, r=3, " +
-                               (f"SpatialHashingCellList(list_size={2 * n}), ParallelUpdate, "
+                               (f"SpatialHashingCellList(list_size={args.list_size or 2 * n}), "
+                                "ParallelUpdate, "
                                 if hashing else
                                 f"FullGridCellList [-1,{n_side + 1}]^3, "
                                 "ParallelIncrementalUpdate, ") +

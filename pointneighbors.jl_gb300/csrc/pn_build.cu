@@ -475,39 +475,32 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
 // traversal matches against the cells of a stencil.  The reference instead stores one
 // coordinate tuple and a collision flag per list and compares each point's cell while
 // traversing (nhs_grid.jl:479-513); both visit exactly the points of the stencil's cells.
+// Every point's cell (w = 1 when binned, 0 after an error) and the bounding box of the
+// occupied cells (one atomic per warp and bound).
 template <typename T, int D, bool PER>
 __global__ void __launch_bounds__(BIN_THREADS)
-k_hash_bin(const GridDev<T> g, const HashMod hm, const T* __restrict__ y, int64_t n_y,
-           const int32_t* __restrict__ idx, int32_t m, int32_t* __restrict__ bucket_of,
-           int4* __restrict__ key_of, int32_t* __restrict__ slot_of,
-           int32_t* __restrict__ counts, int32_t* __restrict__ bbox, int32_t* __restrict__ err) {
+k_hash_key(const GridDev<T> g, const T* __restrict__ y, int64_t n_y,
+           const int32_t* __restrict__ idx, int32_t m, int4* __restrict__ key_of,
+           int32_t* __restrict__ bbox, int32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t t = base + threadIdx.x;
-    int32_t bucket = -1;
+    bool ok = false;
     int32_t c[3] = {0, 0, 0};
     if (t < m) {
       const int64_t i = idx ? (int64_t)idx[t] : t;
       if (i < 0 || i >= n_y) {
         set_error(err, PN_ERR_INVALID_ARG);
       } else {
-        bool ok = true;
+        ok = true;
 #pragma unroll
         for (int k = 0; k < D; ++k) ok &= hash_cell_1d(g, PER, k, y[i * D + k], c[k]);
-        if (ok) bucket = spatial_hash<D>(c, hm);
-        else set_error(err, PN_ERR_OUT_OF_DOMAIN);
+        if (!ok) set_error(err, PN_ERR_OUT_OF_DOMAIN);
       }
     }
-    const unsigned valid = __ballot_sync(0xffffffffu, bucket >= 0);
-    if (bucket >= 0) {
-      const unsigned peers = __match_any_sync(valid, bucket);
-      const int leader = __ffs(peers) - 1;
-      int32_t b = 0;
-      if (lane == leader) b = atomicAdd(&counts[bucket], __popc(peers));
-      b = __shfl_sync(peers, b, leader);
-      slot_of[t] = b + __popc(peers & lanemask_lt());
-      // bounding box of the occupied cells (one atomic per warp and bound)
+    const unsigned valid = __ballot_sync(0xffffffffu, ok);
+    if (ok) {
 #pragma unroll
       for (int k = 0; k < D; ++k) {
         const int32_t lo = __reduce_min_sync(valid, c[k]);
@@ -518,10 +511,37 @@ k_hash_bin(const GridDev<T> g, const HashMod hm, const T* __restrict__ y, int64_
         }
       }
     }
+    if (t < m) key_of[t] = make_int4(c[0], c[1], c[2], ok ? 1 : 0);
+  }
+}
+
+// The hash list of every binned point and its rank in the list (a warp-aggregated
+// histogram), for the per-list max_points_per_cell check and the hash-list layout.
+template <int D>
+__global__ void __launch_bounds__(BIN_THREADS)
+k_hash_list_bin(const HashMod hm, const int4* __restrict__ key_of, int32_t m,
+                int32_t* __restrict__ bucket_of, int32_t* __restrict__ slot_of,
+                int32_t* __restrict__ counts) {
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = base + threadIdx.x;
+    int32_t bucket = -1;
     if (t < m) {
-      bucket_of[t] = bucket;
-      key_of[t] = make_int4(c[0], c[1], c[2], 0);
+      const int4 k4 = key_of[t];
+      const int32_t c[3] = {k4.x, k4.y, k4.z};
+      if (k4.w) bucket = spatial_hash<D>(c, hm);
     }
+    const unsigned valid = __ballot_sync(0xffffffffu, bucket >= 0);
+    if (bucket >= 0) {
+      const unsigned peers = __match_any_sync(valid, bucket);
+      const int leader = __ffs(peers) - 1;
+      int32_t b = 0;
+      if (lane == leader) b = atomicAdd(&counts[bucket], __popc(peers));
+      b = __shfl_sync(peers, b, leader);
+      slot_of[t] = b + __popc(peers & lanemask_lt());
+    }
+    if (t < m) bucket_of[t] = bucket;
   }
 }
 
@@ -622,19 +642,19 @@ __global__ void k_hash_bbox_init(int32_t* bbox) {
 }
 
 // The dense layout: grid index = cell + off (1-based, column-major over n), binned like the
-// full grid's k_bin from the cells found by k_hash_bin.
+// full grid's k_bin from the cells found by k_hash_key.
 template <int D>
 __global__ void __launch_bounds__(BIN_THREADS)
-k_hash_dense_bin(const int32_t* bucket_of, const int4* __restrict__ key_of,
-                 int32_t m, int3 off, int3 n, int32_t* cell_of,  // may be bucket_of itself
-                 int32_t* __restrict__ slot_of, int32_t* __restrict__ counts) {
+k_hash_dense_bin(const int4* __restrict__ key_of, int32_t m, int3 off, int3 n,
+                 int32_t* __restrict__ cell_of, int32_t* __restrict__ slot_of,
+                 int32_t* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t t = base + threadIdx.x;
     int32_t cell = -1;
-    if (t < m && bucket_of[t] >= 0) {
-      const int4 c = key_of[t];
+    const int4 c = t < m ? key_of[t] : make_int4(0, 0, 0, 0);
+    if (c.w) {
       cell = c.x + off.x - 1;
       if (D >= 2) cell += (c.y + off.y - 1) * n.x;
       if (D == 3) cell += (c.z + off.z - 1) * n.x * n.y;
@@ -686,32 +706,49 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
   if (rc == PN_OK) rc = ensure_hash_capacity(s, s->cap);
   if (rc != PN_OK) return rc;
   const int32_t nl = (int32_t)s->list_size;
-  // 1. cells, hash lists (with the per-list max_points_per_cell check) and the bounding box
+  // 1. cells and their bounding box
   s->n_total = nl;
   s->hash_dense = false;
-  cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * nl, st);
   k_hash_bbox_init<<<1, 32, 0, st>>>(s->d_hbbox); count_launch();
+  const int blocks = std::max(1, std::min(div_up(std::max<int64_t>(m, 1), BIN_THREADS), 152 * 8));
   if (m > 0) {
     const GridDev<T> g = make_grid<T>(s);
-    const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
     const bool per = s->periodic != 0;
-#define PN_HASH_BIN(DD, PP)                                                                  \
-  k_hash_bin<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(                                     \
-      g, hash_mod(s->list_size), y, n_y, idx, (int32_t)m, s->d_cell_of, s->d_hkey_t,         \
-      s->d_slot_of, s->d_counts, s->d_hbbox, s->d_err)
+#define PN_HASH_KEY(DD, PP)                                                                  \
+  k_hash_key<T, DD, PP><<<blocks, BIN_THREADS, 0, st>>>(g, y, n_y, idx, (int32_t)m,          \
+                                                        s->d_hkey_t, s->d_hbbox, s->d_err)
     switch (s->ndims * 2 + (per ? 1 : 0)) {
-      case 2: PN_HASH_BIN(1, false); break;
-      case 3: PN_HASH_BIN(1, true); break;
-      case 4: PN_HASH_BIN(2, false); break;
-      case 5: PN_HASH_BIN(2, true); break;
-      case 6: PN_HASH_BIN(3, false); break;
-      default: PN_HASH_BIN(3, true); break;
+      case 2: PN_HASH_KEY(1, false); break;
+      case 3: PN_HASH_KEY(1, true); break;
+      case 4: PN_HASH_KEY(2, false); break;
+      case 5: PN_HASH_KEY(2, true); break;
+      case 6: PN_HASH_KEY(3, false); break;
+      default: PN_HASH_KEY(3, true); break;
     }
-#undef PN_HASH_BIN
+#undef PN_HASH_KEY
     count_launch();
   }
-  scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
-  // 2. the layout: a dense grid over the occupied cells' box when it has at most list_size
+  // 2. the hash lists' histogram: for the per-list max_points_per_cell check, and for the
+  // hash-list layout below
+  auto list_bin = [&]() {
+    cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * nl, st);
+    if (m > 0) {
+      const HashMod hm = hash_mod(s->list_size);
+      switch (s->ndims) {
+        case 1: k_hash_list_bin<1><<<blocks, BIN_THREADS, 0, st>>>(hm, s->d_hkey_t, (int32_t)m, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+        case 2: k_hash_list_bin<2><<<blocks, BIN_THREADS, 0, st>>>(hm, s->d_hkey_t, (int32_t)m, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+        default: k_hash_list_bin<3><<<blocks, BIN_THREADS, 0, st>>>(hm, s->d_hkey_t, (int32_t)m, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      }
+      count_launch();
+    }
+    scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
+  };
+  bool lists_binned = false;
+  if (s->cfg.max_points_per_cell > 0) {
+    list_bin();
+    lists_binned = true;
+  }
+  // 3. the layout: a dense grid over the occupied cells' box when it has at most list_size
   // cells (read back: one synchronisation, like the reference's update!), else the lists
   cudaMemcpyAsync(s->h_hbbox, s->d_hbbox, sizeof(int32_t) * 6, cudaMemcpyDeviceToHost, st);
   if (cudaStreamSynchronize(st) != cudaSuccess) return PN_ERR_CUDA;
@@ -744,13 +781,12 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
     s->n_total = (int32_t)cells;
     s->hash_dense = true;
     cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * cells, st);
-    const int blocks = std::max(1, std::min(div_up(m, BIN_THREADS), 152 * 8));
     const int3 off = make_int3(s->hash_off[0], s->hash_off[1], s->hash_off[2]);
     const int3 n = make_int3((int32_t)dims[0], (int32_t)dims[1], (int32_t)dims[2]);
     switch (s->ndims) {
-      case 1: k_hash_dense_bin<1><<<blocks, BIN_THREADS, 0, st>>>(s->d_cell_of, s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
-      case 2: k_hash_dense_bin<2><<<blocks, BIN_THREADS, 0, st>>>(s->d_cell_of, s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
-      default: k_hash_dense_bin<3><<<blocks, BIN_THREADS, 0, st>>>(s->d_cell_of, s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      case 1: k_hash_dense_bin<1><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      case 2: k_hash_dense_bin<2><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      default: k_hash_dense_bin<3><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
     }
     count_launch();
     // (the search's scan state has room for the tiles of list_size >= cells counts)
@@ -761,7 +797,8 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
                                               nullptr); count_launch();
     launch_finalize<T>(s, y, (int32_t)m, st);
   } else if (m > 0) {
-    // 3. the lists: each list's points ranked by (cell, x, index), one entry per cell
+    // 4. the lists: each list's points ranked by (cell, x, index), one entry per cell
+    if (!lists_binned) list_bin();
     const int b = div_up(m, 256);
     k_hash_scatter<<<b, 256, 0, st>>>(s->d_cell_of, s->d_slot_of, s->d_hkey_t, idx, (int32_t)m,
                                       s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
