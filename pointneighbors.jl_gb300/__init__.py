@@ -149,7 +149,7 @@ class FullGridCellList:
 class SpatialHashingCellList:
     """SpatialHashingCellList{ndims}(; list_size, max_points_per_cell = 100)
     (spatial_hashing.jl:79-89): the cells of an unbounded domain hashed into `list_size`
-    lists (about twice the number of points is the reference's advice).
+    lists (the reference recommends about twice the number of points).
     `max_points_per_cell` limits each list; 0 removes the limit."""
 
     def __init__(self, ndims, *, list_size, max_points_per_cell=100):
