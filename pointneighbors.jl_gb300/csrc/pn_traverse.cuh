@@ -1390,10 +1390,18 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   // One loop over all the query's neighbours (row by row, low then high word): a lane moves
   // to its next mask word when it has used up the current one, so lanes with different
   // counts per row do not wait for one another row by row.
-  // wi = 2 row + half indexes the query's 2 NR mask words
+  // wi = 2 row + half indexes the query's 2 NR mask words.  The next row's start and mask
+  // are loaded when a row is entered, so a lane that moves to the next row finds them in
+  // registers instead of stalling its warp on the load.
   int wi = 0;
   int32_t rb0 = __ldg(&a.pc_b0[k]);
   ulonglong2 m = __ldg(&a.pc_mask[k]);
+  int32_t nb0 = 0;
+  ulonglong2 nm = make_ulonglong2(0ull, 0ull);
+  if (NR > 1) {
+    nb0 = __ldg(&a.pc_b0[a.pc_stride + k]);
+    nm = __ldg(&a.pc_mask[a.pc_stride + k]);
+  }
   uint64_t w = m.x;
   for (;;) {
     while (w == 0) {
@@ -1401,10 +1409,15 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
       if (wi & 1) {
         w = m.y;
       } else {
-        const int64_t o = (int64_t)(wi >> 1) * a.pc_stride + k;
-        rb0 = __ldg(&a.pc_b0[o]);
-        m = __ldg(&a.pc_mask[o]);
+        rb0 = nb0;
+        m = nm;
         w = m.x;
+        const int nr = (wi >> 1) + 1;
+        if (nr < NR) {
+          const int64_t o = (int64_t)nr * a.pc_stride + k;
+          nb0 = __ldg(&a.pc_b0[o]);
+          nm = __ldg(&a.pc_mask[o]);
+        }
       }
     }
     if (w == 0) break;
