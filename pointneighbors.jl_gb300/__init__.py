@@ -32,7 +32,8 @@ lib = _lib.load
 
 __all__ = [
     "GridNeighborhoodSearch", "FullGridCellList", "SpatialHashingCellList", "spatial_hash",
-    "PeriodicBox", "ParallelUpdate",
+    "PeriodicBox", "ParallelUpdate", "SemiParallelUpdate", "SerialIncrementalUpdate",
+    "SerialUpdate",
     "ParallelIncrementalUpdate", "initialize", "update", "foreach_point_neighbor",
     "requires_update", "copy_neighborhood_search", "cell_coords", "eachneighbor",
     "neighbor_lists", "CountNeighbors", "NeighborIndexSum", "NBodyAcceleration",
@@ -203,8 +204,54 @@ class ParallelIncrementalUpdate:
         return type(o) is type(self)
 
 
+class SemiParallelUpdate(ParallelIncrementalUpdate):
+    """SemiParallelUpdate() (nhs_grid.jl:158-168): the reference marks the changed cells in
+    parallel and moves their points serially; on the GPU it is the incremental update of
+    ParallelIncrementalUpdate (the same neighbour sets)."""
+
+    def __repr__(self):
+        return "SemiParallelUpdate()"
+
+
+class SerialIncrementalUpdate(ParallelIncrementalUpdate):
+    """SerialIncrementalUpdate() (nhs_grid.jl:170-181): a serial incremental update in the
+    reference; the incremental update of ParallelIncrementalUpdate here."""
+
+    def __repr__(self):
+        return "SerialIncrementalUpdate()"
+
+
+class SerialUpdate(ParallelUpdate):
+    """SerialUpdate() (nhs_grid.jl:183-194): a serial rebuild in the reference; the rebuild of
+    ParallelUpdate here (the same cells; the GPU's in-cell order does not depend on threads)."""
+
+    def __repr__(self):
+        return "SerialUpdate()"
+
+
 _STRATEGIES = {ParallelUpdate: _lib.PN_PARALLEL_UPDATE,
-               ParallelIncrementalUpdate: _lib.PN_PARALLEL_INCREMENTAL_UPDATE}
+               ParallelIncrementalUpdate: _lib.PN_PARALLEL_INCREMENTAL_UPDATE,
+               SemiParallelUpdate: _lib.PN_PARALLEL_INCREMENTAL_UPDATE,
+               SerialIncrementalUpdate: _lib.PN_PARALLEL_INCREMENTAL_UPDATE,
+               SerialUpdate: _lib.PN_PARALLEL_UPDATE}
+# supported_update_strategies (full_grid.jl:39-42, spatial_hashing.jl:42-45), first = default
+_FULL_GRID_STRATEGIES = (ParallelUpdate, ParallelIncrementalUpdate, SemiParallelUpdate,
+                         SerialIncrementalUpdate, SerialUpdate)
+_HASHING_STRATEGIES = (ParallelUpdate, SerialUpdate)
+
+
+def check_update_strategy(cell_list, update_strategy):
+    """The strategy to use (the cell list's first supported one for None), or the reference's
+    ArgumentError (nhs_grid.jl:86-93)."""
+    supported = (_HASHING_STRATEGIES if isinstance(cell_list, SpatialHashingCellList)
+                 else _FULL_GRID_STRATEGIES)
+    if update_strategy is None:
+        return supported[0]()
+    if type(update_strategy) not in supported:
+        options = "(" + ", ".join(t.__name__ for t in supported) + ")"
+        raise ArgumentError(f"{update_strategy} is not a valid update strategy for this "
+                            f"cell list. Available options are {options}")
+    return update_strategy
 
 
 class GridNeighborhoodSearch:
@@ -234,14 +281,7 @@ class GridNeighborhoodSearch:
         if cell_list.ndims != ndims:
             raise ArgumentError(f"a {ndims}D cell list is required for a "
                                 f"GridNeighborhoodSearch{{{ndims}}}")
-        if update_strategy is None:
-            update_strategy = ParallelUpdate()
-        elif type(update_strategy) not in _STRATEGIES or \
-                (hashing and not isinstance(update_strategy, ParallelUpdate)):
-            options = "(ParallelUpdate,)" if hashing else \
-                "(ParallelUpdate, ParallelIncrementalUpdate)"
-            raise ArgumentError(f"{update_strategy} is not a valid update strategy for this "
-                                f"cell list. Available options are {options}")
+        update_strategy = check_update_strategy(cell_list, update_strategy)
         if isinstance(search_radius, numbers.Integral) or isinstance(search_radius, bool):
             raise ArgumentError("`search_radius` cannot be an integer type, since computed "
                                 "distances will be converted to this type")

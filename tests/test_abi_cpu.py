@@ -210,6 +210,16 @@ def test_host_api_argument_errors(pkg):
         P.GridNeighborhoodSearch(2, search_radius=1.0, cell_list=cl3)
     with pytest.raises(P.ArgumentError, match="is not a valid update strategy"):
         P.GridNeighborhoodSearch(3, search_radius=1.0, cell_list=cl3, update_strategy="test")
+    # the reference's five strategies for a FullGridCellList, two for spatial hashing
+    for strat in (P.ParallelUpdate(), P.ParallelIncrementalUpdate(), P.SemiParallelUpdate(),
+                  P.SerialIncrementalUpdate(), P.SerialUpdate()):
+        assert P.check_update_strategy(cl3, strat) is strat
+    assert P.check_update_strategy(cl3, None) == P.ParallelUpdate()
+    hl = P.SpatialHashingCellList(3, list_size=10)
+    assert P.check_update_strategy(hl, P.SerialUpdate()) == P.SerialUpdate()
+    with pytest.raises(P.ArgumentError, match=r"Available options are \(ParallelUpdate, "
+                                              r"SerialUpdate\)"):
+        P.check_update_strategy(hl, P.SemiParallelUpdate())
     with pytest.raises(P.ArgumentError, match="cannot be an integer type"):
         P.GridNeighborhoodSearch(3, search_radius=1, cell_list=cl3)
     box32 = P.PeriodicBox(min_corner=np.zeros(3, np.float32), max_corner=np.ones(3, np.float32))

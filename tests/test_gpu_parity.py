@@ -612,3 +612,25 @@ def test_grid_equals_trivial_1d_and_rectangular_boxes(P, O, case, dt):
     oe, oab = O.foreach(g, cl, x, x, O.F_POTENTIAL, prm, want_abs=True)
     tol = TOL_F32 if dt == np.float32 else TOL_F64
     assert _rel_err(e.cpu().numpy().astype(np.float64), oe, oab) < tol
+
+
+def test_every_update_strategy_gives_the_same_lists(P, O):
+    """The reference's five strategies for a FullGridCellList (full_grid.jl:39-42): on the GPU
+    the serial and semi-parallel ones are the parallel rebuild and incremental update, and
+    all give the brute-force lists after initialize! and update!."""
+    W = P.workloads
+    r = 2.5
+    c1 = W.reference_test_cloud((30, 31, 29), r, seed=1)
+    c2 = W.reference_test_cloud((30, 31, 29), r, seed=2)
+    mn = np.minimum(c1.min(0), c2.min(0)) - r
+    mx = np.maximum(c1.max(0), c2.max(0)) + r
+    toff, tnb = O.trivial_lists(O.grid_create(3, r, mn, mx), c2, c2)
+    for strat in (P.ParallelUpdate(), P.ParallelIncrementalUpdate(), P.SemiParallelUpdate(),
+                  P.SerialIncrementalUpdate(), P.SerialUpdate()):
+        nhs = make_nhs(P, 3, r, mn, mx, len(c1), strategy=strat)
+        P.initialize(nhs, dcoords(c1), dcoords(c1))
+        x = dcoords(c2)
+        P.update(nhs, x, x)
+        off, nb = P.neighbor_lists(x, x, nhs)
+        assert np.array_equal(off.cpu().numpy(), toff), strat
+        assert np.array_equal(nb.cpu().numpy(), tnb), strat
