@@ -309,6 +309,9 @@ int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t 
  * transpose_backend layout for GPUs, without a fixed column height). */
 typedef struct pn_precomputed pn_precomputed;
 int pn_pre_create(const pn_config* cfg, int32_t max_neighbors, pn_precomputed** out);
+/* The same with a SpatialHashingCellList grid search (pn_create_spatial_hashing). */
+int pn_pre_create_spatial_hashing(const pn_config* cfg, int64_t list_size,
+                                  int32_t max_neighbors, pn_precomputed** out);
 int pn_pre_destroy(pn_precomputed* s);
 /* initialize!(search, x, y) (nhs_precomputed.jl:130-147): the grid search bins y, then the
  * neighbour lists of every point of x are built (one host synchronisation to size them).

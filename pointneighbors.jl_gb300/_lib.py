@@ -133,6 +133,8 @@ _SIGNATURES = {
     "pn_export_cells": (C.c_int, [_P, _P, _P, _P]),
     "pn_count_neighbors_noalloc": (C.c_int, [C.POINTER(pn_config), _P, C.c_int64, _P, _P]),
     "pn_pre_create": (C.c_int, [C.POINTER(pn_config), C.c_int32, C.POINTER(_P)]),
+    "pn_pre_create_spatial_hashing": (C.c_int, [C.POINTER(pn_config), C.c_int64, C.c_int32,
+                                                C.POINTER(_P)]),
     "pn_pre_destroy": (C.c_int, [_P]),
     "pn_pre_initialize": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P, C.c_int64, _P]),
     "pn_pre_update": (C.c_int, [_P, _P, C.c_int64, _P, C.c_int64, _P, C.c_int64, C.c_int32,

@@ -204,12 +204,14 @@ using namespace pn;
 
 extern "C" {
 
-int pn_pre_create(const pn_config* cfg, int32_t max_neighbors, pn_precomputed** out) {
+static int pre_create(const pn_config* cfg, int64_t list_size, int32_t max_neighbors,
+                      pn_precomputed** out) {
   if (!cfg || !out || max_neighbors < 0) return PN_ERR_INVALID_ARG;
   *out = nullptr;
   pn_precomputed* s = new (std::nothrow) pn_precomputed();
   if (!s) return PN_ERR_OUT_OF_MEMORY;
-  int rc = pn_create(cfg, &s->grid);
+  int rc = list_size > 0 ? pn_create_spatial_hashing(cfg, list_size, &s->grid)
+                         : pn_create(cfg, &s->grid);
   if (rc == PN_OK && cudaMallocHost(&s->h_total, sizeof(int64_t)) != cudaSuccess) {
     cudaGetLastError();
     rc = PN_ERR_OUT_OF_MEMORY;
@@ -224,6 +226,16 @@ int pn_pre_create(const pn_config* cfg, int32_t max_neighbors, pn_precomputed** 
   s->ndims = cfg->ndims;
   *out = s;
   return PN_OK;
+}
+
+int pn_pre_create(const pn_config* cfg, int32_t max_neighbors, pn_precomputed** out) {
+  return pre_create(cfg, 0, max_neighbors, out);
+}
+
+int pn_pre_create_spatial_hashing(const pn_config* cfg, int64_t list_size,
+                                  int32_t max_neighbors, pn_precomputed** out) {
+  if (list_size < 1) return PN_ERR_INVALID_ARG;
+  return pre_create(cfg, list_size, max_neighbors, out);
 }
 
 int pn_pre_destroy(pn_precomputed* s) {

@@ -6,8 +6,9 @@ from __future__ import annotations
 
 import ctypes as C
 
-from . import (ArgumentError, GridNeighborhoodSearch, PointNeighborsError, _coords, _finish,
-               _lib, _ptr, _raise, _stream, _torch, lib)
+from . import (ArgumentError, GridNeighborhoodSearch, PointNeighborsError,
+               SpatialHashingCellList, _coords, _finish, _lib, _ptr, _raise, _stream, _torch,
+               lib)
 
 # nhs_precomputed.jl:113-124
 _MAX_NEIGHBORS = {1: 32, 2: 64, 3: 320}
@@ -60,7 +61,11 @@ class PrecomputedNeighborhoodSearch:
         C.pointer(cfg)[0] = grid._cfg
         cfg.n_points = self.n_points
         h = C.c_void_p()
-        rc = lib().pn_pre_create(C.byref(cfg), self.max_neighbors, C.byref(h))
+        if isinstance(grid.cell_list, SpatialHashingCellList):
+            rc = lib().pn_pre_create_spatial_hashing(C.byref(cfg), grid.cell_list.list_size,
+                                                     self.max_neighbors, C.byref(h))
+        else:
+            rc = lib().pn_pre_create(C.byref(cfg), self.max_neighbors, C.byref(h))
         if rc != _lib.PN_OK:
             _raise(rc, "PrecomputedNeighborhoodSearch")
         self._h = h

@@ -240,3 +240,25 @@ def test_hashing_dense_and_list_layouts_agree(P, O):
         scale = np.abs(ref).max()
         assert np.max(np.abs(outs["lists"][k] - ref)) <= 1e-5 * scale
         assert np.max(np.abs(outs["dense_cache"][k] - ref)) <= 1e-5 * scale
+
+
+@pytest.mark.parametrize("list_size", [None, 97])
+def test_precomputed_over_hashing(P, O, list_size):
+    """PrecomputedNeighborhoodSearch whose lists a SpatialHashingCellList grid search
+    computes (dense layout and hash lists): its lists equal brute force after update!."""
+    W = P.workloads
+    r = 2.5
+    c1 = W.reference_test_cloud((21, 20, 19), r, seed=1)
+    c2 = W.reference_test_cloud((21, 20, 19), r, seed=2)
+    n = len(c1)
+    grid = hashed(P, 3, r, n, list_size=list_size)
+    pre = P.PrecomputedNeighborhoodSearch(3, n_points=n, update_neighborhood_search=grid)
+    P.initialize(pre, dcoords(c1), dcoords(c1))
+    x = dcoords(c2)
+    P.update(pre, x, x)
+    off, nb = P.neighbor_lists(x, x, pre)
+    toff, tnb = O.trivial_lists(O.grid_create(3, r, c2.min(0) - r, c2.max(0) + r), c2, c2)
+    assert np.array_equal(off.cpu().numpy(), toff) and np.array_equal(nb.cpu().numpy(), tnb)
+    cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt), x, x, pre)
+    assert np.array_equal(cnt.cpu().numpy(), np.diff(toff))
