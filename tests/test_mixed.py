@@ -199,3 +199,20 @@ def test_mixed_adjoint_matches_float64_search(P):
     assert abs(float(lm.detach()) - float(l64.detach())) <= 1e-5 * abs(float(l64.detach()))
     gm, g64 = xm.grad.cpu().numpy(), x64.grad.cpu().numpy()
     assert np.max(np.abs(gm - g64)) <= 1e-3 * np.max(np.abs(g64))
+
+
+def test_golden_gpu_tutorial_mixed(P, golden):
+    """docs/literate/src/tut_gpu_usage.jl:38-50 with Float64 coordinates and the tutorial's
+    Float32 radius 3.0f0 (the tutorial's mixed-precision variant): the neighbour counts'
+    extrema of test/gpu.jl:35."""
+    c = golden["gpu_tutorial"]
+    pts = P.workloads.lattice(c["n_per_dim"], dtype=np.float64)
+    r = np.float32(c["radius"])
+    cl = P.FullGridCellList(min_corner=pts.min(0), max_corner=pts.max(0), search_radius=r)
+    nhs = P.GridNeighborhoodSearch(2, search_radius=r, n_points=len(pts), cell_list=cl)
+    assert nhs.mixed
+    x = dcoords(pts)
+    P.initialize(nhs, x, x)
+    n = torch.zeros(len(pts), dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(n), x, x, nhs)
+    assert (int(n.min()), int(n.max())) == tuple(c["expected_extrema"])
