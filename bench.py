@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--list-size", type=int, default=0,
                     help="SpatialHashingCellList lists (default 2n); fewer lists than the "
                          "occupied cells' box has cells select the hash-list layout")
+    ap.add_argument("--clouds", type=int, default=512,
+                    help="batched workload: number of clouds")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="wcsph",
@@ -676,7 +678,7 @@ def run_gpu_batched(args, rank, world, local):
     L = P._lib
     lib = P.lib()
     torch.cuda.set_device(local)
-    clouds = P.workloads.batched_clouds(n_clouds=512, seed=1)
+    clouds = P.workloads.batched_clouds(n_clouds=args.clouds, seed=1)
     ncl = len(clouds)
     sizes = [len(c["x"]) for c in clouds]
     off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
@@ -799,11 +801,11 @@ def run_gpu_batched(args, rank, world, local):
         pairs += int(cnt.to(torch.int64).sum()) * sum(1 for s_ in range(Wm, Wm + K)
                                                       if walk[s_] is xs)
     out = {"metric": "batched WCSPH step speed-up: per-cloud launches / CUDA-graph batch "
-                     "(512 clouds, same GPU)",
+                     f"({args.clouds} clouds, same GPU)",
            "value": per_cloud_ms / graph_ms, "unit": "x", "n_gpus": world, "steps": K,
            "warmup": Wm, "ms_per_step": graph_ms, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded perturbed lattices)",
-           "config": {"workload": f"512 clouds, N log-uniform [1e3, 2e5] (side round(N^(1/3)), "
+           "config": {"workload": f"{args.clouds} clouds, N log-uniform [1e3, 2e5] (side round(N^(1/3)), "
                                   f"total {N:,} points), radius U[2, 3.5], h = r/2, box "
                                   "[-1, side+1]^3, positions alternating x0 / x0 + N(0,0.05^2), "
                                   "update! + WCSPH density + force",
