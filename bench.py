@@ -43,7 +43,7 @@ METRIC = "WCSPH pair-evals/s (8M pts, FP32, r=3, density+force+incremental updat
 UNIT = "pair-evals/s"
 # Algorithmic bytes per point of one force sweep (FP32): read x 12, v 12, rho 4, the
 # point's index 4, write the acceleration 12.
-FORCE_BYTES_PER_POINT = {"float32": 44, "float64": 84}
+FORCE_BYTES_PER_POINT = {"float32": 44, "float64": 84, "mixed": 56}
 # DRAM bytes per point of one force sweep measured by ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum, 4,096,000-point capture of the same workload): over the pair cache
 # (the default) most of it is the cache's hit masks; without the cache (stencil) it is
@@ -59,7 +59,9 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n-side", type=int, default=200, help="lattice points per dimension")
-    ap.add_argument("--dtype", default="float32", choices=["float32", "float64"])
+    ap.add_argument("--dtype", default="float32", choices=["float32", "float64", "mixed"],
+                    help="mixed: Float64 coordinates with a Float32 search radius (Float32 "
+                         "pair arithmetic and arrays), the wcsph workload only")
     ap.add_argument("--cpu-sample", type=int, default=400_000,
                     help="query points in the CPU baseline sample")
     ap.add_argument("--pair-cache", type=int, default=1,
@@ -186,13 +188,19 @@ def run_gpu(args, rank, world, local):
     P = __graft_entry__.package()
     W = P.workloads
     torch.cuda.set_device(local)
+    if args.dtype == "mixed":
+        args.pair_cache = 0  # the pair cache is not used with mixed precision
+    # coordinates in dt, pair arithmetic and per-point arrays in vdt (Float32 for "mixed")
     dt = np.float32 if args.dtype == "float32" else np.float64
-    tdt = torch.float32 if dt == np.float32 else torch.float64
+    vdt = np.float64 if args.dtype == "float64" else np.float32
+    tcd = torch.float32 if dt == np.float32 else torch.float64
+    tdt = torch.float32 if vdt == np.float32 else torch.float64
     n_side = args.n_side
     x0, v, dx = W.wcsph_cloud(n_side, seed=1, dtype=dt)
+    v = v.astype(vdt)
     x1 = (x0.astype(np.float64) + dx).astype(dt)
     n = len(x0)
-    r = dt(3.0)
+    r = vdt(3.0)
     hashing = args.cell_list == "spatial_hashing"
     if hashing:
         # the occupied cells fit 2n lists: the dense layout, which takes the pair cache
@@ -224,7 +232,7 @@ def run_gpu(args, rank, world, local):
     walk = [torch.as_tensor(x1, device="cuda")]
     for _ in range(Wm + K - 1):
         walk.append(walk[-1] + dt(0.05) * torch.randn(walk[-1].shape, generator=gen,
-                                                      device="cuda", dtype=tdt))
+                                                      device="cuda", dtype=tcd))
     # ordered pairs (self included) at every step's positions, with a separate search
     cl2 = P.FullGridCellList(min_corner=np.full(3, -1.0, dt), max_corner=np.full(3, n_side + 1.0, dt),
                              search_radius=r, max_points_per_cell=0)
@@ -295,7 +303,7 @@ def run_gpu(args, rank, world, local):
         v_h = torch.as_tensor(v).reshape(-1).pin_memory()
         rho_h = [torch.empty(n, dtype=tdt).pin_memory() for _ in range(2)]
         acc_h = [torch.empty(3 * n, dtype=tdt).pin_memory() for _ in range(2)]
-        xb = [torch.empty((n, 3), dtype=tdt, device="cuda") for _ in range(2)]
+        xb = [torch.empty((n, 3), dtype=tcd, device="cuda") for _ in range(2)]
         xbT = [t.T for t in xb]
         vb = [torch.empty(3 * n, dtype=tdt, device="cuda") for _ in range(2)]
         rb = [torch.empty(n, dtype=tdt, device="cuda") for _ in range(2)]
@@ -364,9 +372,10 @@ def run_gpu(args, rank, world, local):
         # the last step's outputs equal the device-timed run's (same positions, same search)
         same = bool(torch.equal(rho_h[(K - 1) % 2], rho.cpu()) and
                     torch.equal(acc_h[(K - 1) % 2], acc.cpu()))
-        tb = 4 if dt == np.float32 else 8
-        e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT, "h2d_bytes_per_step": 6 * n * tb,
-               "d2h_bytes_per_step": 4 * n * tb, "ms_per_step": 1e3 * e2e_s / K,
+        cb, vb_ = np.dtype(dt).itemsize, np.dtype(vdt).itemsize
+        e2e = {"value": e2e_pairs / e2e_s, "unit": UNIT,
+               "h2d_bytes_per_step": 3 * n * cb + 3 * n * vb_,
+               "d2h_bytes_per_step": 4 * n * vb_, "ms_per_step": 1e3 * e2e_s / K,
                "outputs_equal_device_run": same,
                "path": "pinned host -> cudaMemcpyAsync (copy stream, double-buffered) -> "
                        "pn_update + pn_foreach_point_neighbor (density, force) -> "
@@ -404,7 +413,9 @@ def run_gpu(args, rank, world, local):
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": 1e3 * max_s / K, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if dt == np.float32 else "f64",
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"float32": "f32", "float64": "f64",
+                  "mixed": "f64 coordinates, f32 pair arithmetic"}[args.dtype],
         "data": "synthetic (seeded perturbed lattice, numpy PCG64)",
         "config": {"workload": f"WCSPH step, {n_side}^3 = {n:,} points 3D lattice, spacing 1, "
                                "U[-0.25,0.25] noise, r=3, " +

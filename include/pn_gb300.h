@@ -63,8 +63,10 @@ typedef enum { PN_FLOAT32 = 0, PN_FLOAT64 = 1 } pn_dtype;
  * the Float64 difference converted to Float32, and d^2, the periodic correction and the test
  * d^2 <= r^2 are Float32 (neighborhood_search.jl:402-410).  The pair functions' arrays
  * (masses, density, pressure, velocity, accel, energy, ...) are then Float32, the type of
- * pos_diff and distance.  Not taken by pn_count_neighbors_noalloc or pn_batch_create; the
- * pair cache is not used. */
+ * pos_diff and distance.  Neighbour sets are the reference's exactly; for x is y the pair
+ * functions receive pos_diff within about 2^-22 of the reference's Float32 value away from
+ * the radius (the exact value near it).  Not taken by pn_count_neighbors_noalloc or
+ * pn_batch_create; the pair cache is not used. */
 #define PN_FLAG_FLOAT32_SEARCH 1
 
 /* nhs_grid.jl:135-192 update strategies available for a FullGridCellList. */

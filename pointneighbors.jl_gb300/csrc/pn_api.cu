@@ -32,12 +32,13 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 static void free_points(pn_search* s) {
   void* ptrs[] = {s->d_cell_of, s->d_slot_of, s->d_tmp_perm, s->d_perm, s->d_cell_of_slot,
                   s->d_pos,     s->d_pa,      s->d_pb,       s->d_main_perm, s->d_ovf_list,
-                  s->d_ovf_cell, s->d_ovf_slot};
+                  s->d_ovf_cell, s->d_ovf_slot, s->d_pos32, s->d_pos32lo};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   s->d_cell_of = s->d_slot_of = s->d_tmp_perm = s->d_perm = s->d_cell_of_slot = nullptr;
   s->d_main_perm = s->d_ovf_list = s->d_ovf_cell = s->d_ovf_slot = nullptr;
   s->d_pos = s->d_pa = s->d_pb = nullptr;
+  s->d_pos32 = s->d_pos32lo = nullptr;
   s->cap = 0;
 }
 
@@ -65,6 +66,10 @@ int ensure_capacity(pn_search* s, int64_t n) {
   alloc(&s->d_pos, tb * 4 * slots);
   alloc(&s->d_pa, tb * 4 * slots);
   alloc(&s->d_pb, tb * 4 * slots);
+  if (s->mixed) {
+    alloc((void**)&s->d_pos32, sizeof(float) * 4 * slots);
+    alloc((void**)&s->d_pos32lo, sizeof(float) * 4 * slots);
+  }
   alloc((void**)&s->d_main_perm, i4 * cap);
   alloc((void**)&s->d_ovf_list, i4 * cap);
   alloc((void**)&s->d_ovf_cell, i4 * cap);

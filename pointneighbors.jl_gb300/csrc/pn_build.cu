@@ -464,6 +464,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   s->main_perm_valid = false;
   s->n_ovf = 0;
   s->updates_since_build = 0;
+  refresh_pos32(s, st);
   return cuda_status(cudaGetLastError());
 }
 
@@ -940,12 +941,52 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
                                             s->d_ovf_start, s->d_ovf_n, gate); count_launch();
   s->ovf_active = true;
   s->pc_valid = false;
+  refresh_pos32(s, st);
   // The mover count feeds the rebuild policy of the next update; it is read back lazily.
   cudaMemcpyAsync(s->h_ovf_n, s->d_ovf_n, sizeof(int32_t), cudaMemcpyDeviceToHost, st);
   cudaEventRecord(s->ev_ovf, st);
   s->ovf_pending = true;
   ++s->updates_since_build;
   return cuda_status(cudaGetLastError());
+}
+
+// The Float32 split of the cell-sorted coordinates: hi = fl32(x), lo = fl32(x - hi) (x - hi
+// is exact in Float64); vacated slots keep NaN.
+template <int D>
+__global__ void __launch_bounds__(256)
+k_to_pos32(const double* __restrict__ pos, const int32_t* __restrict__ n_slots,
+           int64_t n_max, float* __restrict__ pos32, float* __restrict__ pos32lo) {
+  const int64_t n = min((int64_t)*n_slots, n_max);
+  constexpr int S = PS<D>::value;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (int64_t)gridDim.x * blockDim.x) {
+    float h[4] = {0.0f, 0.0f, 0.0f, 0.0f}, l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+      const double x = pos[k * S + d];
+      h[d] = __double2float_rn(x);
+      l[d] = __double2float_rn(__dsub_rn(x, (double)h[d]));
+    }
+#pragma unroll
+    for (int d = 0; d < S; ++d) {
+      pos32[k * S + d] = h[d];
+      pos32lo[k * S + d] = l[d];
+    }
+  }
+}
+
+void refresh_pos32(pn_search* s, cudaStream_t st) {
+  if (!s->mixed || s->d_pos32 == nullptr || s->n_binned == 0) return;
+  const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
+  const int64_t n_max = 2 * s->cap;
+  const int b = std::max(1, std::min(div_up(n_max, 256), 152 * 8));
+  const double* pos = static_cast<const double*>(s->d_pos);
+  switch (s->ndims) {
+    case 1: k_to_pos32<1><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo); break;
+    case 2: k_to_pos32<2><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo); break;
+    default: k_to_pos32<3><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo); break;
+  }
+  count_launch();
 }
 
 template int update_incremental<float>(pn_search*, const float*, int64_t, cudaStream_t);

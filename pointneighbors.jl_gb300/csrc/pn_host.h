@@ -49,6 +49,8 @@ struct pn_search {
   void* d_pos = nullptr;           // [2 cap * 4] T
   void* d_pa = nullptr;            // [2 cap * 4] T  WCSPH neighbour state (x, y, z, p/rho^2)
   void* d_pb = nullptr;            // [2 cap * 4] T  WCSPH neighbour state (vx, vy, vz, rho)
+  float* d_pos32 = nullptr;        // [2 cap * 4] PN_FLAG_FLOAT32_SEARCH: pos rounded to Float32
+  float* d_pos32lo = nullptr;      // [2 cap * 4] and the rest, pos - pos32, rounded to Float32
   int32_t* d_qcount = nullptr;     // [qcount_cap] per-query counts (neighbour lists)
   int64_t qcount_cap = 0;
   int64_t* d_part = nullptr;       // partial sums of the 64-bit scan
@@ -141,6 +143,8 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st);
 template <typename T>
 int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t st);
 int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
+// The Float32 copy of the cell-sorted coordinates of a mixed-precision search (d_pos32).
+void refresh_pos32(pn_search* s, cudaStream_t st);
 int export_hash_lists(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
 int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st);
 // generic pieces of the build, reused by the batched build (pn_batch.cu)

@@ -730,8 +730,43 @@ struct MixedGeom {
   float box[3];        // PeriodicBox size (Float32)
   int32_t per;         // periodic box present (the traversal's PER)
   const double* pos;   // cell-sorted coordinates (a candidate's Float64 values)
-  const float* state;  // 3D force / adjoint sweeps: F's aux is state[4 js + 3], else null
+  const float* state;  // 3D force / adjoint sweeps: F's aux is state[4 js + 3], or null
+  const float* hi;     // MixedFast: the coordinates split into Float32 hi + lo parts
+  const float* lo;
+  float eb;            // MixedFast: bound on what the split loses of x - y
 };
+
+// Error-free sum: s + e == a + b exactly (Knuth's TwoSum, additions only).
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+  s = __fadd_rn(a, b);
+  const float bb = __fsub_rn(s, a);
+  e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// Float32(Float64(x - y)) for x = xh + xl + ex, y = yh + yl + ey (xh = fl32(x), xl =
+// fl32(x - xh)), with Float32 operations only.  (s, t) and (p, q) hold xh - yh and xl - yl
+// exactly; their sum, formed as zh + zl with zh its nearest Float32, is off from x - y by at
+// most eb (the lost ex - ey plus the rounding of t + p + q).  zh is the answer when x - y and
+// its Float64 rounding lie strictly inside zh's rounding interval: |zl| + eb + |zh| 2^-52
+// below half a unit in zh's last place (a quarter below a power of two, where the interval
+// is narrower underneath).  Returns false otherwise (then x - y is formed in Float64).
+__device__ __forceinline__ bool diff_f32(float xh, float xl, float yh, float yl, float eb,
+                                         float& r) {
+  float s, t, p, q;
+  two_sum(xh, -yh, s, t);
+  two_sum(xl, -yl, p, q);
+  const float w = __fadd_rn(__fadd_rn(t, p), q);
+  float zh, zl;
+  two_sum(s, w, zh, zl);
+  const float az = fabsf(zh);
+  if (!(az >= 1e-30f)) return false;  // tiny or zero (or NaN)
+  const int bits = __float_as_int(az);
+  float half_ulp = __int_as_float((bits & 0x7f800000) - (24 << 23));
+  if ((bits & 0x007fffff) == 0) half_ulp = __fmul_rn(half_ulp, 0.5f);
+  if (!(__fsub_rn(half_ulp, fabsf(zl)) > __fadd_rn(eb, __fmul_rn(az, 2.3e-16f)))) return false;
+  r = zh;
+  return true;
+}
 template <class PF>
 struct MixedParams {
   PF f;
@@ -741,7 +776,7 @@ struct MixedParams {
 template <int D, class F>
 struct Mixed {
   static constexpr bool kCountOnly = false;  // every candidate is re-tested in Float32
-  static constexpr bool kInline = F::kInline;
+  static constexpr bool kInline = false;     // a costly pair step (see MixedFast)
   using Params = MixedParams<typename F::Params>;  // the same type for every D
   using Acc = typename F::Acc;
   static __device__ __forceinline__ Query<float, D> narrow(const Query<double, D>& q) {
@@ -795,6 +830,93 @@ template <template <typename, int> class F>
 struct MixedOf {
   template <typename T, int D>
   using type = Mixed<D, F<float, D>>;
+};
+
+// The same rule for the cell-sorted queries (x is y), with the traversal itself in Float32:
+// its candidates come from a Float32 copy of the coordinates (or the Float32 WCSPH state)
+// with the radius widened past that rounding.  This wrapper decides the reference's Float32
+// test exactly -- on a hi/lo Float32 difference, and where d2 lies near r^2 on the exact
+// Float32(Float64(xi - yj)) (diff_f32) -- and gives the pair function that difference
+// (the exact one near r^2, else one within about 2^-22 of it).
+template <int D, class F>
+struct MixedFast {
+  static constexpr bool kCountOnly = false;
+  // candidates are classified in chunks, then each lane walks its own accepted ones (the
+  // inline form, with lanes waiting at every candidate another lane accepts, measured the
+  // same or slower)
+  static constexpr bool kInline = false;
+  using Params = MixedParams<typename F::Params>;
+  struct Acc { typename F::Acc f; float xl[D]; };
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
+  static __device__ __forceinline__ void fail(const Params& p, const Query<float, D>& q) {
+    F::fail(p.f, q);
+  }
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<float, D>& q) {
+    F::init(a.f, p.f, q);
+    load_pos<float, D>(p.m.lo, q.k, a.xl);
+  }
+  // The exact Float32(Float64(xi - yj)) from the hi/lo split (q.x holds the query's hi
+  // part), in Float64 where the split cannot decide the rounding.
+  static __device__ __forceinline__ void exact_diff(const Acc& a, const Params& p,
+                                                    const Query<float, D>& q, int32_t js,
+                                                    const float* yh, const float* yl,
+                                                    float* pf) {
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < D; ++k) ok &= diff_f32(q.x[k], a.xl[k], yh[k], yl[k], p.m.eb, pf[k]);
+    if (!ok) {
+      double xi[D], yj[D];
+      load_pos<double, D>(p.m.pos, q.k, xi);
+      load_pos<double, D>(p.m.pos, js, yj);
+#pragma unroll
+      for (int k = 0; k < D; ++k) pf[k] = __double2float_rn(xsub(xi[k], yj[k]));
+    }
+  }
+  static __device__ __forceinline__ void wrap_f32(const Params& p, float* pf) {
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      pf[k] = xsub(pf[k], xmul(p.m.box[k], xrint(xdiv(pf[k], p.m.box[k]))));
+  }
+  // pos_diff as (xh - yh) + (xl - yl) in Float32: within about 2^-22 |pos_diff| of the
+  // reference's Float32(Float64(xi - yj)), close enough for the pair function's sums.  The
+  // neighbour test (and the periodic image) is decided on it unless d2 lies within a
+  // relative 1e-5 of r^2, where the exact pos_diff decides instead.
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<float, D>& q,
+                                              int32_t js, const float*, float, float aux) {
+    float yh[D], yl[D], pf[D];
+    load_pos<float, D>(p.m.hi, js, yh);
+    load_pos<float, D>(p.m.lo, js, yl);
+#pragma unroll
+    for (int k = 0; k < D; ++k)
+      pf[k] = js == q.k ? 0.0f : __fadd_rn(__fsub_rn(q.x[k], yh[k]), __fsub_rn(a.xl[k], yl[k]));
+    const float band = __fmul_rn(p.m.r2, 1e-5f);
+    float d2 = d2_exact<float, D>(pf);
+    bool exact = fabsf(__fsub_rn(d2, p.m.r2)) <= band;
+    if (!exact && p.m.per && d2 > p.m.r2) {
+      wrap_f32(p, pf);
+      d2 = d2_exact<float, D>(pf);
+      exact = fabsf(__fsub_rn(d2, p.m.r2)) <= band;
+    }
+    if (exact && js != q.k) {
+      exact_diff(a, p, q, js, yh, yl, pf);
+      d2 = d2_exact<float, D>(pf);
+      if (p.m.per && d2 > p.m.r2) {
+        wrap_f32(p, pf);
+        d2 = d2_exact<float, D>(pf);
+      }
+    }
+    if (!(d2 <= p.m.r2)) return;
+    F::pair(a.f, p.f, q, js, pf, d2, aux);
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<float, D>& q) {
+    F::finish(a.f, p.f, q);
+  }
+};
+
+template <template <typename, int> class F>
+struct MixedFastOf {
+  template <typename T, int D>
+  using type = MixedFast<D, F<float, D>>;
 };
 
 

@@ -133,6 +133,13 @@ static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m, cudaStream_t 
   return PN_OK;
 }
 
+// Pair functions that only ever run in the sorted traversal (MixedFast): the other kernels
+// are not instantiated for them.
+template <class F>
+struct sorted_only { static constexpr bool value = false; };
+template <int D, class G>
+struct sorted_only<MixedFast<D, G>> { static constexpr bool value = true; };
+
 template <typename T, template <typename, int> class F>
 static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename F<T, 1>::Params& p,
                        bool sorted, int64_t n_launch, cudaStream_t st) {
@@ -141,7 +148,10 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
   const int key = s->ndims * 2 + (s->periodic ? 1 : 0);
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
-    if (a.pc_mask != nullptr && sorted) {                                               \
+    if constexpr (sorted_only<F<T, DD>>::value) {                                       \
+      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
+      count_launch();                                                                   \
+    } else if (a.pc_mask != nullptr && sorted) {                                        \
       k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);       \
       count_launch();                                                                   \
     } else if (a.nb != nullptr) {                                                       \
@@ -176,7 +186,9 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
     default: return PN_ERR_INVALID_ARG;
   }
 #undef PN_TRAV_CASE
-  if ((a.nb != nullptr || a.pc_mask != nullptr) && a.nb_fallback && sorted) {
+  if constexpr (sorted_only<F<T, 1>>::value) {
+    return cuda_status(cudaGetLastError());
+  } else if ((a.nb != nullptr || a.pc_mask != nullptr) && a.nb_fallback && sorted) {
     // queries the pair cache or the lists could not hold: the stencil traversal, for
     // those only (the full grid's; neither is offered over hash lists)
     TravArgs<T> g = a;
@@ -296,24 +308,44 @@ static MixedGeom mixed_geom(const pn_search* s, TravArgs<double>* a) {
 // coordinates, Mixed<D, F<float, D>> with the geometry m.
 template <typename T, typename V, template <typename, int> class F>
 static int launch_pair(const pn_search* s, const TravArgs<T>& a, const typename F<V, 1>::Params& p,
-                       const MixedGeom& m, bool sorted, int64_t n_launch, cudaStream_t st) {
+                       const MixedGeom& m, bool sorted, int64_t n_launch, cudaStream_t st,
+                       const TravArgs<float>* fast = nullptr) {
   if constexpr (std::is_same<T, V>::value) {
     (void)m;
+    (void)fast;
     return launch_trav<T, F>(s, a, p, sorted, n_launch, st);
   } else {
     const MixedParams<typename F<V, 1>::Params> mp{p, m};
+    if (fast != nullptr)  // sorted queries: the Float32 traversal
+      return launch_trav<float, MixedFastOf<F>::template type>(s, *fast, mp, sorted, n_launch,
+                                                                st);
     return launch_trav<T, MixedOf<F>::template type>(s, a, mp, sorted, n_launch, st);
   }
 }
 
-// In 3D the WCSPH / adjoint state (x, y, z, aux) has the coordinates' layout: the force and
-// backward sweeps read their candidates from it and get aux with the same load.  Over
-// Float64 coordinates the candidates stay the coordinates and Mixed loads aux.
-template <typename T, typename V>
-static void use_state(const pn_search* s, TravArgs<T>& a, MixedGeom& m, const V* state) {
-  if (s->ndims != 3) return;
-  if constexpr (std::is_same<T, V>::value) a.pos = state;
-  else m.state = state;
+// The Float32 traversal of a mixed search's sorted queries: over the Float32 copy of the
+// coordinates, with the radius widened past its rounding.  Each rounded coordinate is off by
+// at most u |x| (u = 2^-24), so a pos_diff component by at most u (|xi| + |xj| + |pd|); the
+// margin below covers that for every coordinate of the grid, plus the periodic correction's
+// and the Float32 distance test's own rounding.
+static TravArgs<float> mixed_fast_args(const pn_search* s, int64_t n_q) {
+  TravArgs<float> a = trav_args<float>(s, nullptr, 0, nullptr, n_q);
+  a.pos = s->d_pos32;
+  const double u = std::ldexp(1.0, -24);
+  double ext = 0.0, box = 0.0;
+  for (int k = 0; k < s->ndims; ++k) {
+    ext = std::max(ext, std::max(std::fabs(s->min_pad[k]), std::fabs(s->max_pad[k])));
+    box += s->box_size[k];
+  }
+  const double rs = s->radius * (1.0 + 1e-5) +
+                    4.0 * std::sqrt((double)s->ndims) * u * (2.0 * ext + 2.0 * s->radius) +
+                    4.0 * u * box;
+  a.g.r = (float)rs;
+  a.g.r2 = (float)(rs * rs * (1.0 + 1e-6));
+  const double uf = std::numeric_limits<float>::epsilon() / 2;
+  a.r2_lo = (float)((double)a.g.r2 * (1.0 - 32.0 * uf));
+  a.r2_hi = (float)((double)a.g.r2 * (1.0 + 32.0 * uf));
+  return a;
 }
 
 // One foreach_point_neighbor call after its checks: the traversal arguments and the launch
@@ -325,7 +357,27 @@ struct TravCall {
   bool sorted;    // the queries are the cell-sorted slots (x is y, every point binned)
   bool cache_on;  // the pair cache is walked or built by this call
   int64_t n_q, n_sorted, n_launch;
+  bool fast;               // mixed precision, sorted queries: the Float32 traversal a32
+  TravArgs<float> a32;
+  const TravArgs<float>* fast_args() const { return fast ? &a32 : nullptr; }
 };
+
+// In 3D the WCSPH / adjoint state (x, y, z, aux) has the coordinates' layout: the force and
+// backward sweeps read their candidates from it and get aux with the same load.  A mixed
+// search's Float32 traversal does the same on its Float32 state; its Float64 traversal (list
+// mode) keeps the coordinates as candidates and Mixed loads aux.
+template <typename T, typename V>
+static void use_state(const pn_search* s, TravArgs<T>& a, MixedGeom& m, TravCall<T>& c,
+                      const V* state) {
+  if (s->ndims != 3) return;
+  if constexpr (std::is_same<T, V>::value) {
+    a.pos = state;
+  } else if (c.fast) {
+    c.a32.pos = state;
+  } else {
+    m.state = state;
+  }
+}
 
 // Walk the pair cache (valid since the last density / adjoint-forward sweep).
 template <typename T>
@@ -370,6 +422,17 @@ static int prepare_call(pn_search* s, const T* x, int64_t n_x, const T* y, int64
   c.n_launch = c.sorted ? c.n_sorted : c.n_q;
   c.cache_on = !kMixed && (!s->hashed || s->hash_dense) && lists == nullptr && c.sorted &&
                s->pc_cap > 0;
+  c.fast = kMixed && c.sorted && lists == nullptr && s->d_pos32 != nullptr && !s->hashed;
+  if (c.fast) {
+    c.a32 = mixed_fast_args(s, c.n_q);
+    c.m.hi = s->d_pos32;
+    c.m.lo = s->d_pos32lo;
+    // ex - ey and the rounding of t + p + q: a few units of 2^-48 of the coordinates
+    double ext = 0.0;
+    for (int k = 0; k < s->ndims; ++k)
+      ext = std::max(ext, std::max(std::fabs(s->min_pad[k]), std::fabs(s->max_pad[k])));
+    c.m.eb = (float)(std::ldexp(1.0, -44) * (ext + s->radius));
+  }
   if (c.cache_on && s->pc_valid) use_pair_cache(s, c.a);
   return PN_OK;
 }
@@ -395,12 +458,13 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
     case PN_F_COUNT: {
       const auto* u = static_cast<const pn_count_params*>(params);
       CountParams<V> p{u->counts, 0};
-      return launch_pair<T, V, FCount>(s, a, p, m, sorted, n_launch, st);
+      return launch_pair<T, V, FCount>(s, a, p, m, sorted, n_launch, st, c.fast_args());
     }
     case PN_F_INDEX_SUM: {
       const auto* u = static_cast<const pn_index_sum_params*>(params);
       IndexSumParams<V> p{u->sums, s->d_perm};
-      return launch_pair<T, V, FIndexSum>(s, a, p, m, sorted, n_launch, st);
+      return launch_pair<T, V, FIndexSum>(s, a, p, m, sorted, n_launch, st,
+                                           c.fast_args());
     }
     case PN_F_NEIGHBOR_LIST: {
       const auto* u = static_cast<const pn_neighbor_list_params*>(params);
@@ -412,7 +476,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
         counts = s->d_qcount;
       }
       CountParams<V> pc{counts, 1};
-      int rc = launch_pair<T, V, FCount>(s, a, pc, m, sorted, n_launch, st);
+      int rc = launch_pair<T, V, FCount>(s, a, pc, m, sorted, n_launch, st, c.fast_args());
       if (rc != PN_OK) return rc;
       rc = scan64(s, counts, n_q, u->offsets, st);
       if (rc != PN_OK) return rc;
@@ -421,7 +485,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
       if (u->neighbors == nullptr || u->capacity <= 0) return cuda_status(cudaGetLastError());
       k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err); count_launch();
       EmitParams<V> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
-      rc = launch_pair<T, V, FEmit>(s, a, pe, m, sorted, n_launch, st);
+      rc = launch_pair<T, V, FEmit>(s, a, pe, m, sorted, n_launch, st, c.fast_args());
       if (rc != PN_OK) return rc;
       if (u->sort_rows) rc = sort_rows(s, u->offsets, n_q, u->neighbors, u->capacity, st);
       return rc;
@@ -431,14 +495,15 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
       const V eps_v = std::numeric_limits<V>::epsilon();
       NBodyParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->G, std::sqrt(eps_v),
                        static_cast<V*>(u->accel)};
-      return launch_pair<T, V, FNBody>(s, a, p, m, sorted, n_launch, st);
+      return launch_pair<T, V, FNBody>(s, a, p, m, sorted, n_launch, st, c.fast_args());
     }
     case PN_F_POTENTIAL: {
       const auto* u = static_cast<const pn_potential_params*>(params);
       if ((const void*)x != (const void*)y) return PN_ERR_INVALID_ARG;
       PotentialParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->cutoff,
                            (V)(1.0 / u->cutoff), static_cast<V*>(u->energy)};
-      return launch_pair<T, V, FPotential>(s, a, p, m, sorted, n_launch, st);
+      return launch_pair<T, V, FPotential>(s, a, p, m, sorted, n_launch, st,
+                                            c.fast_args());
     }
     default:
       return foreach_sph<T, V>(s, functor, n_x, params, c, st);

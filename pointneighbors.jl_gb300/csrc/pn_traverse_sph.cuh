@@ -42,12 +42,12 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
           done = true;
         }
       }
-      if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st);
+      if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st, c.fast_args());
       if (rc != PN_OK || !step) return rc;
       ForceParams<V> pf{p.c, static_cast<const V*>(s->d_pa), static_cast<const V*>(s->d_pb),
                         static_cast<V*>(u->accel)};
-      use_state(s, a, m, pf.pa);
-      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st);
+      use_state(s, a, m, c, pf.pa);
+      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st, c.fast_args());
     }
     case PN_F_WCSPH_FORCE: {
       const auto* u = static_cast<const pn_wcsph_params*>(params);
@@ -69,8 +69,8 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
         }
       }
       ForceParams<V> pf{sph_const<V>(s, u), pa, pb, static_cast<V*>(u->accel)};
-      use_state(s, a, m, pf.pa);
-      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st);
+      use_state(s, a, m, c, pf.pa);
+      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st, c.fast_args());
     }
     case PN_F_ADJOINT_FORWARD:
     case PN_F_ADJOINT_BACKWARD: {
@@ -103,7 +103,9 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
             done = true;
           }
         }
-        if (!done) rc = launch_pair<T, V, FAdjointForward>(s, a, p, m, sorted, n_launch, st);
+        if (!done)
+          rc = launch_pair<T, V, FAdjointForward>(s, a, p, m, sorted, n_launch, st,
+                                                  c.fast_args());
         if (rc != PN_OK) return rc;
         k_sum_partials<V><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
         k_sum_final<<<1, 256, 0, st>>>(s->d_sum_part, SUM_BLOCKS, u->loss); count_launch();
@@ -126,8 +128,9 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
       }
       p.grad = static_cast<V*>(u->grad);
       p.scale = u->grad_scale;
-      use_state(s, a, m, static_cast<const V*>(p.pa));
-      return launch_pair<T, V, FAdjointBackward>(s, a, p, m, sorted, n_launch, st);
+      use_state(s, a, m, c, static_cast<const V*>(p.pa));
+      return launch_pair<T, V, FAdjointBackward>(s, a, p, m, sorted, n_launch, st,
+                                                 c.fast_args());
     }
     default:
       return PN_ERR_UNSUPPORTED_FUNCTOR;
