@@ -171,6 +171,32 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# Float32 operations of one WCSPH force pair evaluation (pos_diff and d2 8, r_min test 1,
+# sqrt and q 3, the kernel's t, t^3 and gradient factor 6, v.x 9, mu 4, viscosity 5, the
+# pair's factor 4, the accumulation 6); an FMA counts as two.
+FORCE_FLOPS_PER_PAIR = 44
+
+
+def fp32_peak(P):
+    """The GPU's Float32 FMA issue peak in TFLOP/s: best of five timed launches of the
+    library's FMA probe (8 independent FMA chains per thread, one wave of 152 x 8 blocks)."""
+    import torch
+    out = torch.empty(P._lib.PN_FMA_PROBE_THREADS, dtype=torch.float32, device="cuda")
+    iters = 16384
+    flops = 2.0 * 8 * iters * P._lib.PN_FMA_PROBE_THREADS
+    st = P._stream()
+    best = 0.0
+    for _ in range(6):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        if P.lib().pn_fma_probe(out.data_ptr(), iters, st) != 0:
+            raise RuntimeError("pn_fma_probe failed")
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, flops / (e0.elapsed_time(e1) / 1e3) / 1e12)
+    return best
+
+
 def hbm_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -406,6 +432,20 @@ def run_gpu(args, rank, world, local):
                          "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
                          "93 % (density), DRAM < 2 % of peak")}
 
+    # the roofline that binds: Float32 issue, for the force sweep's pair arithmetic
+    fp32_tf = fp32_peak(P)
+    force_flops = FORCE_FLOPS_PER_PAIR * pairs_per_sweep
+    fp32_roofline = {"bound": "fp32 issue", "kernel": roofline["kernel"],
+                     "achieved": force_flops / t_force / 1e12, "peak": fp32_tf,
+                     "peak_kind": "measured (pn_fma_probe)", "unit": "TFLOP/s",
+                     "frac": force_flops / t_force / 1e12 / fp32_tf,
+                     "flops_per_pair": FORCE_FLOPS_PER_PAIR,
+                     "note": "pair arithmetic only (no candidate tests: the force sweep walks "
+                             "the pair cache's neighbours); the rest of the issue slots go to "
+                             "addressing, loads and the mask walk" if args.pair_cache > 0 else
+                             "pair arithmetic only; the candidate tests and addressing take "
+                             "the rest of the issue slots"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(x1, v, args, dt)
@@ -434,7 +474,8 @@ def run_gpu(args, rank, world, local):
         "update_ms": statistics.median(upd), "density_ms": statistics.median(den),
         "force_ms": statistics.median(frc), "wall_ms_per_step": 1e3 * wall / K,
         "gpu_launches": int(launches), "launches_per_step": launches / K,
-        "roofline": roofline, "e2e": e2e, "clocks": clocks, "cpu_baseline": cpu,
+        "roofline": roofline, "fp32_roofline": fp32_roofline, "e2e": e2e, "clocks": clocks,
+        "cpu_baseline": cpu,
         "gpu": torch.cuda.get_device_name(),
     }
     if rank == 0:

@@ -420,6 +420,14 @@ int pn_abi_version(void);
 /* Number of CUDA kernels the library has launched in this process (all searches). */
 unsigned long long pn_launch_count(void);
 
+/* Measurement aid (no counterpart in the reference): one launch of a kernel whose every
+ * thread runs `iters` rounds of 8 independent Float32 FMA chains (152 x 8 blocks of 256
+ * threads), writing one value per thread to out[152 * 8 * 256] so nothing is elided.  It
+ * performs 2 * 8 * iters * 311,296 Float32 operations; timing it gives the GPU's Float32
+ * issue peak, the roofline of the traversal's arithmetic. */
+#define PN_FMA_PROBE_THREADS (152 * 8 * 256)
+int pn_fma_probe(float* out, int32_t iters, pn_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -25,6 +25,7 @@ PN_ERR_BOUNDS = 9
 PN_ERR_CAPACITY = 10
 PN_ERR_SCRATCH_LIMIT = 11
 PN_NOALLOC_SCRATCH_BYTES = 4 * 1024 * 1024
+PN_FMA_PROBE_THREADS = 152 * 8 * 256
 
 PN_FLOAT32, PN_FLOAT64 = 0, 1
 PN_FLAG_FLOAT32_SEARCH = 1
@@ -113,6 +114,7 @@ _P = C.c_void_p
 _SIGNATURES = {
     "pn_abi_version": (C.c_int, []),
     "pn_launch_count": (C.c_ulonglong, []),
+    "pn_fma_probe": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),
     "pn_create_spatial_hashing": (C.c_int, [C.POINTER(pn_config), C.c_int64, C.POINTER(_P)]),
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),

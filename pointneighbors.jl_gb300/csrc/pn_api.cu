@@ -265,6 +265,24 @@ static int create(const pn_config* cfg, int64_t list_size, pn_search** out) {
   return PN_OK;
 }
 
+// 8 independent FMA chains per thread (enough to cover the FMA latency with 8 resident
+// blocks of 256 threads per SM); the multipliers stay near 1 so the values stay finite.
+static __global__ void __launch_bounds__(256) k_fma_probe(float* __restrict__ out, int32_t iters) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float v[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) v[c] = 1.0f + 1e-7f * (float)(t + c);
+  const float m = 0.9999999f, a = 1e-8f;
+  for (int32_t i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v[c] = fmaf(v[c], m, a);
+  }
+  float s = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 8; ++c) s += v[c];
+  out[t] = s;
+}
+
 static int record(pn_search* s, int rc, cudaStream_t st) {
   s->last_stream = st;
   if (rc != PN_OK && s->host_error == 0) s->host_error = rc;
@@ -280,6 +298,13 @@ extern "C" {
 int pn_abi_version(void) { return PN_ABI_VERSION; }
 
 unsigned long long pn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+int pn_fma_probe(float* out, int32_t iters, pn_stream_t stream) {
+  if (!out || iters <= 0) return PN_ERR_INVALID_ARG;
+  k_fma_probe<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(out, iters);
+  count_launch();
+  return cuda_status(cudaGetLastError());
+}
 
 int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, 0, out); }
 
