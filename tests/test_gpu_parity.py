@@ -634,3 +634,13 @@ def test_every_update_strategy_gives_the_same_lists(P, O):
         off, nb = P.neighbor_lists(x, x, nhs)
         assert np.array_equal(off.cpu().numpy(), toff), strat
         assert np.array_equal(nb.cpu().numpy(), tnb), strat
+
+
+def test_fma_probe(P):
+    """The measurement aid behind bench.py's Float32 roofline: every thread's value is
+    finite (nothing elided) and a launch takes a plausible time."""
+    out = torch.zeros(P._lib.PN_FMA_PROBE_THREADS, dtype=torch.float32, device="cuda")
+    assert P.lib().pn_fma_probe(out.data_ptr(), 64, P._stream()) == 0
+    torch.cuda.synchronize()
+    assert bool(torch.isfinite(out).all()) and float(out.min()) > 0
+

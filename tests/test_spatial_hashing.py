@@ -262,3 +262,32 @@ def test_precomputed_over_hashing(P, O, list_size):
     cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
     P.foreach_point_neighbor(P.CountNeighbors(cnt), x, x, pre)
     assert np.array_equal(cnt.cpu().numpy(), np.diff(toff))
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_hashing_dense_layout_queries(P, O, periodic):
+    """Queries x not y over the dense layout: inside the occupied box, just outside it (their
+    3^d cells still reach it) and far away (no neighbours, not a BoundsError), and a subset
+    of the points of y."""
+    rng = np.random.default_rng(29)
+    lo, hi = np.array([1.3, -2.0, 0.5]), np.array([13.0, 9.0, 10.2])
+    y = rng.uniform(lo, hi, size=(12000, 3))
+    r = 1.2
+    if periodic:
+        xq = rng.uniform(lo, hi, size=(3000, 3))
+    else:
+        xq = np.concatenate([rng.uniform(lo - 1.5 * r, hi + 1.5 * r, size=(3000, 3)),
+                             rng.uniform(100.0, 120.0, size=(50, 3))])
+    nhs = hashed(P, 3, r, len(y), box=(lo, hi) if periodic else None)
+    yd, xd = dcoords(y), dcoords(xq)
+    P.initialize(nhs, xd, yd)
+    assert nhs.grid_info()["grid_size"][0] > 1  # the dense layout
+    off, nb = P.neighbor_lists(xd, yd, nhs)
+    g = (O.grid_create(3, r, lo, hi, periodic_box=(lo, hi), max_ppc=1000) if periodic
+         else O.grid_create(3, r, lo - 3 * r, hi + 3 * r, max_ppc=1000))
+    toff, tnb = O.trivial_lists(g, xq, y)
+    assert np.array_equal(off.cpu().numpy(), toff) and np.array_equal(nb.cpu().numpy(), tnb)
+    pts = np.arange(0, len(xq), 5)
+    cnt = torch.full((len(xq),), -1, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt), xd, yd, nhs, points=pts)
+    assert np.array_equal(cnt.cpu().numpy()[pts], np.diff(toff)[pts])
