@@ -31,6 +31,8 @@ from . import _lib, build, workloads  # noqa: F401
 lib = _lib.load
 
 __all__ = [
+    "foreach_point_neighbor_unsafe", "foreach_neighbor", "foreach_neighbor_unsafe",
+    "mapreduce_neighbor", "mapreduce_neighbor_unsafe", "initialize_grid", "update_grid",
     "GridNeighborhoodSearch", "FullGridCellList", "SpatialHashingCellList", "spatial_hash",
     "PeriodicBox", "ParallelUpdate", "SemiParallelUpdate", "SerialIncrementalUpdate",
     "SerialUpdate",
@@ -697,6 +699,61 @@ def foreach_point_neighbor(f, x, y, nhs: GridNeighborhoodSearch, *, points=None,
     rc = fn(nhs._h, f.functor, _ptr(x), x.shape[1], _ptr(y), y.shape[1], _ptr(pts),
             0 if pts is None else pts.numel(), C.byref(p), _stream())
     _finish(nhs, rc, check, "foreach_point_neighbor")
+
+
+def foreach_point_neighbor_unsafe(f, x, y, nhs, *, points=None, check=True):
+    """foreach_point_neighbor_unsafe (neighborhood_search.jl:203-234): the reference skips
+    its bounds checks of `points`; the device checks them anyway, so this is
+    foreach_point_neighbor."""
+    return foreach_point_neighbor(f, x, y, nhs, points=points, check=check)
+
+
+def foreach_neighbor(f, system_coords, neighbor_coords, nhs, point, *, check=True):
+    """foreach_neighbor(f, system_coords, neighbor_coords, nhs, point)
+    (neighborhood_search.jl:250-267): the pair function over the neighbours of one point of
+    `system_coords` (0-based here); its outputs are written at that point."""
+    return foreach_point_neighbor(f, system_coords, neighbor_coords, nhs, points=[int(point)],
+                                  check=check)
+
+
+foreach_neighbor_unsafe = foreach_neighbor
+
+
+def mapreduce_neighbor(f, op, system_coords, neighbor_coords, nhs, point, *, init):
+    """mapreduce_neighbor(f, op, system_coords, neighbor_coords, nhs, point; init)
+    (neighborhood_search.jl:360-421) for the reductions the library computes: `f` is
+    "count" (the number of neighbours, self included) or "index" (the 1-based neighbour
+    indices), `op` is `+` (operator.add or "+").  Returns init + the reduction; the empty
+    neighbourhood returns init, like the reference."""
+    import operator
+    if op not in (operator.add, "+"):
+        raise UnsupportedFunctorError("mapreduce_neighbor: only op = + is compiled")
+    torch = _torch()
+    x = _bound(nhs, system_coords, "system_coords")
+    n = x.shape[1]
+    if f == "count":
+        out = torch.zeros(n, dtype=torch.int32, device="cuda")
+        pf = CountNeighbors(out)
+    elif f == "index":
+        out = torch.zeros(n, dtype=torch.int64, device="cuda")
+        pf = NeighborIndexSum(out)
+    else:
+        raise UnsupportedFunctorError("mapreduce_neighbor: f must be \"count\" or \"index\"")
+    foreach_neighbor(pf, system_coords, neighbor_coords, nhs, point)
+    return init + int(out[int(point)])
+
+
+mapreduce_neighbor_unsafe = mapreduce_neighbor
+
+
+def initialize_grid(nhs, y, *, eachindex_y=None, check=True):
+    """initialize_grid!(nhs, y; eachindex_y) (nhs_grid.jl:227-281)."""
+    return initialize(nhs, y, y, eachindex_y=eachindex_y, check=check)
+
+
+def update_grid(nhs, y, *, eachindex_y=None, check=True):
+    """update_grid!(nhs, y; eachindex_y) (nhs_grid.jl:292-477)."""
+    return update(nhs, y, y, eachindex_y=eachindex_y, check=check)
 
 
 def neighbor_lists(x, y, nhs: GridNeighborhoodSearch, *, points=None, sort=True):

@@ -644,3 +644,30 @@ def test_fma_probe(P):
     torch.cuda.synchronize()
     assert bool(torch.isfinite(out).all()) and float(out.min()) > 0
 
+
+
+def test_per_point_api(P, O):
+    """foreach_neighbor / mapreduce_neighbor for one point (neighborhood_search.jl:250-421)
+    and the initialize_grid! / update_grid! spellings, against brute force."""
+    W = P.workloads
+    r = 2.5
+    c = W.reference_test_cloud((12, 13, 11), r, seed=3)
+    mn, mx = c.min(0) - r, c.max(0) + r
+    nhs = make_nhs(P, 3, r, mn, mx, len(c))
+    x = dcoords(c)
+    P.initialize_grid(nhs, x)
+    toff, tnb = O.trivial_lists(O.grid_create(3, r, mn, mx), c, c)
+    for i in (0, 77, len(c) - 1):
+        row = tnb[toff[i]:toff[i + 1]]
+        assert P.mapreduce_neighbor("count", "+", x, x, nhs, i, init=0) == len(row)
+        assert P.mapreduce_neighbor("index", "+", x, x, nhs, i, init=5) == 5 + int((row + 1).sum())
+        cnt = torch.full((len(c),), -7, dtype=torch.int32, device="cuda")
+        P.foreach_neighbor(P.CountNeighbors(cnt), x, x, nhs, i)
+        got = cnt.cpu().numpy()
+        assert got[i] == len(row) and (np.delete(got, i) == -7).all()
+    c2 = c + 0.1
+    x2 = dcoords(c2)
+    P.update_grid(nhs, x2)
+    off, nb = P.neighbor_lists(x2, x2, nhs)
+    toff, tnb = O.trivial_lists(O.grid_create(3, r, mn, mx), c2, c2)
+    assert np.array_equal(off.cpu().numpy(), toff) and np.array_equal(nb.cpu().numpy(), tnb)
