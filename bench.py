@@ -214,8 +214,6 @@ def run_gpu(args, rank, world, local):
     P = __graft_entry__.package()
     W = P.workloads
     torch.cuda.set_device(local)
-    if args.dtype == "mixed":
-        args.pair_cache = 0  # the pair cache is not used with mixed precision
     # coordinates in dt, pair arithmetic and per-point arrays in vdt (Float32 for "mixed")
     dt = np.float32 if args.dtype == "float32" else np.float64
     vdt = np.float64 if args.dtype == "float64" else np.float32

@@ -66,7 +66,7 @@ typedef enum { PN_FLOAT32 = 0, PN_FLOAT64 = 1 } pn_dtype;
  * pos_diff and distance.  Neighbour sets are the reference's exactly; for x is y the pair
  * functions receive pos_diff within about 2^-22 of the reference's Float32 value away from
  * the radius (the exact value near it).  Not taken by pn_count_neighbors_noalloc or
- * pn_batch_create; the pair cache is not used. */
+ * pn_batch_create. */
 #define PN_FLAG_FLOAT32_SEARCH 1
 
 /* nhs_grid.jl:135-192 update strategies available for a FullGridCellList. */

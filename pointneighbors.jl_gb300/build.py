@@ -18,8 +18,9 @@ CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpn_gb300.so")
 SOURCES = ["pn_api.cu", "pn_build.cu", "pn_traverse_f32.cu", "pn_traverse_f64.cu",
-           "pn_traverse_mixed.cu", "pn_traverse_f32_sph.cu", "pn_traverse_f64_sph.cu",
-           "pn_traverse_mixed_sph.cu", "pn_noalloc.cu", "pn_batch.cu", "pn_precomputed.cu"]
+           "pn_traverse_mixed.cu", "pn_traverse_mixed_lists.cu", "pn_traverse_f32_sph.cu",
+           "pn_traverse_f64_sph.cu", "pn_traverse_mixed_sph.cu", "pn_noalloc.cu",
+           "pn_batch.cu", "pn_precomputed.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
               "-Xcompiler", "-fPIC,-ffp-contract=off,-fno-fast-math", "-Xptxas", "-O3"]

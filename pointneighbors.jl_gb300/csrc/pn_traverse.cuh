@@ -845,6 +845,8 @@ struct MixedFast {
   // inline form, with lanes waiting at every candidate another lane accepts, measured the
   // same or slower)
   static constexpr bool kInline = false;
+  // a pair cache (F = WithMask<...>) records only the pairs this wrapper accepts
+  static constexpr bool kRowHook = has_row_hook<F>::value;
   using Params = MixedParams<typename F::Params>;
   struct Acc { typename F::Acc f; float xl[D]; };
   static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
@@ -854,6 +856,14 @@ struct MixedFast {
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<float, D>& q) {
     F::init(a.f, p.f, q);
     load_pos<float, D>(p.m.lo, q.k, a.xl);
+  }
+  static __device__ __forceinline__ void row_begin(Acc& a, const Params& p,
+                                                   const Query<float, D>& q, int ri, int32_t b0,
+                                                   int32_t e0) {
+    if constexpr (kRowHook) F::row_begin(a.f, p.f, q, ri, b0, e0);
+  }
+  static __device__ __forceinline__ void no_rows(Acc& a) {
+    if constexpr (kRowHook) F::no_rows(a.f);
   }
   // The exact Float32(Float64(xi - yj)) from the hi/lo split (q.x holds the query's hi
   // part), in Float64 where the split cannot decide the rounding.

@@ -133,12 +133,19 @@ static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m, cudaStream_t 
   return PN_OK;
 }
 
-// Pair functions that only ever run in the sorted traversal (MixedFast): the other kernels
-// are not instantiated for them.
+// Pair functions that only ever run on the cell-sorted queries (MixedFast): the stencil
+// traversal, the pair cache's walk and its fallback; the other kernels are not instantiated
+// for them.
 template <class F>
 struct sorted_only { static constexpr bool value = false; };
 template <int D, class G>
 struct sorted_only<MixedFast<D, G>> { static constexpr bool value = true; };
+// Pair functions that never walk a pair cache (Mixed, the Float64 traversal of a mixed
+// search's other queries): its walk and fallback kernels are not instantiated for them.
+template <class F>
+struct never_cached { static constexpr bool value = false; };
+template <int D, class G>
+struct never_cached<Mixed<D, G>> { static constexpr bool value = true; };
 
 template <typename T, template <typename, int> class F>
 static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename F<T, 1>::Params& p,
@@ -149,11 +156,16 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
     if constexpr (sorted_only<F<T, DD>>::value) {                                       \
-      k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);        \
+      if (a.pc_mask != nullptr)                                                         \
+        k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
+      else                                                                              \
+        k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);      \
       count_launch();                                                                   \
     } else if (a.pc_mask != nullptr && sorted) {                                        \
-      k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);       \
-      count_launch();                                                                   \
+      if constexpr (!never_cached<F<T, DD>>::value) {                                   \
+        k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
+        count_launch();                                                                 \
+      }                                                                                 \
     } else if (a.nb != nullptr) {                                                       \
       if (sorted)                                                                       \
         k_lists_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
@@ -186,7 +198,7 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
     default: return PN_ERR_INVALID_ARG;
   }
 #undef PN_TRAV_CASE
-  if constexpr (sorted_only<F<T, 1>>::value) {
+  if constexpr (never_cached<F<T, 1>>::value) {
     return cuda_status(cudaGetLastError());
   } else if ((a.nb != nullptr || a.pc_mask != nullptr) && a.nb_fallback && sorted) {
     // queries the pair cache or the lists could not hold: the stencil traversal, for
@@ -420,9 +432,10 @@ static int prepare_call(pn_search* s, const T* x, int64_t n_x, const T* y, int64
   // Sorted mode launches one thread per possible slot; the kernel reads the live count.
   c.n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   c.n_launch = c.sorted ? c.n_sorted : c.n_q;
-  c.cache_on = !kMixed && (!s->hashed || s->hash_dense) && lists == nullptr && c.sorted &&
-               s->pc_cap > 0;
   c.fast = kMixed && c.sorted && lists == nullptr && s->d_pos32 != nullptr && !s->hashed;
+  // the pair cache, on the Float32 traversal for a mixed search
+  c.cache_on = (!kMixed || c.fast) && (!s->hashed || s->hash_dense) && lists == nullptr &&
+               c.sorted && s->pc_cap > 0;
   if (c.fast) {
     c.a32 = mixed_fast_args(s, c.n_q);
     c.m.hi = s->d_pos32;
@@ -433,7 +446,10 @@ static int prepare_call(pn_search* s, const T* x, int64_t n_x, const T* y, int64
       ext = std::max(ext, std::max(std::fabs(s->min_pad[k]), std::fabs(s->max_pad[k])));
     c.m.eb = (float)(std::ldexp(1.0, -44) * (ext + s->radius));
   }
-  if (c.cache_on && s->pc_valid) use_pair_cache(s, c.a);
+  if (c.cache_on && s->pc_valid) {
+    if (c.fast) use_pair_cache(s, c.a32);
+    else use_pair_cache(s, c.a);
+  }
   return PN_OK;
 }
 

@@ -14,7 +14,10 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
   MixedGeom& m = c.m;
   const bool sorted = c.sorted, cache_on = c.cache_on;
   const int64_t n_sorted = c.n_sorted, n_launch = c.n_launch;
-  auto use_cache = [&]() { use_pair_cache(s, a); };
+  auto use_cache = [&]() {
+    if (c.fast) use_pair_cache(s, c.a32);  // a mixed search's Float32 traversal
+    else use_pair_cache(s, a);
+  };
   switch (functor) {
     case PN_F_WCSPH_DENSITY:
     case PN_F_WCSPH_STEP: {
@@ -30,17 +33,23 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
       }
       int rc = PN_OK;
       bool done = false;
-      if constexpr (!kMixed) {
-        if (cache_on && !s->pc_valid) {
-          MaskPairParams<DensityParams<T>> pp{p, {}};
-          rc = pc_prepare(s, n_sorted, &pp.m, st);
-          if (rc == PN_OK) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
-          if (rc == PN_OK) {
-            s->pc_valid = true;
-            use_cache();
+      if (cache_on && !s->pc_valid) {
+        MaskPairParams<DensityParams<V>> pp{p, {}};
+        rc = pc_prepare(s, n_sorted, &pp.m, st);
+        if (rc == PN_OK) {
+          if constexpr (kMixed) {
+            const MixedParams<MaskPairParams<DensityParams<V>>> mp{pp, m};
+            rc = launch_trav<float, MixedFastOf<FDensityMask>::template type>(
+                s, c.a32, mp, sorted, n_launch, st);
+          } else {
+            rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
           }
-          done = true;
         }
+        if (rc == PN_OK) {
+          s->pc_valid = true;
+          use_cache();
+        }
+        done = true;
       }
       if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st, c.fast_args());
       if (rc != PN_OK || !step) return rc;
@@ -93,15 +102,20 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
         p.density = static_cast<V*>(u->density);
         p.terms = static_cast<V*>(u->terms);
         bool done = false;
-        if constexpr (!kMixed) {
-          if (cache_on && !s->pc_valid) {
-            MaskPairParams<AdjointParams<T>> pp{p, {}};
-            rc = pc_prepare(s, n_sorted, &pp.m, st);
-            if (rc == PN_OK)
+        if (cache_on && !s->pc_valid) {
+          MaskPairParams<AdjointParams<V>> pp{p, {}};
+          rc = pc_prepare(s, n_sorted, &pp.m, st);
+          if (rc == PN_OK) {
+            if constexpr (kMixed) {
+              const MixedParams<MaskPairParams<AdjointParams<V>>> mp{pp, m};
+              rc = launch_trav<float, MixedFastOf<FAdjointForwardMask>::template type>(
+                  s, c.a32, mp, sorted, n_launch, st);
+            } else {
               rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
-            if (rc == PN_OK) s->pc_valid = true;
-            done = true;
+            }
           }
+          if (rc == PN_OK) s->pc_valid = true;
+          done = true;
         }
         if (!done)
           rc = launch_pair<T, V, FAdjointForward>(s, a, p, m, sorted, n_launch, st,

@@ -216,3 +216,49 @@ def test_golden_gpu_tutorial_mixed(P, golden):
     n = torch.zeros(len(pts), dtype=torch.int32, device="cuda")
     P.foreach_point_neighbor(P.CountNeighbors(n), x, x, nhs)
     assert (int(n.min()), int(n.max())) == tuple(c["expected_extrema"])
+
+
+@pytest.mark.parametrize("periodic", [False, True])
+def test_mixed_pair_cache(P, O, periodic):
+    """The pair cache over a mixed search's Float32 traversal: the density sweep records
+    the pairs the exact Float32 test accepts, the force walks them; density bit-identical
+    to the search without the cache, force within the FP32 bar of the FP64 oracle."""
+    W = P.workloads
+    x, v, _ = W.wcsph_cloud(20, seed=13, dtype=np.float64)
+    n = len(x)
+    r = np.float32(3.0)
+    lo, hi = (np.zeros(3), np.full(3, 20.0)) if periodic else (np.full(3, -1.0), np.full(3, 21.0))
+    if periodic:
+        x = np.mod(x, 20.0)
+    xd = dcoords(x)
+    vd = torch.as_tensor(v.astype(np.float32), device="cuda").reshape(-1)
+    out = []
+    for cache in (False, True):
+        box = P.PeriodicBox(min_corner=lo.astype(np.float32),
+                            max_corner=hi.astype(np.float32)) if periodic else None
+        cl = P.FullGridCellList(min_corner=lo, max_corner=hi, search_radius=r,
+                                max_points_per_cell=0)
+        nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
+                                       periodic_box=box, pair_cache=cache)
+        assert nhs.mixed
+        P.initialize(nhs, xd, xd)
+        rho = torch.zeros(n, device="cuda")
+        prs = torch.zeros(n, device="cuda")
+        acc = torch.zeros(3 * n, device="cuda")
+        for _ in range(2):  # the second step walks the cache
+            P.foreach_point_neighbor(P.WCSPHStep(density=rho, pressure=prs, velocity=vd,
+                                                 accel=acc, **W.WCSPH), xd, xd, nhs)
+        out.append((rho.clone(), prs.clone(), acc.clone()))
+    assert torch.equal(out[0][0], out[1][0]) and torch.equal(out[0][1], out[1][1])
+    g = (O.grid_create_mixed(3, r, lo, hi, periodic_box=(lo, hi)) if periodic
+         else O.grid_create_mixed(3, r, lo, hi))
+    cl_o = O.build(g, x)
+    c = W.WCSPH
+    prm, keep = O.make_params(rho=out[1][0].cpu().numpy().astype(np.float64),
+                              pressure=out[1][1].cpu().numpy().astype(np.float64),
+                              vel=v.astype(np.float32).astype(np.float64),
+                              r_min=float(np.sqrt(np.finfo(np.float32).eps)) * c["h"], **c)
+    oacc, oabs = O.foreach(g, cl_o, x, x, O.F_WCSPH_FORCE, prm, want_abs=True)
+    for k in (0, 1):
+        got = out[k][2].cpu().numpy().astype(np.float64).reshape(n, 3)
+        assert _rel_err(got, oacc, oabs) < TOL_F32
