@@ -430,10 +430,12 @@ def run_gpu(args, rank, world, local):
                          "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
                          "93 % (density), DRAM < 2 % of peak")}
 
-    # the roofline that binds: Float32 issue, for the force sweep's pair arithmetic
+    # the roofline that binds: Float32 issue, for the force sweep's pair arithmetic (the
+    # Float64 variant's pair arithmetic runs on the Float64 units: not reported)
     fp32_tf = fp32_peak(P)
     force_flops = FORCE_FLOPS_PER_PAIR * pairs_per_sweep
-    fp32_roofline = {"bound": "fp32 issue", "kernel": roofline["kernel"],
+    fp32_roofline = None if args.dtype == "float64" else {
+                     "bound": "fp32 issue", "kernel": roofline["kernel"],
                      "achieved": force_flops / t_force / 1e12, "peak": fp32_tf,
                      "peak_kind": "measured (pn_fma_probe)", "unit": "TFLOP/s",
                      "frac": force_flops / t_force / 1e12 / fp32_tf,
