@@ -345,29 +345,45 @@ def run_gpu(args, rank, world, local):
         for e in ev_done + ev_out:
             e.record(comp)
 
+        # per timed step: copy-in, compute and copy-out durations (events on their streams)
+        tev = [[torch.cuda.Event(enable_timing=True) for _ in range(6)] for _ in range(K)]
+        timing = [False]
+
         def h2d(k, xh):
             bi = k % 2
             with torch.cuda.stream(s_in):
                 s_in.wait_event(ev_done[bi])  # step k-2 no longer reads buffer bi
+                if timing[0]:
+                    tev[k][0].record(s_in)
                 xb[bi].copy_(xh, non_blocking=True)
                 vb[bi].copy_(v_h, non_blocking=True)
+                if timing[0]:
+                    tev[k][1].record(s_in)
                 ev_in[bi].record(s_in)
 
         def compute(k):
             bi = k % 2
             comp.wait_event(ev_in[bi])
             comp.wait_event(ev_out[bi])  # step k-2's outputs have left
+            if timing[0]:
+                tev[k][2].record(comp)
             P.update(nhs, xbT[bi], xbT[bi], check=False)
             P.foreach_point_neighbor(dens_b[bi], xbT[bi], xbT[bi], nhs, check=False)
             P.foreach_point_neighbor(force_b[bi], xbT[bi], xbT[bi], nhs, check=False)
+            if timing[0]:
+                tev[k][3].record(comp)
             ev_done[bi].record(comp)
 
         def d2h(k):
             bi = k % 2
             with torch.cuda.stream(s_out):
                 s_out.wait_event(ev_done[bi])
+                if timing[0]:
+                    tev[k][4].record(s_out)
                 rho_h[bi].copy_(rb[bi], non_blocking=True)
                 acc_h[bi].copy_(ab[bi], non_blocking=True)
+                if timing[0]:
+                    tev[k][5].record(s_out)
                 ev_out[bi].record(s_out)
 
         def run(steps, src):
@@ -383,12 +399,16 @@ def run_gpu(args, rank, world, local):
         torch.cuda.synchronize()
         barrier(world)
         a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e2e_sampler = ClockSampler(torch.cuda.current_device()) if rank == 0 else None
+        timing[0] = True
         a0.record(comp)
         s_in.wait_event(a0)
         run(K, lambda k: walk_h[k])
         a1.record(comp)
         torch.cuda.synchronize()
         barrier(world)
+        timing[0] = False
+        e2e_clocks = e2e_sampler.stop() if e2e_sampler else None
         e2e_s, e2e_pairs = aggregate(a0.elapsed_time(a1) / 1e3, 2.0 * pairs_timed, world,
                                      device=torch.device("cuda"))
         if P.lib().pn_sync(nhs.handle) != 0:
@@ -401,6 +421,11 @@ def run_gpu(args, rank, world, local):
                "h2d_bytes_per_step": 3 * n * cb + 3 * n * vb_,
                "d2h_bytes_per_step": 4 * n * vb_, "ms_per_step": 1e3 * e2e_s / K,
                "outputs_equal_device_run": same,
+               "h2d_ms": statistics.median(tev[k][0].elapsed_time(tev[k][1]) for k in range(K)),
+               "compute_ms": statistics.median(tev[k][2].elapsed_time(tev[k][3])
+                                               for k in range(K)),
+               "d2h_ms": statistics.median(tev[k][4].elapsed_time(tev[k][5]) for k in range(K)),
+               "clocks": e2e_clocks,
                "path": "pinned host -> cudaMemcpyAsync (copy stream, double-buffered) -> "
                        "pn_update + pn_foreach_point_neighbor (density, force) -> "
                        "cudaMemcpyAsync (second copy stream) -> pinned host density and "
