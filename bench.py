@@ -425,6 +425,8 @@ def run_gpu(args, rank, world, local):
                "compute_ms": statistics.median(tev[k][2].elapsed_time(tev[k][3])
                                                for k in range(K)),
                "d2h_ms": statistics.median(tev[k][4].elapsed_time(tev[k][5]) for k in range(K)),
+               "h2d_ms_max": max(tev[k][0].elapsed_time(tev[k][1]) for k in range(K)),
+               "compute_ms_max": max(tev[k][2].elapsed_time(tev[k][3]) for k in range(K)),
                "clocks": e2e_clocks,
                "path": "pinned host -> cudaMemcpyAsync (copy stream, double-buffered) -> "
                        "pn_update + pn_foreach_point_neighbor (density, force) -> "
