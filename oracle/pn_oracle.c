@@ -1,8 +1,8 @@
 /*
  * pn_oracle.c -- CPU restatement of PointNeighbors.jl's GridNeighborhoodSearch +
  * FullGridCellList (ParallelUpdate), TrivialNeighborhoodSearch and the benchmark pair
- * functions.  TEST INFRASTRUCTURE ONLY: the checker for the CUDA library, never part of
- * the product path.  Build: oracle/build_oracle.py (gcc -O2 -fopenmp -ffp-contract=off).
+ * functions.  TEST INFRASTRUCTURE ONLY: what the CUDA library is compared with, never
+ * part of the product path.  Build: oracle/build_oracle.py (gcc -O2 -fopenmp -ffp-contract=off).
  *
  * Reference files followed (paths inside PointNeighbors.jl v0.6.7):
  *   src/util.jl:2-34                      extract_svector, floor_to_int

@@ -4,8 +4,8 @@
  * benchmarks.
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product path links or calls this code: it is
- * the checker that the CUDA path is compared against (tests/, __graft_entry__.smoke(),
- * and bench.py's CPU-baseline leg).
+ * what the CUDA path is compared against (tests/, __graft_entry__.smoke(), and bench.py's
+ * CPU-baseline leg).
  *
  * Parity pin: the reference (Julia) cannot run in this environment, so this restatement
  * is pinned against the known-answer vectors that the reference's own test suite holds

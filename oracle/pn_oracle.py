@@ -1,8 +1,8 @@
 """ctypes wrapper around the CPU oracle (oracle/pn_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() and by the
-CPU-baseline leg of bench.py, always as the checker or the timed CPU restatement, never
-as part of the product path.
+CPU-baseline leg of bench.py, always as the answer the CUDA path is compared with or the
+timed CPU restatement, never as part of the product path.
 
 Arrays of points use the reference's memory layout: a Julia `T[d, N]` column-major
 matrix is a C-contiguous numpy array of shape (N, d) here.  Point indices are 0-based.

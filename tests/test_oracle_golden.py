@@ -1,8 +1,8 @@
 """Pin the CPU oracle against the known answers of the reference's own test suite.
 
 The reference (Julia) cannot run here, so these vectors -- transcribed from its tests in
-tests/golden/make_golden.py -- are what makes the oracle trustworthy as the checker for
-the CUDA path.  CPU only.
+tests/golden/make_golden.py -- are what makes the oracle trustworthy as the answer the
+CUDA path is compared with.  CPU only.
 """
 import numpy as np
 import pytest
