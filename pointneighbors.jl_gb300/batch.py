@@ -16,8 +16,8 @@ import ctypes as C
 import numpy as np
 
 from . import (ArgumentError, CountNeighbors, GridNeighborhoodSearch, PairFunction,
-               WCSPHDensity, WCSPHForce, WCSPHStep, _coords, _finish, _lib, _out, _raise,
-               _stream, _tdtype, lib)
+               WCSPHDensity, WCSPHForce, WCSPHStep, _coords, _lib, _out, _raise, _stream,
+               _tdtype, lib)
 
 
 def _batch_params(f: PairFunction, nhs_list, x, n_total):
