@@ -270,6 +270,19 @@ def test_spatial_hashing_collisions(O, golden):
             assert rows == case["neighbors"]
 
 
+def test_host_spatial_hash_equals_oracle(O, pkg):
+    """The host API's spatial_hash (the list a user sees through export_cells/eachneighbor)
+    equals the oracle's restatement of spatial_hashing.jl:142-156, for negative and large
+    cells (the Int64 products and xor wrap) and list sizes from 1 to above 2^31."""
+    rng = np.random.default_rng(11)
+    for d in (1, 2, 3):
+        for _ in range(300):
+            scale = int(rng.choice([4, 1000, 2**20, 2**31 - 2]))
+            cell = [int(v) for v in rng.integers(-scale, scale, d)]
+            ls = int(rng.choice([1, 7, 1000, 2**20 + 3, 2**31 + 5]))
+            assert pkg.spatial_hash(cell, ls) == O.spatial_hash(cell, ls), (cell, ls)
+
+
 def test_coordinates_flattened(O, golden):
     c = golden["coordinates_flattened"]
     for v in c["values"]:
