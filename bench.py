@@ -11,7 +11,9 @@ N(0, 0.1^2).  A step is the hot path once over the whole cloud:
 pair-evals/s = 2 sweeps x (ordered pairs with d^2 <= r^2, self included) per step / time.
 `value` is device time with the inputs resident in HBM; `e2e` is the same step through the
 C ABI with the coordinates and velocities copied from pinned host memory and the density
-and acceleration copied back inside the timed region.
+and acceleration copied back inside the timed region (double-buffered on two copy streams;
+`e2e.h2d_ms`, `compute_ms` and `d2h_ms` are each phase's median duration per step, measured
+with events on its own stream, and `*_max` the slowest step's).
 
 `--impl reference` times the CPU restatement of the reference's algorithm (the oracle:
 threaded cell-list build + per-point traversal, pair math in FP64) on the host cores, on a
