@@ -428,6 +428,14 @@ unsigned long long pn_launch_count(void);
 #define PN_FMA_PROBE_THREADS (152 * 8 * 256)
 int pn_fma_probe(float* out, int32_t iters, pn_stream_t stream);
 
+/* Self-test of the device-side wait bound (no counterpart in the reference).  The one
+ * device-side wait of the library is the cell-list scan's look-back on its predecessor
+ * tiles, bounded by an iteration limit after which it records PN_ERR_TIMEOUT and returns.
+ * This runs that scan on a small private array whose first tile never publishes, so the
+ * wait must give up (after about a second), and returns the status the scan recorded:
+ * PN_ERR_TIMEOUT when the bound works.  Synchronous on `stream`; the context stays usable. */
+int pn_selftest_bounded_wait(pn_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

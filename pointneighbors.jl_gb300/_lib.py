@@ -115,6 +115,7 @@ _SIGNATURES = {
     "pn_abi_version": (C.c_int, []),
     "pn_launch_count": (C.c_ulonglong, []),
     "pn_fma_probe": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
+    "pn_selftest_bounded_wait": (C.c_int, [C.c_void_p]),
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),
     "pn_create_spatial_hashing": (C.c_int, [C.POINTER(pn_config), C.c_int64, C.POINTER(_P)]),
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),

@@ -306,6 +306,10 @@ int pn_fma_probe(float* out, int32_t iters, pn_stream_t stream) {
   return cuda_status(cudaGetLastError());
 }
 
+int pn_selftest_bounded_wait(pn_stream_t stream) {
+  return selftest_bounded_wait((cudaStream_t)stream);
+}
+
 int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, 0, out); }
 
 int pn_create_spatial_hashing(const pn_config* cfg, int64_t list_size, pn_search** out) {

@@ -849,6 +849,44 @@ void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long
 
 int32_t scan_tile_count(int64_t n) { return div_up(n, SCAN_TILE); }
 
+// The scan's bounded look-back with a predecessor that never publishes: the tile counter
+// starts at 1, so the one block launched takes tile 1 of 2 and waits for tile 0 until its
+// iteration limit, then records PN_ERR_TIMEOUT.  Every access stays inside the private
+// arrays (counts and start of 2 tiles, state of 2 tiles + the counter).
+int selftest_bounded_wait(cudaStream_t st) {
+  const int32_t n = 2 * SCAN_TILE;
+  int32_t* counts = nullptr;
+  int32_t* start = nullptr;
+  int32_t* err = nullptr;
+  unsigned long long* state = nullptr;
+  cudaError_t e = cudaMalloc(&counts, sizeof(int32_t) * n);
+  if (e == cudaSuccess) e = cudaMalloc(&start, sizeof(int32_t) * (n + 1));
+  if (e == cudaSuccess) e = cudaMalloc(&err, sizeof(int32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&state, sizeof(unsigned long long) * 3);
+  int32_t status = -1;
+  if (e == cudaSuccess) {
+    const unsigned long long first_tile = 1;
+    cudaMemsetAsync(counts, 0, sizeof(int32_t) * n, st);
+    cudaMemsetAsync(err, 0, sizeof(int32_t), st);
+    cudaMemsetAsync(state, 0, sizeof(unsigned long long) * 3, st);
+    e = cudaMemcpyAsync(state + 2, &first_tile, sizeof first_tile, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) {
+      k_scan_cells<<<1, SCAN_THREADS, 0, st>>>(counts, n, start, state, 2, 0, nullptr, err,
+                                               nullptr, 0);
+      count_launch();
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(&status, err, sizeof status, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  }
+  cudaFree(state);
+  cudaFree(err);
+  cudaFree(start);
+  cudaFree(counts);
+  return e == cudaSuccess ? status : cuda_status(e);
+}
+
 void scatter_slots(const int32_t* cell_of, const int32_t* slot_of, int32_t m,
                    const int32_t* start, int32_t* tmp_perm, int32_t* cell_of_slot,
                    cudaStream_t st) {

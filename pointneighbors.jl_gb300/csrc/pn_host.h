@@ -151,6 +151,7 @@ int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_
 void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long long* state,
                  int32_t tiles, int32_t* err, cudaStream_t st);
 int32_t scan_tile_count(int64_t n);
+int selftest_bounded_wait(cudaStream_t st);
 void scatter_slots(const int32_t* cell_of, const int32_t* slot_of, int32_t m,
                    const int32_t* start, int32_t* tmp_perm, int32_t* cell_of_slot,
                    cudaStream_t st);

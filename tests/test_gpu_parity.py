@@ -645,6 +645,22 @@ def test_fma_probe(P):
     assert bool(torch.isfinite(out).all()) and float(out.min()) > 0
 
 
+def test_bounded_wait_gives_up(P):
+    """The library's one device-side wait (the cell-list scan's look-back) is bounded: with
+    a predecessor tile that never publishes, the scan records PN_ERR_TIMEOUT and returns
+    (after about a second), and the context stays usable for the next search."""
+    import time
+    t0 = time.perf_counter()
+    assert P.lib().pn_selftest_bounded_wait(P._stream()) == P._lib.PN_ERR_TIMEOUT
+    assert time.perf_counter() - t0 < 60
+    pts = np.array([[0.0, 0.0], [1.0, 0.0], [5.0, 5.0]])
+    nhs = make_nhs(P, 2, 1.5, [-2.0, -2.0], [7.0, 7.0], 3)
+    x = dcoords(pts)
+    P.initialize(nhs, x, x)
+    cnt = torch.zeros(3, dtype=torch.int32, device="cuda")
+    P.foreach_point_neighbor(P.CountNeighbors(cnt), x, x, nhs)
+    assert cnt.tolist() == [2, 2, 1]
+
 
 def test_per_point_api(P, O):
     """foreach_neighbor / mapreduce_neighbor for one point (neighborhood_search.jl:250-421)
