@@ -208,6 +208,17 @@ typedef struct {
  * integer-like radius is not representable here; periodic boxes with < 3 cells. */
 int pn_create(const pn_config* cfg, pn_search** out);
 
+/* The same search from a FullGridCellList's own state, for a binding that holds a search
+ * the reference's constructors built (full_grid.jl:30-35,66-79): cfg->min_corner and
+ * max_corner are the corners the cell list stores (`cell_list.min_corner`, `max_corner`,
+ * already padded by 1001//1000 * search_radius), grid_size[k] = size(cell_list.linear_indices,
+ * k) for k < ndims (all zero for a template), and cfg->max_points_per_cell =
+ * size(cell_list.cells.backend, 1), the DynamicVectorOfVectors capacity
+ * (vector_of_vectors.jl:3-31).  The stored values are taken as they are, so the cells equal
+ * the reference's bit for bit; subtracting the padding from the stored corners and padding
+ * again does not round-trip in floating point.  Everything else as pn_create. */
+int pn_create_from_grid(const pn_config* cfg, const int64_t* grid_size, pn_search** out);
+
 /* GridNeighborhoodSearch{NDIMS}(; search_radius, n_points, periodic_box,
  *   cell_list = SpatialHashingCellList{NDIMS}(; list_size, max_points_per_cell))
  * (spatial_hashing.jl:79-89, nhs_grid.jl:77-129): an unbounded domain whose cells
@@ -222,8 +233,10 @@ int pn_create(const pn_config* cfg, pn_search** out);
 int pn_create_spatial_hashing(const pn_config* cfg, int64_t list_size, pn_search** out);
 
 /* copy_neighborhood_search(nhs, search_radius, n_points) (nhs_grid.jl:640-649,
- * full_grid.jl:179-185, spatial_hashing.jl:133-141): same corners or list size, periodic
- * box, strategy and cell capacity. */
+ * full_grid.jl:179-185, spatial_hashing.jl:133-141): same list size, periodic box, strategy
+ * and cell capacity; a FullGridCellList's stored corners (unpadded for a template, whose
+ * radius is zero) are the new cell list's corners, padded by the new radius, like
+ * copy_cell_list passes them to the constructor. */
 int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
                    pn_search** out);
 
@@ -290,6 +303,9 @@ int pn_get_grid_info(const pn_search* s, pn_grid_info* out);
 /* The geometry pn_create would compute for `cfg` (FullGridCellList padding and cell
  * counts, periodic n_cells and cell_size), on the host only: no device is touched. */
 int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out);
+/* The same for pn_create_from_grid's arguments. */
+int pn_compute_geometry_from_grid(const pn_config* cfg, const int64_t* grid_size,
+                                  pn_grid_info* out);
 
 /* cell_coords(x, nhs) (nhs_grid.jl:622-638, util.jl:19-34) for n points:
  * out int64[n * ndims], the reference's 1-based (periodic) cell coordinates. */

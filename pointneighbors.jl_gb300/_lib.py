@@ -117,6 +117,7 @@ _SIGNATURES = {
     "pn_fma_probe": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "pn_selftest_bounded_wait": (C.c_int, [C.c_void_p]),
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),
+    "pn_create_from_grid": (C.c_int, [C.POINTER(pn_config), C.POINTER(C.c_int64), C.POINTER(_P)]),
     "pn_create_spatial_hashing": (C.c_int, [C.POINTER(pn_config), C.c_int64, C.POINTER(_P)]),
     "pn_copy_search": (C.c_int, [_P, C.c_double, C.c_int64, C.POINTER(_P)]),
     "pn_destroy": (C.c_int, [_P]),
@@ -132,6 +133,8 @@ _SIGNATURES = {
     "pn_requires_update": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "pn_get_grid_info": (C.c_int, [_P, C.POINTER(pn_grid_info)]),
     "pn_compute_geometry": (C.c_int, [C.POINTER(pn_config), C.POINTER(pn_grid_info)]),
+    "pn_compute_geometry_from_grid": (C.c_int, [C.POINTER(pn_config), C.POINTER(C.c_int64),
+                                                C.POINTER(pn_grid_info)]),
     "pn_cell_coords": (C.c_int, [_P, _P, C.c_int64, _P, _P]),
     "pn_export_cells": (C.c_int, [_P, _P, _P, _P]),
     "pn_count_neighbors_noalloc": (C.c_int, [C.POINTER(pn_config), _P, C.c_int64, _P, _P]),

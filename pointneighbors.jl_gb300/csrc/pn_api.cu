@@ -128,11 +128,23 @@ static int geometry(pn_search* s) {
   }
   for (int k = 0; k < d; ++k) {
     const T mn = (T)c.min_corner[k], mx = (T)c.max_corner[k];
-    const T mnp = (T)(mn - (T)pad), mxp = (T)(mx + (T)pad);
+    // from a cell list's stored state: the corners are padded already
+    const T mnp = s->from_grid ? mn : (T)(mn - (T)pad);
+    const T mxp = s->from_grid ? mx : (T)(mx + (T)pad);
     s->min_pad[k] = (double)mnp;
     s->max_pad[k] = (double)mxp;
     s->cell_size[k] = (double)r;
-    if (!s->is_template) {
+    if (s->from_grid) {
+      // size(linear_indices): zero for a template, else at least one cell
+      const int64_t gk = s->given_grid[k];
+      if (s->is_template ? gk != 0 : (gk < 1 || gk > (int64_t)INT32_MAX - 1))
+        return PN_ERR_INVALID_ARG;
+      if (!s->is_template) {
+        s->grid_size[k] = gk;
+        total *= gk;
+        if (total > (int64_t)INT32_MAX - 1) return PN_ERR_INVALID_ARG;
+      }
+    } else if (!s->is_template) {
       const T q = (T)((T)(mxp - mnp) / (T)r);
       if (!(q >= (T)1) || !(q < (T)2147483647.0)) return PN_ERR_INVALID_ARG;
       s->grid_size[k] = (int64_t)std::ceil((double)q);
@@ -212,8 +224,11 @@ static int geometry_for(pn_search* s) {
   return s->dtype == PN_FLOAT64 ? geometry<double, double>(s) : geometry<float, float>(s);
 }
 
-// list_size > 0: a SpatialHashingCellList with that many lists, else a FullGridCellList.
-static int create(const pn_config* cfg, int64_t list_size, pn_search** out) {
+// list_size > 0: a SpatialHashingCellList with that many lists, else a FullGridCellList;
+// grid (FullGridCellList only): the cell list's own state (padded corners in cfg, cells per
+// dimension here) instead of the constructor's arguments.
+static int create(const pn_config* cfg, int64_t list_size, pn_search** out,
+                  const int64_t* grid = nullptr) {
   if (!cfg || !out) return PN_ERR_INVALID_ARG;
   *out = nullptr;
   if (cfg->ndims < 1 || cfg->ndims > 3) return PN_ERR_INVALID_ARG;
@@ -230,6 +245,10 @@ static int create(const pn_config* cfg, int64_t list_size, pn_search** out) {
   s->dtype = cfg->dtype;
   s->hashed = list_size > 0 ? 1 : 0;
   s->list_size = list_size > 0 ? list_size : 0;
+  if (grid != nullptr) {
+    s->from_grid = 1;
+    for (int k = 0; k < 3; ++k) s->given_grid[k] = k < cfg->ndims ? grid[k] : 0;
+  }
   int rc = geometry_for(s);
   if (rc != PN_OK) {
     delete s;
@@ -317,12 +336,26 @@ int pn_create_spatial_hashing(const pn_config* cfg, int64_t list_size, pn_search
   return create(cfg, list_size, out);
 }
 
+int pn_create_from_grid(const pn_config* cfg, const int64_t* grid_size, pn_search** out) {
+  if (!grid_size) return PN_ERR_INVALID_ARG;
+  return create(cfg, 0, out, grid_size);
+}
+
 int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
                    pn_search** out) {
   if (!tmpl) return PN_ERR_INVALID_ARG;
   pn_config c = tmpl->cfg;
   c.search_radius = search_radius;
   c.n_points = n_points;
+  // copy_cell_list (full_grid.jl:179-185) hands the template's stored corners -- padded by
+  // the template's radius, i.e. not at all for a template -- to the constructor, which pads
+  // them by the new radius
+  if (!tmpl->hashed) {
+    for (int k = 0; k < tmpl->ndims; ++k) {
+      c.min_corner[k] = tmpl->min_pad[k];
+      c.max_corner[k] = tmpl->max_pad[k];
+    }
+  }
   const int rc = create(&c, tmpl->list_size, out);
   if (rc == PN_OK) (*out)->rebuild_fraction = tmpl->rebuild_fraction;
   return rc;
@@ -495,7 +528,7 @@ int pn_get_grid_info(const pn_search* s, pn_grid_info* out) {
   return PN_OK;
 }
 
-int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out) {
+static int compute_geometry(const pn_config* cfg, const int64_t* grid, pn_grid_info* out) {
   if (!cfg || !out || cfg->ndims < 1 || cfg->ndims > 3) return PN_ERR_INVALID_ARG;
   if (cfg->dtype != PN_FLOAT32 && cfg->dtype != PN_FLOAT64) return PN_ERR_INVALID_ARG;
   pn_search tmp;
@@ -504,9 +537,23 @@ int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out) {
   tmp.dtype = cfg->dtype;
   tmp.hashed = 0;
   tmp.list_size = 0;
+  if (grid != nullptr) {
+    tmp.from_grid = 1;
+    for (int k = 0; k < 3; ++k) tmp.given_grid[k] = k < cfg->ndims ? grid[k] : 0;
+  }
   int rc = geometry_for(&tmp);
   if (rc != PN_OK) return rc;
   return pn_get_grid_info(&tmp, out);
+}
+
+int pn_compute_geometry(const pn_config* cfg, pn_grid_info* out) {
+  return compute_geometry(cfg, nullptr, out);
+}
+
+int pn_compute_geometry_from_grid(const pn_config* cfg, const int64_t* grid_size,
+                                  pn_grid_info* out) {
+  if (!grid_size) return PN_ERR_INVALID_ARG;
+  return compute_geometry(cfg, grid_size, out);
 }
 
 int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stream_t stream) {

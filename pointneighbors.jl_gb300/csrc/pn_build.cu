@@ -86,11 +86,14 @@ k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* _
 // Exclusive scan of counts[0..n) into start[0..n], start[n] = total.  Tiles are taken in
 // launch order from a counter, so a tile only ever waits for tiles that are already
 // running; every wait is bounded and reports PN_ERR_TIMEOUT if it gives up.
+// stats (or null): stats[0] = the largest count (atomicMax, cleared by the caller),
+// stats[1] = 1 when some count exceeds max_ppc (the build then skips the in-cell sort).
 __global__ void __launch_bounds__(SCAN_THREADS)
 k_scan_cells(const int32_t* __restrict__ counts, int32_t n, int32_t* __restrict__ start,
              unsigned long long* __restrict__ state, int32_t n_tiles, int32_t max_ppc,
              const int32_t* __restrict__ base_ptr, int32_t* __restrict__ err,
-             const int32_t* __restrict__ gate, int32_t gate_want) {
+             const int32_t* __restrict__ gate, int32_t gate_want,
+             int32_t* __restrict__ stats = nullptr) {
   if (gate && *gate != gate_want) return;  // the same word for every block
   __shared__ int s_tile, s_prefix;
   __shared__ int s_warp[SCAN_THREADS / 32];
@@ -115,7 +118,14 @@ k_scan_cells(const int32_t* __restrict__ counts, int32_t n, int32_t* __restrict_
     sum += v[i];
     mx = max(mx, v[i]);
   }
-  if (max_ppc > 0 && mx > max_ppc) set_error(err, PN_ERR_CELL_FULL);
+  if (max_ppc > 0 && mx > max_ppc) {
+    set_error(err, PN_ERR_CELL_FULL);
+    if (stats) stats[1] = 1;
+  }
+  if (stats) {
+    const int wmx = __reduce_max_sync(0xffffffffu, mx);
+    if (lane == 0 && wmx > 0) atomicMax(&stats[0], wmx);
+  }
   int incl = sum;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -199,23 +209,37 @@ __device__ __forceinline__ void store_pos(T* pos, int64_t k, const T* v) {
   for (int c = 0; c < S; ++c) pos[k * S + c] = c < D ? v[c] : (T)0;
 }
 
+// Cells with more points than this are ranked by k_finalize_large (their keys streamed
+// through shared memory) instead of one thread per slot reading the whole cell.
+constexpr int32_t LARGE_CELL = 256;
+constexpr int LARGE_TILE = 1024;
+
+// stats (see k_scan_cells) or null: with stats, cells above LARGE_CELL are left to
+// k_finalize_large, and after a failed max_points_per_cell check every slot keeps its
+// scatter position (no sort: the build has failed, but the arrays hold valid indices).
 template <typename T, int D>
 __device__ __forceinline__ void finalize_slot(const int32_t* __restrict__ tmp_perm,
                                               const int32_t* __restrict__ cell_of_slot,
                                               const int32_t* __restrict__ start, int64_t k,
                                               const T* __restrict__ y, int32_t* __restrict__ perm,
-                                              T* __restrict__ pos) {
+                                              T* __restrict__ pos,
+                                              const int32_t* __restrict__ stats = nullptr) {
   const int32_t c = cell_of_slot[k];
   const int32_t s = start[c], e = start[c + 1];
   const int32_t v = tmp_perm[k];
+  const bool failed = stats != nullptr && stats[1] != 0;
+  if (stats != nullptr && !failed && e - s > LARGE_CELL) return;
   // inside the cell: ascending first coordinate, ties by point index (a total order, so
   // the layout is deterministic); a stencil row's three cells are then one x-sorted run
   const T xv = y[(int64_t)v * D];
-  int32_t rank = 0;
-  for (int32_t q = s; q < e; ++q) {
-    const int32_t u = __ldg(&tmp_perm[q]);
-    const T xu = __ldg(&y[(int64_t)u * D]);
-    rank += (xu < xv) || (xu == xv && u < v);
+  int32_t rank = (int32_t)k - s;
+  if (!failed) {
+    rank = 0;
+    for (int32_t q = s; q < e; ++q) {
+      const int32_t u = __ldg(&tmp_perm[q]);
+      const T xu = __ldg(&y[(int64_t)u * D]);
+      rank += (xu < xv) || (xu == xv && u < v);
+    }
   }
   const int32_t dst = s + rank;
   perm[dst] = v;
@@ -229,13 +253,102 @@ template <typename T, int D>
 __global__ void __launch_bounds__(256)
 k_finalize(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
            const int32_t* __restrict__ start, int32_t n_total, const T* __restrict__ y,
-           int32_t* __restrict__ perm, T* __restrict__ pos, const int32_t* __restrict__ gate) {
+           int32_t* __restrict__ perm, T* __restrict__ pos, const int32_t* __restrict__ gate,
+           const int32_t* __restrict__ stats = nullptr) {
   if (gate && *gate != GATE_REBUILD) return;
   // Only start[n_total] slots were filled: points that failed the bounds check were not
   // binned, so the slot count is read on the device.
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= start[n_total]) return;
-  finalize_slot<T, D>(tmp_perm, cell_of_slot, start, k, y, perm, pos);
+  finalize_slot<T, D>(tmp_perm, cell_of_slot, start, k, y, perm, pos, stats);
+}
+
+// The in-cell rank of the slots of cells above LARGE_CELL points (cells, or hash lists with
+// HASH, whose order is (cell key, first coordinate, point index)).  A block takes 256
+// consecutive slots; when some of them lie in large cells, the block streams the keys of
+// those cells through shared memory, LARGE_TILE at a time, and every thread counts the keys
+// of its own cell that order before its own.  A cell of k points costs k^2 comparisons
+// from shared memory instead of k^2 dependent global loads.  Grid-stride over the slots;
+// returns at once when the build has no large cell (stats[0]) or failed the cell limit.
+template <typename T, int D, bool HASH>
+__global__ void __launch_bounds__(256)
+k_finalize_large(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
+                 const int4* __restrict__ key_tmp, const int32_t* __restrict__ start,
+                 int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
+                 T* __restrict__ pos, int4* __restrict__ key, const int32_t* __restrict__ stats,
+                 const int32_t* __restrict__ gate) {
+  if (gate && *gate != GATE_REBUILD) return;
+  if (stats[0] <= LARGE_CELL || stats[1] != 0) return;
+  __shared__ T s_x[LARGE_TILE];
+  __shared__ int32_t s_u[LARGE_TILE];
+  __shared__ int4 s_k[HASH ? LARGE_TILE : 1];
+  __shared__ int32_t s_lo, s_hi;
+  const int32_t n = start[n_total];
+  for (int64_t t0 = (int64_t)blockIdx.x * blockDim.x; t0 < n;
+       t0 += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = t0 + threadIdx.x;
+    bool large = false;
+    int32_t s = 0, e = 0, v = 0;
+    T xv = (T)0;
+    int4 kv = make_int4(0, 0, 0, 0);
+    if (threadIdx.x == 0) {
+      s_lo = INT32_MAX;
+      s_hi = INT32_MIN;
+    }
+    __syncthreads();
+    if (k < n) {
+      const int32_t c = cell_of_slot[k];
+      s = start[c];
+      e = start[c + 1];
+      large = e - s > LARGE_CELL;
+    }
+    if (large) {
+      atomicMin(&s_lo, s);
+      atomicMax(&s_hi, e);
+      v = tmp_perm[k];
+      xv = y[(int64_t)v * D];
+      if (HASH) kv = key_tmp[k];
+    }
+    __syncthreads();
+    const int32_t lo = s_lo, hi = s_hi;  // hi <= lo: no large cell in this block
+    int32_t rank = 0;
+    for (int32_t base = lo; base < hi; base += LARGE_TILE) {
+      const int32_t m = min(LARGE_TILE, hi - base);
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int32_t u = tmp_perm[base + i];
+        s_u[i] = u;
+        s_x[i] = y[(int64_t)u * D];
+        if (HASH) s_k[i] = key_tmp[base + i];
+      }
+      __syncthreads();
+      if (large) {
+        const int32_t i0 = max(s - base, 0), i1 = min(e - base, m);
+        for (int32_t i = i0; i < i1; ++i) {
+          const T xu = s_x[i];
+          const int32_t u = s_u[i];
+          bool before = (xu < xv) || (xu == xv && u < v);
+          if (HASH) {
+            const int4 ku = s_k[i];
+            const bool eq = ku.x == kv.x && ku.y == kv.y && ku.z == kv.z;
+            const bool lt = ku.x != kv.x ? ku.x < kv.x : (ku.y != kv.y ? ku.y < kv.y : ku.z < kv.z);
+            before = lt || (eq && before);
+          }
+          rank += before;
+        }
+      }
+      __syncthreads();
+    }
+    if (large) {
+      const int32_t dst = s + rank;
+      perm[dst] = v;
+      if (HASH) key[dst] = kv;
+      T p[D];
+#pragma unroll
+      for (int d = 0; d < D; ++d) p[d] = y[(int64_t)v * D + d];
+      store_pos<T, D>(pos, dst, p);
+    }
+    __syncthreads();  // every thread has read s_lo / s_hi before they are reset
+  }
 }
 
 // ---------------------------------------------------------------- incremental update
@@ -309,7 +422,10 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
         const unsigned peers = __match_any_sync(mv, cell);
         const int leader = __ffs(peers) - 1;
         int32_t cb = 0;
-        if (lane == leader) cb = atomicAdd(&ovf_counts[cell], __popc(peers));
+        if (lane == leader) {
+          cb = atomicAdd(&ovf_counts[cell], __popc(peers));
+          atomicMax(&ovf_n[1], cb + __popc(peers));  // the largest overflow cell so far
+        }
         cb = __shfl_sync(peers, cb, leader);
         ovf_list[m] = i;
         ovf_cell[m] = cell;
@@ -352,14 +468,16 @@ k_finalize_movers(const int32_t* __restrict__ tmp_perm, const int32_t* __restric
 
 // The decision: rebuild when the points outside their main cell exceed `fraction` of the
 // binned points (the traversal cost of the overflow lists grows with them, while a full
-// rebuild costs about as much as marking the movers).
+// rebuild costs about as much as marking the movers), or when some cell's overflow list
+// would exceed LARGE_CELL points (k_finalize_movers ranks one cell's list per thread).
 // gate[1] ("unsorted") tells the traversal that the main slots are no longer sorted by x
 // inside their cells (the overflow path refreshes positions in place).
 __global__ void k_decide_update(const int32_t* __restrict__ ovf_n,
                                 const int32_t* __restrict__ n_main, double fraction,
                                 int32_t* __restrict__ gate) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
-    const int32_t m = (double)*ovf_n > fraction * (double)*n_main ? GATE_REBUILD : GATE_OVERFLOW;
+    const int32_t m = ((double)ovf_n[0] > fraction * (double)*n_main || ovf_n[1] > LARGE_CELL)
+                          ? GATE_REBUILD : GATE_OVERFLOW;
     gate[0] = m;
     gate[1] = m == GATE_OVERFLOW ? 1 : 0;
   }
@@ -413,6 +531,11 @@ static void dispatch_bin(pn_search* s, const T* y, int64_t n_y, const int32_t* i
   }
 }
 
+// The build's cell statistics (k_scan_cells): [0] largest cell, [1] cell limit exceeded.
+static int32_t* build_stats(pn_search* s) { return s->d_err + 5; }
+
+// The in-cell sort: k_finalize for cells up to LARGE_CELL points, then k_finalize_large
+// (one wave of blocks; it returns at once when the build has no larger cell).
 template <typename T>
 static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st,
                             const int32_t* gate = nullptr) {
@@ -420,23 +543,40 @@ static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st
   if (blocks == 0) return;
   T* pos = static_cast<T*>(s->d_pos);
   const int32_t nt = s->n_total;
+  const int32_t* stats = build_stats(s);
+  const int lb = std::min(blocks, 152 * 4);
   switch (s->ndims) {
-    case 1: k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate); count_launch(); break;
-    case 2: k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate); count_launch(); break;
-    default: k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate); count_launch(); break;
+    case 1:
+      k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats);
+      k_finalize_large<T, 1, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate);
+      break;
+    case 2:
+      k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats);
+      k_finalize_large<T, 2, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate);
+      break;
+    default:
+      k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats);
+      k_finalize_large<T, 3, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate);
+      break;
   }
+  count_launch();
+  count_launch();
 }
 
 // Exclusive scan of the cell histogram into s->d_start (one launch).
 // start[c] = *base_ptr + sum(counts[0..c)) when base_ptr is given.
+// The cell-list scans record the build's statistics; the overflow lists' scan does not.
 static void scan_cells(pn_search* s, const int32_t* counts, int32_t* start, cudaStream_t st,
                        const int32_t* base_ptr = nullptr, int32_t max_ppc = 0,
-                       const int32_t* gate = nullptr, int32_t gate_want = 0) {
+                       const int32_t* gate = nullptr, int32_t gate_want = 0,
+                       bool stats = true) {
   cudaMemsetAsync(s->d_scan_state, 0, sizeof(unsigned long long) * (s->scan_tiles + 1), st);
   k_scan_cells<<<s->scan_tiles, SCAN_THREADS, 0, st>>>(counts, s->n_total, start,
                                                        s->d_scan_state, s->scan_tiles,
                                                        max_ppc, base_ptr, s->d_err, gate,
-                                                       gate_want); count_launch();
+                                                       gate_want,
+                                                       stats ? build_stats(s) : nullptr);
+  count_launch();
 }
 
 template <typename T>
@@ -448,6 +588,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * s->n_total, st);
   cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
   cudaMemsetAsync(s->d_err + 3, 0, sizeof(int32_t), st);  // cells sorted by x again
+  cudaMemsetAsync(build_stats(s), 0, 2 * sizeof(int32_t), st);
   if (m > 0) dispatch_bin<T>(s, y, n_y, idx, (int32_t)m, st);
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell);
   if (m > 0) {
@@ -577,20 +718,26 @@ __global__ void __launch_bounds__(256)
 k_hash_finalize(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ bucket_of_slot,
                 const int4* __restrict__ key_tmp, const int32_t* __restrict__ start,
                 int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
-                T* __restrict__ pos, int4* __restrict__ key) {
+                T* __restrict__ pos, int4* __restrict__ key, const int32_t* __restrict__ stats) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= start[n_total]) return;
   const int32_t b = bucket_of_slot[k];
   const int32_t s = start[b], e = start[b + 1];
+  // as finalize_slot: large lists go to k_finalize_large, a failed limit check keeps order
+  const bool failed = stats[1] != 0;
+  if (!failed && e - s > LARGE_CELL) return;
   const int32_t v = tmp_perm[k];
   const int4 kv = key_tmp[k];
   const T xv = y[(int64_t)v * D];
-  int32_t rank = 0;
-  for (int32_t q = s; q < e; ++q) {
-    const int32_t u = __ldg(&tmp_perm[q]);
-    const int4 ku = __ldg(&key_tmp[q]);
-    const T xu = __ldg(&y[(int64_t)u * D]);
-    rank += key_less(ku, kv) || (key_eq(ku, kv) && ((xu < xv) || (xu == xv && u < v)));
+  int32_t rank = (int32_t)k - s;
+  if (!failed) {
+    rank = 0;
+    for (int32_t q = s; q < e; ++q) {
+      const int32_t u = __ldg(&tmp_perm[q]);
+      const int4 ku = __ldg(&key_tmp[q]);
+      const T xu = __ldg(&y[(int64_t)u * D]);
+      rank += key_less(ku, kv) || (key_eq(ku, kv) && ((xu < xv) || (xu == xv && u < v)));
+    }
   }
   const int32_t dst = s + rank;
   perm[dst] = v;
@@ -710,6 +857,7 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
   // 1. cells and their bounding box
   s->n_total = nl;
   s->hash_dense = false;
+  cudaMemsetAsync(build_stats(s), 0, 2 * sizeof(int32_t), st);
   k_hash_bbox_init<<<1, 32, 0, st>>>(s->d_hbbox); count_launch();
   const int blocks = std::max(1, std::min(div_up(std::max<int64_t>(m, 1), BIN_THREADS), 152 * 8));
   if (m > 0) {
@@ -792,7 +940,7 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
     count_launch();
     // (the search's scan state has room for the tiles of list_size >= cells counts)
     scan_counts(s->d_counts, (int32_t)cells, s->d_start, s->d_scan_state,
-                scan_tile_count(cells), s->d_err, st);
+                scan_tile_count(cells), s->d_err, st, build_stats(s));
     k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
                                               s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
                                               nullptr); count_launch();
@@ -806,10 +954,14 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
                                       s->d_hkey_tmp); count_launch();
     T* pos = static_cast<T*>(s->d_pos);
     switch (s->ndims) {
-      case 1: k_hash_finalize<T, 1><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey); break;
-      case 2: k_hash_finalize<T, 2><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey); break;
-      default: k_hash_finalize<T, 3><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey); break;
+      case 1: k_hash_finalize<T, 1><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey, build_stats(s));
+              k_finalize_large<T, 1, true><<<std::min(b, 152 * 4), 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey, build_stats(s), nullptr); break;
+      case 2: k_hash_finalize<T, 2><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey, build_stats(s));
+              k_finalize_large<T, 2, true><<<std::min(b, 152 * 4), 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey, build_stats(s), nullptr); break;
+      default: k_hash_finalize<T, 3><<<b, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey, build_stats(s));
+              k_finalize_large<T, 3, true><<<std::min(b, 152 * 4), 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_hkey_tmp, s->d_start, nl, y, s->d_perm, pos, s->d_hkey, build_stats(s), nullptr); break;
     }
+    count_launch();
     count_launch();
     // the heads go into d_slot_of (free again after the scatter), their scan into hcellidx
     k_hash_heads<<<b, 256, 0, st>>>(s->d_cell_of_slot, s->d_hkey, s->d_start + nl, (int32_t)m,
@@ -841,10 +993,10 @@ template int build_hash<double>(pn_search*, const double*, int64_t, const int32_
 // (pn_batch.cu bins the points of many clouds itself, then reuses these on the
 // concatenated cell and slot arrays.)
 void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long long* state,
-                 int32_t tiles, int32_t* err, cudaStream_t st) {
+                 int32_t tiles, int32_t* err, cudaStream_t st, int32_t* stats) {
   cudaMemsetAsync(state, 0, sizeof(unsigned long long) * (tiles + 1), st);
   k_scan_cells<<<tiles, SCAN_THREADS, 0, st>>>(counts, n, start, state, tiles, 0, nullptr, err,
-                                               nullptr, 0); count_launch();
+                                               nullptr, 0, stats); count_launch();
 }
 
 int32_t scan_tile_count(int64_t n) { return div_up(n, SCAN_TILE); }
@@ -943,7 +1095,8 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
     s->main_perm_valid = true;
   }
   cudaMemsetAsync(s->d_ovf_counts, 0, sizeof(int32_t) * s->n_total, st);
-  cudaMemsetAsync(s->d_ovf_n, 0, sizeof(int32_t), st);
+  cudaMemsetAsync(s->d_ovf_n, 0, 2 * sizeof(int32_t), st);  // movers, largest overflow cell
+  cudaMemsetAsync(build_stats(s), 0, 2 * sizeof(int32_t), st);
   cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
   const bool per = s->periodic != 0;
   switch (s->ndims * 2 + (per ? 1 : 0)) {
@@ -959,7 +1112,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
                                     gate); count_launch();
   // overflow path
   scan_cells(s, s->d_ovf_counts, s->d_ovf_start, st, s->d_start + s->n_total, 0, gate,
-             GATE_OVERFLOW);
+             GATE_OVERFLOW, false);
   switch (s->ndims) {
     case 1: launch_movers<T, 1>(s, y, st); break;
     case 2: launch_movers<T, 2>(s, y, st); break;

@@ -27,6 +27,10 @@ struct pn_search {
   // geometry (values exact in T, stored as double)
   int32_t ndims, dtype, periodic, is_template;
   int32_t mixed;        // PN_FLAG_FLOAT32_SEARCH: Float64 coordinates, Float32 pair arithmetic
+  // pn_create_from_grid: cfg.min_corner / max_corner are the cell list's stored (padded)
+  // corners and the grid has given_grid cells per dimension, both taken as they are
+  int32_t from_grid = 0;
+  int64_t given_grid[3] = {0, 0, 0};
   int32_t hashed;       // SpatialHashingCellList (n_total = list_size hash lists)
   int64_t list_size;
   int64_t grid_size[3], n_cells[3];
@@ -148,8 +152,9 @@ void refresh_pos32(pn_search* s, cudaStream_t st);
 int export_hash_lists(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
 int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st);
 // generic pieces of the build, reused by the batched build (pn_batch.cu)
+// stats (or null): receives the largest count and the limit flag (see k_scan_cells)
 void scan_counts(const int32_t* counts, int32_t n, int32_t* start, unsigned long long* state,
-                 int32_t tiles, int32_t* err, cudaStream_t st);
+                 int32_t tiles, int32_t* err, cudaStream_t st, int32_t* stats = nullptr);
 int32_t scan_tile_count(int64_t n);
 int selftest_bounded_wait(cudaStream_t st);
 void scatter_slots(const int32_t* cell_of, const int32_t* slot_of, int32_t m,

@@ -228,3 +228,75 @@ def test_host_api_argument_errors(pkg):
     assert P.requires_update(None) == (False, True)
     with pytest.raises(P.UnsupportedFunctorError):
         P.foreach_point_neighbor(lambda i, j, pd, d: None, None, None, None)
+
+
+def _cfg_from_grid(L, ndims, dtype, r, corners_lo, corners_hi, box=None):
+    cfg = L.pn_config()
+    cfg.ndims = ndims
+    cfg.dtype = L.PN_FLOAT32 if dtype == np.float32 else L.PN_FLOAT64
+    cfg.search_radius = float(dtype(r))
+    for k in range(ndims):
+        cfg.min_corner[k] = corners_lo[k]
+        cfg.max_corner[k] = corners_hi[k]
+    if box is not None:
+        cfg.periodic = 1
+        for k in range(ndims):
+            cfg.periodic_min[k] = float(dtype(box[0][k]))
+            cfg.periodic_max[k] = float(dtype(box[1][k]))
+    return cfg
+
+
+@pytest.mark.parametrize("g", GEOMS + [(3, np.float64, 3.0, [-1.0] * 3, [101.0] * 3, None),
+                                       (3, np.float64, 1.0, [0.0] * 3, [10.0] * 3, None)])
+def test_geometry_from_grid_state(L, g):
+    """pn_compute_geometry_from_grid takes a reference FullGridCellList's stored state -- its
+    padded corners and size(linear_indices) -- as it is and gives the geometry the
+    constructor computed from the unpadded corners, bit for bit.  (Removing the padding
+    from the stored corners and padding again is not an identity in floating point; the
+    cases where that round trip moves a corner are listed by this test's second half.)"""
+    ndims, dt, r, mn, mx, box = g
+    rc, gi = _geometry(L, ndims, dt, r, mn, mx, box)
+    assert rc == 0
+    grid = (C.c_int64 * 3)(*[gi.grid_size[k] if k < ndims else 0 for k in range(3)])
+    cfg = _cfg_from_grid(L, ndims, dt, r, list(gi.min_corner), list(gi.max_corner), box)
+    g2 = L.pn_grid_info()
+    assert L.load().pn_compute_geometry_from_grid(C.byref(cfg), grid, C.byref(g2)) == 0
+    for k in range(ndims):
+        assert g2.grid_size[k] == gi.grid_size[k]
+        assert g2.min_corner[k] == gi.min_corner[k] and g2.max_corner[k] == gi.max_corner[k]
+        assert g2.cell_size[k] == gi.cell_size[k] and g2.n_cells[k] == gi.n_cells[k]
+    # the naive route: unpad the stored corners in T, then construct as usual
+    pad = dt(dt(1001) / dt(1000)) * dt(r)
+    lo = [float(dt(dt(gi.min_corner[k]) + pad)) for k in range(ndims)]
+    hi = [float(dt(dt(gi.max_corner[k]) - pad)) for k in range(ndims)]
+    rc3, g3 = _geometry(L, ndims, dt, r, lo, hi, box)
+    moved = rc3 != 0 or any(g3.min_corner[k] != gi.min_corner[k] or
+                            g3.max_corner[k] != gi.max_corner[k] or
+                            g3.grid_size[k] != gi.grid_size[k] for k in range(ndims))
+    exact_inputs = all(float(dt(mn[k])) == lo[k] and float(dt(mx[k])) == hi[k]
+                       for k in range(ndims))
+    # where unpadding recovers the constructor's corners the naive route agrees; only
+    # where it does not can the geometry move (hence the stored state is taken as it is)
+    assert not (moved and exact_inputs)
+
+
+def test_geometry_from_grid_golden_corners(L, golden):
+    """test/cell_lists/full_grid.jl:28-29: corners 0 and 10 with radius 1 are stored as
+    -1.001 and 11.001; from that stored state the search has the same 13 cells."""
+    c = golden["full_grid_bounds"]
+    rc, gi = _geometry(L, 3, np.float64, c["radius"], [c["min_corner"]] * 3,
+                       [c["max_corner"]] * 3)
+    assert rc == 0 and gi.min_corner[0] == c["expected_min_pad"]
+    assert gi.max_corner[0] == c["expected_max_pad"]
+    cfg = _cfg_from_grid(L, 3, np.float64, c["radius"], [c["expected_min_pad"]] * 3,
+                         [c["expected_max_pad"]] * 3)
+    g2 = L.pn_grid_info()
+    grid = (C.c_int64 * 3)(*gi.grid_size)
+    assert L.load().pn_compute_geometry_from_grid(C.byref(cfg), grid, C.byref(g2)) == 0
+    assert list(g2.grid_size) == list(gi.grid_size) == [13, 13, 13]
+    # a template (radius 0) stores no cells; a non-template needs at least one per dimension
+    cfg0 = _cfg_from_grid(L, 3, np.float64, 0.0, [0.0] * 3, [10.0] * 3)
+    assert L.load().pn_compute_geometry_from_grid(C.byref(cfg0), (C.c_int64 * 3)(0, 0, 0),
+                                                  C.byref(g2)) == 0 and g2.is_template
+    bad = (C.c_int64 * 3)(13, 0, 13)
+    assert L.load().pn_compute_geometry_from_grid(C.byref(cfg), bad, C.byref(g2)) == L.PN_ERR_INVALID_ARG
