@@ -22,6 +22,7 @@ check); `check=False` leaves them asynchronous on torch's current stream.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import numbers
 
 import numpy as np
@@ -147,6 +148,34 @@ class FullGridCellList:
         pad = T(R(R(1001) / R(1000)) * r)
         self.min_corner = (self._min - pad).astype(T)
         self.max_corner = (self._max + pad).astype(T)
+        self.grid_size = None  # computed by the search from the corners
+
+    @classmethod
+    def from_state(cls, *, min_corner, max_corner, grid_size, max_points_per_cell=100,
+                   search_radius=0.0):
+        """A cell list given by the fields a reference FullGridCellList stores
+        (full_grid.jl:30-35): its padded `min_corner`/`max_corner`, `size(linear_indices)`
+        and the backend's capacity `size(cells.backend, 1)`.  The search takes them as they
+        are (pn_create_from_grid) instead of padding corners again."""
+        self = cls.__new__(cls)
+        mn = _vec(min_corner, np.float64)
+        mx = _vec(max_corner, np.float64)
+        gs = [int(v) for v in np.atleast_1d(grid_size)]
+        if mn.size != mx.size or mn.size != len(gs):
+            raise ArgumentError("min_corner, max_corner and grid_size must have the same length")
+        if mn.size > 3:
+            raise ArgumentError("this GPU FullGridCellList supports 1 to 3 dimensions")
+        R = _eltype(search_radius) if not isinstance(search_radius, numbers.Integral) else np.float64
+        T = np.float32 if _eltype(min_corner) == np.float32 and R == np.float32 else np.float64
+        self.eltype = T
+        self.ndims = mn.size
+        self.min_corner = mn.astype(T)
+        self.max_corner = mx.astype(T)
+        self._min, self._max = self.min_corner, self.max_corner
+        self.search_radius = search_radius
+        self.max_points_per_cell = int(max_points_per_cell)
+        self.grid_size = tuple(gs)
+        return self
 
 
 class SpatialHashingCellList:
@@ -256,6 +285,27 @@ def check_update_strategy(cell_list, update_strategy):
     return update_strategy
 
 
+def _periodic_argument_error(box, r, ndims, cell_list, from_state):
+    """The ArgumentError for a periodic search the library rejected: the reference's message
+    when a dimension has fewer than 3 periodic cells (nhs_grid.jl:113-116), else the reason
+    that is this library's own (the grid must hold the periodic cells and their neighbours,
+    n_cells + 2 <= cells of the padded grid, and have fewer than 2^31 cells)."""
+    T = _eltype(r)
+    for k in range(ndims):
+        size = T(T(box.max_corner[k]) - T(box.min_corner[k]))
+        if math.floor((float(size) + 10 * 2.220446049250313e-16) / float(r)) < 3:
+            raise ArgumentError("the `GridNeighborhoodSearch` needs at least 3 cells in "
+                                "each dimension when used with periodicity. Please use no "
+                                "NHS for very small problems.")
+    if cell_list is not None:
+        raise ArgumentError("the cell list must cover the periodic box: it needs n_cells + 2 "
+                            "cells per dimension" +
+                            (" (grid_size too small for the PeriodicBox)" if from_state else
+                             " (build it over the PeriodicBox's corners)") +
+                            ", and fewer than 2^31 cells in total")
+    raise ArgumentError("invalid PeriodicBox for this search")
+
+
 class GridNeighborhoodSearch:
     """GridNeighborhoodSearch{ndims}(; search_radius, n_points, periodic_box, cell_list,
     update_strategy) over a FullGridCellList (nhs_grid.jl:67-129).
@@ -307,6 +357,7 @@ class GridNeighborhoodSearch:
         cfg.dtype = _lib.PN_FLOAT32 if C_ == np.float32 else _lib.PN_FLOAT64
         cfg.flags = _lib.PN_FLAG_FLOAT32_SEARCH if self.mixed else 0
         cfg.search_radius = float(self.search_radius)
+        from_state = not hashing and cell_list.grid_size is not None
         if not hashing:
             for k in range(self.ndims):
                 cfg.min_corner[k] = float(C_(cell_list._min[k]))
@@ -323,13 +374,16 @@ class GridNeighborhoodSearch:
         h = C.c_void_p()
         if hashing:
             rc = lib().pn_create_spatial_hashing(C.byref(cfg), cell_list.list_size, C.byref(h))
+        elif from_state:
+            grid = (C.c_int64 * 3)(*(list(cell_list.grid_size) + [0] * (3 - self.ndims)))
+            rc = lib().pn_create_from_grid(C.byref(cfg), grid, C.byref(h))
         else:
             rc = lib().pn_create(C.byref(cfg), C.byref(h))
         if rc != _lib.PN_OK:
-            if rc == _lib.PN_ERR_INVALID_ARG and periodic_box is not None:
-                raise ArgumentError("the `GridNeighborhoodSearch` needs at least 3 cells in "
-                                    "each dimension when used with periodicity. Please use no "
-                                    "NHS for very small problems.")
+            if rc == _lib.PN_ERR_INVALID_ARG and periodic_box is not None and \
+                    self.search_radius >= 2.220446049250313e-16:
+                _periodic_argument_error(periodic_box, self.search_radius, self.ndims,
+                                         None if hashing else cell_list, from_state)
             _raise(rc, "GridNeighborhoodSearch")
         self._h = h
         if isinstance(update_strategy, ParallelIncrementalUpdate):

@@ -300,3 +300,20 @@ def test_geometry_from_grid_golden_corners(L, golden):
                                                   C.byref(g2)) == 0 and g2.is_template
     bad = (C.c_int64 * 3)(13, 0, 13)
     assert L.load().pn_compute_geometry_from_grid(C.byref(cfg), bad, C.byref(g2)) == L.PN_ERR_INVALID_ARG
+
+
+def test_periodic_argument_errors(pkg):
+    """The reference's message only for fewer than 3 periodic cells (nhs_grid.jl:113-116);
+    a cell list that does not cover the periodic box gets its own reason.  Both are
+    rejected by the host-side geometry, before any device call."""
+    P = pkg
+    box = P.PeriodicBox(min_corner=np.zeros(2), max_corner=np.full(2, 5.0))
+    cl = P.FullGridCellList(min_corner=np.zeros(2), max_corner=np.full(2, 5.0),
+                            search_radius=2.0)
+    with pytest.raises(P.ArgumentError, match="needs at least 3 cells"):
+        P.GridNeighborhoodSearch(2, search_radius=2.0, periodic_box=box, cell_list=cl)
+    box = P.PeriodicBox(min_corner=np.zeros(2), max_corner=np.full(2, 30.0))
+    small = P.FullGridCellList(min_corner=np.zeros(2), max_corner=np.full(2, 10.0),
+                               search_radius=1.0)
+    with pytest.raises(P.ArgumentError, match="must cover the periodic box"):
+        P.GridNeighborhoodSearch(2, search_radius=1.0, periodic_box=box, cell_list=small)
