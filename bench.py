@@ -80,6 +80,12 @@ def parse():
                     help="batched workload: number of clouds")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="wcsph workload: leave out the batched, adjoint, Float64 and "
+                         "update-path records that the default line carries")
+    ap.add_argument("--rebuild-fraction", type=float, default=0.01,
+                    help="ParallelIncrementalUpdate's rebuild fraction (1.0: update! keeps "
+                         "overflow lists instead of rebuilding)")
     ap.add_argument("--workload", default="wcsph",
                     choices=["wcsph", "nbody2d", "count", "adjoint", "batched",
                              "precomputed"],
@@ -239,9 +245,10 @@ def run_gpu(args, rank, world, local):
         cl = P.FullGridCellList(min_corner=np.full(3, -1.0, dt),
                                 max_corner=np.full(3, n_side + 1.0, dt),
                                 search_radius=r, max_points_per_cell=0)
-        nhs = P.GridNeighborhoodSearch(3, search_radius=r, n_points=n, cell_list=cl,
-                                       update_strategy=P.ParallelIncrementalUpdate(),
-                                       pair_cache=args.pair_cache)
+        nhs = P.GridNeighborhoodSearch(
+            3, search_radius=r, n_points=n, cell_list=cl,
+            update_strategy=P.ParallelIncrementalUpdate(args.rebuild_fraction),
+            pair_cache=args.pair_cache)
     x0d = torch.as_tensor(x0, device="cuda").T
     vd = torch.as_tensor(v, device="cuda").reshape(-1)
     rho = torch.zeros(n, dtype=tdt, device="cuda")
@@ -306,6 +313,13 @@ def run_gpu(args, rank, world, local):
     wall = time.perf_counter() - wall0
     launches = P.lib().pn_launch_count() - launches0
     clocks = sampler.stop() if sampler else None
+    # which of update!'s two paths the timed steps took: the device rebuilds when the points
+    # that left their cell of the last full build exceed rebuild_fraction of all points
+    movers = int(nhs.grid_info()["n_overflow"])
+    if hashing:
+        update_path = "rebuild (ParallelUpdate)"
+    else:
+        update_path = "rebuild" if movers > args.rebuild_fraction * n else "overflow lists"
     st = P.lib().pn_sync(nhs.handle)
     if st != 0:
         raise RuntimeError(f"timed region reported status {st}")
@@ -340,8 +354,10 @@ def run_gpu(args, rank, world, local):
         force_b = [P.WCSPHForce(density=rb[i], pressure=pb[i], velocity=vb[i], accel=ab[i],
                                 reuse_state=True, **W.WCSPH) for i in range(2)]
         comp = torch.cuda.current_stream()
-        s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
+        # positions and velocities are uploaded on two streams (two copy engines)
+        s_in, s_in2, s_out = torch.cuda.Stream(), torch.cuda.Stream(), torch.cuda.Stream()
         ev_in = [torch.cuda.Event() for _ in range(2)]
+        ev_in2 = [torch.cuda.Event() for _ in range(2)]
         ev_done = [torch.cuda.Event() for _ in range(2)]
         ev_out = [torch.cuda.Event() for _ in range(2)]
         for e in ev_done + ev_out:
@@ -353,12 +369,16 @@ def run_gpu(args, rank, world, local):
 
         def h2d(k, xh):
             bi = k % 2
+            with torch.cuda.stream(s_in2):
+                s_in2.wait_event(ev_done[bi])  # step k-2 no longer reads buffer bi
+                vb[bi].copy_(v_h, non_blocking=True)
+                ev_in2[bi].record(s_in2)
             with torch.cuda.stream(s_in):
-                s_in.wait_event(ev_done[bi])  # step k-2 no longer reads buffer bi
+                s_in.wait_event(ev_done[bi])
                 if timing[0]:
                     tev[k][0].record(s_in)
                 xb[bi].copy_(xh, non_blocking=True)
-                vb[bi].copy_(v_h, non_blocking=True)
+                s_in.wait_event(ev_in2[bi])  # the upload ends when both copies have
                 if timing[0]:
                     tev[k][1].record(s_in)
                 ev_in[bi].record(s_in)
@@ -405,6 +425,7 @@ def run_gpu(args, rank, world, local):
         timing[0] = True
         a0.record(comp)
         s_in.wait_event(a0)
+        s_in2.wait_event(a0)
         run(K, lambda k: walk_h[k])
         a1.record(comp)
         torch.cuda.synchronize()
@@ -430,7 +451,8 @@ def run_gpu(args, rank, world, local):
                "h2d_ms_max": max(tev[k][0].elapsed_time(tev[k][1]) for k in range(K)),
                "compute_ms_max": max(tev[k][2].elapsed_time(tev[k][3]) for k in range(K)),
                "clocks": e2e_clocks,
-               "path": "pinned host -> cudaMemcpyAsync (copy stream, double-buffered) -> "
+               "path": "pinned host -> cudaMemcpyAsync (positions and velocities on two copy "
+                       "streams, double-buffered) -> "
                        "pn_update + pn_foreach_point_neighbor (density, force) -> "
                        "cudaMemcpyAsync (second copy stream) -> pinned host density and "
                        "acceleration"}
@@ -502,13 +524,14 @@ def run_gpu(args, rank, world, local):
                    "l2": "working set > L2 (coordinates, sorted copies and outputs ~1 GB), no flush"},
         "update_ms": statistics.median(upd), "density_ms": statistics.median(den),
         "force_ms": statistics.median(frc), "wall_ms_per_step": 1e3 * wall / K,
+        "update_path": update_path, "movers_per_step": movers,
+        "rebuild_fraction": None if hashing else args.rebuild_fraction,
         "gpu_launches": int(launches), "launches_per_step": launches / K,
         "roofline": roofline, "fp32_roofline": fp32_roofline, "e2e": e2e, "clocks": clocks,
         "cpu_baseline": cpu,
         "gpu": torch.cuda.get_device_name(),
     }
-    if rank == 0:
-        print(json.dumps(out))
+    return out
 
 
 # ------------------------------------------------------------------ CPU (oracle)
@@ -671,8 +694,7 @@ def run_gpu_sweep(args, rank, world, local):
            "build_ms": b0.elapsed_time(b1),
            "gpu_launches": int(P.lib().pn_launch_count() - launches0),
            "gpu": torch.cuda.get_device_name()}
-    if rank == 0:
-        print(json.dumps(out))
+    return out
 
 
 def run_gpu_adjoint(args, rank, world, local):
@@ -727,6 +749,23 @@ def run_gpu_adjoint(args, rank, world, local):
     f_ms = statistics.median(ev[k][0].elapsed_time(ev[k][1]) for k in range(K))
     b_ms = statistics.median(ev[k][1].elapsed_time(ev[k][2]) for k in range(K))
     tot_s = sum(ev[k][0].elapsed_time(ev[k][2]) for k in range(K)) / 1e3
+    grad_err = None
+    if dt == np.float32:
+        # the Float32 gradient against the library's Float64 one on the same points (the
+        # Float64 forward/backward agree with the FP64 oracle to 1e-10 in tests/test_adjoint.py)
+        x64 = torch.as_tensor(x.astype(np.float64), device="cuda").T
+        cl64 = P.FullGridCellList(min_corner=np.full(3, -1.0), max_corner=np.full(3, side + 1.0),
+                                  search_radius=3.0, max_points_per_cell=0)
+        nhs64 = P.GridNeighborhoodSearch(3, search_radius=3.0, n_points=n, cell_list=cl64)
+        P.initialize(nhs64, x64, x64)
+        g64 = torch.empty(3 * n, dtype=torch.float64, device="cuda")
+        P.foreach_point_neighbor(P.AdjointLossForward(
+            density=torch.empty(n, dtype=torch.float64, device="cuda"),
+            terms=torch.empty(n, dtype=torch.float64, device="cuda"),
+            loss=torch.empty(1, dtype=torch.float64, device="cuda"), **consts), x64, x64, nhs64)
+        P.foreach_point_neighbor(P.AdjointLossBackward(grad=g64, reuse_state=True, **consts),
+                                 x64, x64, nhs64)
+        grad_err = float((grad.double() - g64).abs().max() / g64.abs().max())
     out = {"metric": f"adjoint pair-evals/s (1M pts, {'FP32' if dt == np.float32 else 'FP64'}, "
                      "r=3, forward loss + backward dL/dx)",
            "value": 2.0 * pairs * K / tot_s, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -737,11 +776,13 @@ def run_gpu_adjoint(args, rank, world, local):
                                   "U[-0.25,0.25] noise, r=3, Wendland h=1.5, 1/r potential cutoff 3",
                       "pairs_per_sweep": pairs},
            "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
+           "grad_rel_err_vs_f64": grad_err,
+           "grad_rel_err_definition": "max |dL/dx (FP32) - dL/dx (FP64, this library)| / "
+                                      "max |dL/dx (FP64)| over all 3M components",
            "loss": float(loss.item()),
            "gpu_launches": int(P.lib().pn_launch_count() - launches0), "clocks": clocks,
            "gpu": torch.cuda.get_device_name()}
-    if rank == 0:
-        print(json.dumps(out))
+    return out
 
 
 def run_gpu_batched(args, rank, world, local):
@@ -898,8 +939,7 @@ def run_gpu_batched(args, rank, world, local):
            "identical_results": {"direct": same_direct, "graph": same_graph},
            "gpu_launches": int(batch_launches * K), "clocks": clocks,
            "gpu": torch.cuda.get_device_name()}
-    if rank == 0:
-        print(json.dumps(out))
+    return out
 
 
 def run_gpu_precomputed(args, rank, world, local):
@@ -1003,8 +1043,44 @@ def run_gpu_precomputed(args, rank, world, local):
            "loops_pair_evals_per_s": 2.0 * pairs / K / (loops_ms / 1e3),
            "wall_ms_per_step": 1e3 * wall / K, "update_host_ms": 1e3 * upd_wall / K,
            "gpu": torch.cuda.get_device_name()}
-    if rank == 0:
-        print(json.dumps(out))
+    return out
+
+
+def extra_records(args, rank, world, local):
+    """The rest of the headline metric ("batched & adjoint vs plain, same GPU"), measured in
+    the same run on the same GPU after the plain step: the batched 512-cloud step against
+    per-cloud launches, the adjoint step's backward/forward ratio, the 8M step in Float64,
+    and the plain step with update! forced onto its overflow-list path.  Each record carries
+    its own CUDA-event times and clock samples."""
+    import copy
+    K, Wm = args.steps, args.warmup
+
+    def sub(**kw):
+        a = copy.copy(args)
+        a.no_e2e, a.no_cpu, a.no_extras = True, True, True
+        for k, v in kw.items():
+            setattr(a, k, v)
+        return a
+
+    rec = {}
+    t = time.perf_counter()
+    rec["update_paths"] = {
+        "overflow": _path_record(run_gpu(sub(rebuild_fraction=1.0), rank, world, local)),
+        "note": "rebuild_fraction 1.0: update! keeps the movers in overflow lists (never "
+                "rebuilds), whose queries the pair cache leaves to the stencil traversal"}
+    rec["batched"] = run_gpu_batched(sub(steps=min(K, 10), warmup=min(Wm, 3)), rank, world, local)
+    rec["adjoint"] = run_gpu_adjoint(sub(dtype="float32"), rank, world, local)
+    rec["fp64"] = _path_record(run_gpu(sub(dtype="float64", steps=min(K, 5),
+                                           warmup=min(Wm, 3)), rank, world, local))
+    rec["extras_wall_s"] = time.perf_counter() - t
+    return rec
+
+
+def _path_record(o):
+    keep = ("metric", "value", "unit", "ms_per_step", "update_ms", "density_ms", "force_ms",
+            "update_path", "movers_per_step", "dtype", "steps", "warmup", "clocks",
+            "gpu_launches")
+    return {k: o[k] for k in keep if k in o}
 
 
 def main():
@@ -1017,15 +1093,19 @@ def main():
     rank, world, local = dist_setup("nccl")
     try:
         if args.workload == "wcsph":
-            run_gpu(args, rank, world, local)
+            out = run_gpu(args, rank, world, local)
+            if not args.no_extras and args.dtype == "float32" and args.cell_list == "full_grid":
+                out.update(extra_records(args, rank, world, local))
         elif args.workload == "adjoint":
-            run_gpu_adjoint(args, rank, world, local)
+            out = run_gpu_adjoint(args, rank, world, local)
         elif args.workload == "batched":
-            run_gpu_batched(args, rank, world, local)
+            out = run_gpu_batched(args, rank, world, local)
         elif args.workload == "precomputed":
-            run_gpu_precomputed(args, rank, world, local)
+            out = run_gpu_precomputed(args, rank, world, local)
         else:
-            run_gpu_sweep(args, rank, world, local)
+            out = run_gpu_sweep(args, rank, world, local)
+        if rank == 0:
+            print(json.dumps(out))
     finally:
         if world > 1:
             import torch.distributed as dist

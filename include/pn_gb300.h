@@ -423,11 +423,16 @@ int pn_batch_sync(pn_batch* b);
  *    PN_NOALLOC_SCRATCH_BYTES, else PN_ERR_SCRATCH_LIMIT (nothing is launched).
  *  - The first call on a device (the current one) looks up the scratch's address there,
  *    which can load the library's module: make that first call before any stream capture.
+ *    The address is kept per device for the life of the process; after cudaDeviceReset
+ *    the module is loaded anew (possibly elsewhere), so do not call this entry point
+ *    again in a process that reset the device.
  *  - Every call shares the scratch, which keeps the last call's contents (each call clears
  *    what must start at zero); calls that overlap on the GPU race, so serialise calls made
  *    from several host threads or streams.
- *  - x and counts are device pointers; the call returns after the counts are written, with
- *    the kernel's status (PN_ERR_OUT_OF_DOMAIN, PN_ERR_CELL_FULL) as its result. */
+ *  - x and counts are device pointers.  The call is synchronous on `stream`: it reads the
+ *    kernel's status back and waits for the stream before it returns that status
+ *    (PN_ERR_OUT_OF_DOMAIN, PN_ERR_CELL_FULL) as its result, so the host blocks until
+ *    the work queued on `stream` before it has finished as well. */
 int pn_count_neighbors_noalloc(const pn_config* cfg, const void* x, int64_t n, int32_t* counts,
                                pn_stream_t stream);
 

@@ -156,3 +156,47 @@ def test_batch_rejects_what_it_does_not_support(P):
     x[13, 0] = 50.0
     with pytest.raises(P.PointNeighborsError, match="outside the domain"):
         batch.initialize(x.T)
+
+
+def test_batch_vs_oracle_64_clouds(P, O):
+    """64 clouds of the batched workload's kind, each checked against the FP64 oracle of its
+    own search (its corners, radius and h = radius / 2): counts bit-exact, density and
+    acceleration within 1e-5 of the sum of |terms|."""
+    from test_gpu_parity import TOL_F32, _rel_err
+    clouds = P.workloads.batched_clouds(n_clouds=64, n_min=100, n_max=3000, seed=11)
+    searches = _searches(P, clouds)
+    xs = torch.as_tensor(_concat(clouds, "x"), device="cuda")
+    vs = torch.as_tensor(_concat(clouds, "v"), device="cuda")
+    batch = P.BatchedNeighborhoodSearch(searches)
+    batch.initialize(xs.T)
+    counts, rho, acc = _batched(P, clouds, batch, xs, vs)
+    n = xs.shape[0]
+    prs = torch.zeros(n, device="cuda")
+    W = dict(P.workloads.WCSPH)
+    h = [c["radius"] / 2 for c in clouds]
+    batch.foreach_point_neighbor(P.WCSPHDensity(density=rho, pressure=prs,
+                                                velocity=vs.reshape(-1), **dict(W, h=h)), xs.T)
+    counts, rho_h, prs_h = counts.cpu().numpy(), rho.cpu().numpy(), prs.cpu().numpy()
+    acc_h = acc.cpu().numpy().reshape(n, 3)
+    off = 0
+    for c in clouds:
+        m = len(c["x"])
+        x = np.asarray(c["x"], np.float32)
+        v = np.asarray(c["v"], np.float64)
+        r = np.float32(c["radius"])
+        g = O.grid_create(3, r, np.asarray(c["min_corner"], np.float32),
+                          np.asarray(c["max_corner"], np.float32), dtype=np.float32)
+        cl = O.build(g, x)
+        sl = slice(off, off + m)
+        assert np.array_equal(counts[sl], O.foreach(g, cl, x, x, O.F_COUNT))
+        consts = dict(W, h=c["radius"] / 2)
+        prm, keep = O.make_params(**consts)
+        orho, oab = O.foreach(g, cl, x, x, O.F_WCSPH_DENSITY, prm, want_abs=True)
+        assert _rel_err(rho_h[sl].astype(np.float64), orho, oab) < TOL_F32
+        prm, keep = O.make_params(rho=rho_h[sl].astype(np.float64),
+                                  pressure=prs_h[sl].astype(np.float64), vel=v,
+                                  r_min=float(np.sqrt(np.finfo(np.float32).eps)) * consts["h"],
+                                  **consts)
+        oacc, oab = O.foreach(g, cl, x, x, O.F_WCSPH_FORCE, prm, want_abs=True)
+        assert _rel_err(acc_h[sl].astype(np.float64), oacc, oab) < TOL_F32
+        off += m

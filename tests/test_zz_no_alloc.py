@@ -68,14 +68,19 @@ def _cases(pkg):
     x3 = W.perturbed_lattice((30, 30, 30), 0.25, seed=3, dtype=np.float32)      # 27,000
     x2 = W.periodic_nbody_cloud(256, seed=4, dtype=np.float64)[0]              # 65,536
     x3b = W.perturbed_lattice((20, 25, 18), 0.4, seed=5, dtype=np.float64)     # 9,000
+    x1 = W.perturbed_lattice((40000,), 0.04, 0.1, 0.0, seed=6, dtype=np.float64)  # 40,000
+    x3p = np.mod(W.perturbed_lattice((24, 24, 24), 0.3, seed=7, dtype=np.float64) - 0.5,
+                 24.0).astype(np.float32)                                      # 13,824
     return [
         ("3D FP32 r=3", x3, 3, np.float32, 3.0, [-1.0] * 3, [32.0] * 3, False),
         ("2D FP64 periodic r=2.5", x2, 2, np.float64, 2.5, [0.0, 0.0], [256.0, 256.0], True),
         ("3D FP64 r=1.7", x3b, 3, np.float64, 1.7, [0.0] * 3, [27.0] * 3, False),
+        ("1D FP64 r=1.3", x1, 1, np.float64, 1.3, [-1.0], [4001.0], False),
+        ("3D FP32 periodic r=2", x3p, 3, np.float32, 2.0, [0.0] * 3, [24.0] * 3, True),
     ]
 
 
-def test_noalloc_counts_equal_the_handle_entry_points(pkg):
+def test_noalloc_counts_equal_the_handle_entry_points(pkg, O):
     import torch
     L = pkg._lib
     L.load()
@@ -92,6 +97,12 @@ def test_noalloc_counts_equal_the_handle_entry_points(pkg):
         assert rc == 0, (name, L.status_string(rc))
         assert np.array_equal(got, want), name
         assert want.min() >= 1, name  # the point itself is always counted
+        # and both equal the oracle's restatement of the reference's grid search
+        lo_t, hi_t = np.asarray(lo, dt), np.asarray(hi, dt)
+        g = O.grid_create(d, dt(r), lo_t, hi_t, periodic_box=(lo_t, hi_t) if per else None,
+                          dtype=dt)
+        xa = np.ascontiguousarray(x, dtype=dt)
+        assert np.array_equal(got, O.foreach(g, O.build(g, xa), xa, xa, O.F_COUNT)), name
 
 
 def test_noalloc_repeated_calls_allocate_nothing(pkg):
