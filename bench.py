@@ -315,11 +315,12 @@ def run_gpu(args, rank, world, local):
     clocks = sampler.stop() if sampler else None
     # which of update!'s two paths the timed steps took: the device rebuilds when the points
     # that left their cell of the last full build exceed rebuild_fraction of all points
+    # (the points held in overflow lists after the last update!: 0 after a rebuild)
     movers = int(nhs.grid_info()["n_overflow"])
     if hashing:
         update_path = "rebuild (ParallelUpdate)"
     else:
-        update_path = "rebuild" if movers > args.rebuild_fraction * n else "overflow lists"
+        update_path = "overflow lists" if movers > 0 else "rebuild"
     st = P.lib().pn_sync(nhs.handle)
     if st != 0:
         raise RuntimeError(f"timed region reported status {st}")
@@ -524,7 +525,7 @@ def run_gpu(args, rank, world, local):
                    "l2": "working set > L2 (coordinates, sorted copies and outputs ~1 GB), no flush"},
         "update_ms": statistics.median(upd), "density_ms": statistics.median(den),
         "force_ms": statistics.median(frc), "wall_ms_per_step": 1e3 * wall / K,
-        "update_path": update_path, "movers_per_step": movers,
+        "update_path": update_path, "points_in_overflow_lists": movers,
         "rebuild_fraction": None if hashing else args.rebuild_fraction,
         "gpu_launches": int(launches), "launches_per_step": launches / K,
         "roofline": roofline, "fp32_roofline": fp32_roofline, "e2e": e2e, "clocks": clocks,
@@ -750,6 +751,7 @@ def run_gpu_adjoint(args, rank, world, local):
     b_ms = statistics.median(ev[k][1].elapsed_time(ev[k][2]) for k in range(K))
     tot_s = sum(ev[k][0].elapsed_time(ev[k][2]) for k in range(K)) / 1e3
     grad_err = None
+    grad_set_diff = None
     if dt == np.float32:
         # the Float32 gradient against the library's Float64 one on the same points (the
         # Float64 forward/backward agree with the FP64 oracle to 1e-10 in tests/test_adjoint.py)
@@ -765,7 +767,18 @@ def run_gpu_adjoint(args, rank, world, local):
             loss=torch.empty(1, dtype=torch.float64, device="cuda"), **consts), x64, x64, nhs64)
         P.foreach_point_neighbor(P.AdjointLossBackward(grad=g64, reuse_state=True, **consts),
                                  x64, x64, nhs64)
-        grad_err = float((grad.double() - g64).abs().max() / g64.abs().max())
+        # The two searches decide the pairs at d ~ r in their own precision, and the
+        # truncated potential's derivative does not vanish at the cutoff, so a pair in one
+        # set only moves both its points' gradients by ~lambda / r^2: compare the points
+        # whose neighbour counts agree (the rest are reported)
+        c32 = torch.zeros(n, dtype=torch.int32, device="cuda")
+        c64 = torch.zeros(n, dtype=torch.int32, device="cuda")
+        P.foreach_point_neighbor(P.CountNeighbors(c32), xd, xd, nhs)
+        P.foreach_point_neighbor(P.CountNeighbors(c64), x64, x64, nhs64)
+        same = (c32 == c64).repeat_interleave(3)
+        diff = (grad.double() - g64).abs()
+        grad_err = float(diff[same].max() / g64.abs().max())
+        grad_set_diff = int((c32 != c64).sum())
     out = {"metric": f"adjoint pair-evals/s (1M pts, {'FP32' if dt == np.float32 else 'FP64'}, "
                      "r=3, forward loss + backward dL/dx)",
            "value": 2.0 * pairs * K / tot_s, "unit": UNIT, "n_gpus": world, "steps": K,
@@ -778,7 +791,9 @@ def run_gpu_adjoint(args, rank, world, local):
            "forward_ms": f_ms, "backward_ms": b_ms, "backward_over_forward": b_ms / f_ms,
            "grad_rel_err_vs_f64": grad_err,
            "grad_rel_err_definition": "max |dL/dx (FP32) - dL/dx (FP64, this library)| / "
-                                      "max |dL/dx (FP64)| over all 3M components",
+                                      "max |dL/dx (FP64)|, over the points whose neighbour "
+                                      "counts agree between the FP32 and FP64 searches",
+           "points_with_other_neighbour_set": grad_set_diff if dt == np.float32 else None,
            "loss": float(loss.item()),
            "gpu_launches": int(P.lib().pn_launch_count() - launches0), "clocks": clocks,
            "gpu": torch.cuda.get_device_name()}
@@ -1078,7 +1093,7 @@ def extra_records(args, rank, world, local):
 
 def _path_record(o):
     keep = ("metric", "value", "unit", "ms_per_step", "update_ms", "density_ms", "force_ms",
-            "update_path", "movers_per_step", "dtype", "steps", "warmup", "clocks",
+            "update_path", "points_in_overflow_lists", "dtype", "steps", "warmup", "clocks",
             "gpu_launches")
     return {k: o[k] for k in keep if k in o}
 

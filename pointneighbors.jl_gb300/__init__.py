@@ -519,8 +519,11 @@ def copy_neighborhood_search(nhs, search_radius, n_points):
         new_cl = SpatialHashingCellList(cl.ndims, list_size=cl.list_size,
                                         max_points_per_cell=cl.max_points_per_cell)
     else:
+        # copy_cell_list (full_grid.jl:179-185) passes the stored corners -- padded by the
+        # old radius, not at all for a template -- to the constructor, which pads them again
         CT = np.result_type(cl.eltype, T)  # a Float64 cell list stays Float64
-        new_cl = FullGridCellList(min_corner=cl._min.astype(CT), max_corner=cl._max.astype(CT),
+        new_cl = FullGridCellList(min_corner=np.asarray(cl.min_corner).astype(CT),
+                                  max_corner=np.asarray(cl.max_corner).astype(CT),
                                   search_radius=T(search_radius),
                                   max_points_per_cell=cl.max_points_per_cell)
     return GridNeighborhoodSearch(nhs.ndims, search_radius=T(search_radius), n_points=n_points,

@@ -66,10 +66,9 @@ int ensure_capacity(pn_search* s, int64_t n) {
   alloc(&s->d_pos, tb * 4 * slots);
   alloc(&s->d_pa, tb * 4 * slots);
   alloc(&s->d_pb, tb * 4 * slots);
-  if (s->mixed) {
+  if (s->mixed || (s->dtype == PN_FLOAT64 && !s->hashed))
     alloc((void**)&s->d_pos32, sizeof(float) * 4 * slots);
-    alloc((void**)&s->d_pos32lo, sizeof(float) * 4 * slots);
-  }
+  if (s->mixed) alloc((void**)&s->d_pos32lo, sizeof(float) * 4 * slots);
   alloc((void**)&s->d_main_perm, i4 * cap);
   alloc((void**)&s->d_ovf_list, i4 * cap);
   alloc((void**)&s->d_ovf_cell, i4 * cap);
@@ -319,6 +318,7 @@ int pn_abi_version(void) { return PN_ABI_VERSION; }
 unsigned long long pn_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 int pn_fma_probe(float* out, int32_t iters, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_fma_probe");
   if (!out || iters <= 0) return PN_ERR_INVALID_ARG;
   k_fma_probe<<<152 * 8, 256, 0, (cudaStream_t)stream>>>(out, iters);
   count_launch();
@@ -326,23 +326,30 @@ int pn_fma_probe(float* out, int32_t iters, pn_stream_t stream) {
 }
 
 int pn_selftest_bounded_wait(pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_selftest_bounded_wait");
   return selftest_bounded_wait((cudaStream_t)stream);
 }
 
-int pn_create(const pn_config* cfg, pn_search** out) { return create(cfg, 0, out); }
+int pn_create(const pn_config* cfg, pn_search** out) {
+  PN_NVTX_RANGE("pn_create");
+  return create(cfg, 0, out);
+}
 
 int pn_create_spatial_hashing(const pn_config* cfg, int64_t list_size, pn_search** out) {
+  PN_NVTX_RANGE("pn_create_spatial_hashing");
   if (list_size < 1) return PN_ERR_INVALID_ARG;
   return create(cfg, list_size, out);
 }
 
 int pn_create_from_grid(const pn_config* cfg, const int64_t* grid_size, pn_search** out) {
+  PN_NVTX_RANGE("pn_create_from_grid");
   if (!grid_size) return PN_ERR_INVALID_ARG;
   return create(cfg, 0, out, grid_size);
 }
 
 int pn_copy_search(const pn_search* tmpl, double search_radius, int64_t n_points,
                    pn_search** out) {
+  PN_NVTX_RANGE("pn_copy_search");
   if (!tmpl) return PN_ERR_INVALID_ARG;
   pn_config c = tmpl->cfg;
   c.search_radius = search_radius;
@@ -394,6 +401,7 @@ int pn_destroy(pn_search* s) {
 
 int pn_initialize(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
                   int64_t n_eachindex_y, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_initialize");
   if (!s || n_y < 0 || (n_y > 0 && !y) || (eachindex_y && n_eachindex_y < 0))
     return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
@@ -422,6 +430,7 @@ int pn_initialize(pn_search* s, const void* y, int64_t n_y, const int32_t* eachi
 
 int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex_y,
               int64_t n_eachindex_y, int32_t points_moving_y, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_update");
   if (!s) return PN_ERR_INVALID_ARG;
   // update! is a no-op when the neighbour points do not move (nhs_grid.jl:289).
   if (!points_moving_y) return PN_OK;
@@ -447,6 +456,7 @@ int pn_update(pn_search* s, const void* y, int64_t n_y, const int32_t* eachindex
 int pn_foreach_point_neighbor(pn_search* s, int32_t functor, const void* x, int64_t n_x,
                               const void* y, int64_t n_y, const int32_t* points,
                               int64_t n_points, const void* params, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_foreach_point_neighbor");
   if (!s) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   int rc = s->dtype == PN_FLOAT64
@@ -557,6 +567,7 @@ int pn_compute_geometry_from_grid(const pn_config* cfg, const int64_t* grid_size
 }
 
 int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_cell_coords");
   if (!s || n < 0 || (n > 0 && (!x || !out))) return PN_ERR_INVALID_ARG;
   if (s->is_template) return PN_ERR_NOT_INITIALIZED;
   cudaStream_t st = (cudaStream_t)stream;
@@ -566,6 +577,7 @@ int pn_cell_coords(pn_search* s, const void* x, int64_t n, int64_t* out, pn_stre
 }
 
 int pn_export_cells(pn_search* s, int32_t* counts, int32_t* points, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_export_cells");
   if (!s || !counts) return PN_ERR_INVALID_ARG;
   if (!s->initialized) return PN_ERR_NOT_INITIALIZED;
   cudaStream_t st = (cudaStream_t)stream;

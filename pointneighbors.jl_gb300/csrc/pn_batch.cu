@@ -399,6 +399,7 @@ extern "C" {
 
 int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_clouds,
                     pn_batch** out) {
+  PN_NVTX_RANGE("pn_batch_create");
   if (!cfgs || !n_points || !out || n_clouds <= 0) return PN_ERR_INVALID_ARG;
   *out = nullptr;
   pn_batch* b = new (std::nothrow) pn_batch();
@@ -522,6 +523,7 @@ int pn_batch_destroy(pn_batch* b) {
 }
 
 int pn_batch_initialize(pn_batch* b, const void* y, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_batch_initialize");
   if (!b) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   const int rc = rebin(b, static_cast<const float*>(y), st);
@@ -530,6 +532,7 @@ int pn_batch_initialize(pn_batch* b, const void* y, pn_stream_t stream) {
 }
 
 int pn_batch_update(pn_batch* b, const void* y, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_batch_update");
   if (!b) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (!b->initialized) return record(b, PN_ERR_NOT_INITIALIZED, st);
@@ -538,6 +541,7 @@ int pn_batch_update(pn_batch* b, const void* y, pn_stream_t stream) {
 
 int pn_batch_foreach_point_neighbor(pn_batch* b, int32_t functor, const void* y,
                                     const void* params, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_batch_foreach_point_neighbor");
   if (!b) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (!b->initialized) return record(b, PN_ERR_NOT_INITIALIZED, st);
@@ -563,6 +567,7 @@ int pn_batch_foreach_point_neighbor(pn_batch* b, int32_t functor, const void* y,
 
 int pn_batch_autotune(pn_batch* b, int32_t functor, const void* y, const void* params,
                       int32_t reps, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_batch_autotune");
   if (!b || !params || !y || reps <= 0) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   const int kind = kind_of(functor);
@@ -621,6 +626,7 @@ int pn_batch_set_schedule(pn_batch* b, int32_t functor, const pn_batch_schedule*
 }
 
 int pn_batch_capture_step(pn_batch* b, const void* y, const pn_wcsph_params* params) {
+  PN_NVTX_RANGE("pn_batch_capture_step");
   if (!b || !y || !params) return PN_ERR_INVALID_ARG;
   if (!b->initialized) return PN_ERR_NOT_INITIALIZED;
   int rc = prepare_params(b, 1, params);
@@ -660,6 +666,7 @@ int pn_batch_capture_step(pn_batch* b, const void* y, const pn_wcsph_params* par
 }
 
 int pn_batch_launch_step(pn_batch* b, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_batch_launch_step");
   if (!b || !b->exec) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   const int rc = cudaGraphLaunch(b->exec, st) == cudaSuccess ? PN_OK : PN_ERR_CUDA;

@@ -373,6 +373,7 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
               int32_t* __restrict__ err) {
   const int lane = threadIdx.x & 31;
   const int32_t nm = *n_main;
+  int32_t ovf_max = 0;  // the largest overflow list this thread has seen grow
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nm;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = base + threadIdx.x;
@@ -424,7 +425,7 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
         int32_t cb = 0;
         if (lane == leader) {
           cb = atomicAdd(&ovf_counts[cell], __popc(peers));
-          atomicMax(&ovf_n[1], cb + __popc(peers));  // the largest overflow cell so far
+          ovf_max = max(ovf_max, cb + __popc(peers));  // the cell's overflow list so far
         }
         cb = __shfl_sync(peers, cb, leader);
         ovf_list[m] = i;
@@ -433,6 +434,14 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
       }
     }
   }
+  // one atomic per block: the block's loop bounds are uniform, so every thread gets here
+  __shared__ int32_t s_max;
+  if (threadIdx.x == 0) s_max = 0;
+  __syncthreads();
+  const int32_t wmax = __reduce_max_sync(0xffffffffu, ovf_max);
+  if (lane == 0 && wmax > 0) atomicMax(&s_max, wmax);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_max > 0) atomicMax(&ovf_n[1], s_max);
 }
 
 // Movers -> their overflow slots (ovf_start is absolute: it starts after the main slots).
@@ -1142,7 +1151,8 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
 }
 
 // The Float32 split of the cell-sorted coordinates: hi = fl32(x), lo = fl32(x - hi) (x - hi
-// is exact in Float64); vacated slots keep NaN.
+// is exact in Float64; lo only for a mixed-precision search, pos32lo null otherwise);
+// vacated slots keep NaN.
 template <int D>
 __global__ void __launch_bounds__(256)
 k_to_pos32(const double* __restrict__ pos, const int32_t* __restrict__ n_slots,
@@ -1161,13 +1171,15 @@ k_to_pos32(const double* __restrict__ pos, const int32_t* __restrict__ n_slots,
 #pragma unroll
     for (int d = 0; d < S; ++d) {
       pos32[k * S + d] = h[d];
-      pos32lo[k * S + d] = l[d];
+      if (pos32lo != nullptr) pos32lo[k * S + d] = l[d];
     }
   }
 }
 
+// Kept for a mixed-precision search (hi and lo) and for a Float64 one (hi: the Float32
+// traversal that finds its candidates, see Exact64 in pn_traverse.cuh).
 void refresh_pos32(pn_search* s, cudaStream_t st) {
-  if (!s->mixed || s->d_pos32 == nullptr || s->n_binned == 0) return;
+  if (s->d_pos32 == nullptr || s->n_binned == 0) return;
   const int32_t* n_slots = s->ovf_active ? s->d_ovf_start + s->n_total : s->d_start + s->n_total;
   const int64_t n_max = 2 * s->cap;
   const int b = std::max(1, std::min(div_up(n_max, 256), 152 * 8));

@@ -3,6 +3,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdint.h>
 
 #include "../../include/pn_gb300.h"
@@ -53,7 +54,8 @@ struct pn_search {
   void* d_pos = nullptr;           // [2 cap * 4] T
   void* d_pa = nullptr;            // [2 cap * 4] T  WCSPH neighbour state (x, y, z, p/rho^2)
   void* d_pb = nullptr;            // [2 cap * 4] T  WCSPH neighbour state (vx, vy, vz, rho)
-  float* d_pos32 = nullptr;        // [2 cap * 4] PN_FLAG_FLOAT32_SEARCH: pos rounded to Float32
+  float* d_pos32 = nullptr;        // [2 cap * 4] pos rounded to Float32 (mixed precision, and
+                                   // a Float64 FullGridCellList search's Float32 traversal)
   float* d_pos32lo = nullptr;      // [2 cap * 4] and the rest, pos - pos32, rounded to Float32
   int32_t* d_qcount = nullptr;     // [qcount_cap] per-query counts (neighbour lists)
   int64_t qcount_cap = 0;
@@ -123,6 +125,17 @@ struct pn_search {
 
 namespace pn {
 
+// An NVTX range around each entry point that queues device work, named after the entry
+// point, so that a profiler's timeline shows the library's calls (header-only NVTX: without
+// a profiler attached a range costs a call through a no-op pointer).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
+#define PN_NVTX_RANGE(name) ::pn::NvtxRange pn_nvtx_range_(name)
+
 // Spare slots at the end of the slot arrays (candidate scans read up to 7 past a run).
 constexpr int64_t SLOT_PAD = 64;
 
@@ -147,7 +160,8 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st);
 template <typename T>
 int cell_coords(pn_search* s, const T* x, int64_t n, int64_t* out, cudaStream_t st);
 int export_cells(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
-// The Float32 copy of the cell-sorted coordinates of a mixed-precision search (d_pos32).
+// The Float32 copy of the cell-sorted coordinates of a mixed-precision or Float64 search
+// (d_pos32, and d_pos32lo for mixed precision).
 void refresh_pos32(pn_search* s, cudaStream_t st);
 int export_hash_lists(pn_search* s, int32_t* counts, int32_t* points, cudaStream_t st);
 int scan64(pn_search* s, const int32_t* in, int64_t n, int64_t* out, cudaStream_t st);

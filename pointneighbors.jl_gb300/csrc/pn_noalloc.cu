@@ -254,6 +254,7 @@ int count_noalloc(const pn_grid_info& gi, const pn_config& cfg, const T* x, int3
 
 extern "C" int pn_count_neighbors_noalloc(const pn_config* cfg, const void* x, int64_t n,
                                           int32_t* counts, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_count_neighbors_noalloc");
   using namespace pn;
   if (!cfg || n < 0 || (n > 0 && (!x || !counts))) return PN_ERR_INVALID_ARG;
   if (!(cfg->search_radius >= 0.0) || cfg->max_points_per_cell < 0) return PN_ERR_INVALID_ARG;

@@ -229,11 +229,13 @@ static int pre_create(const pn_config* cfg, int64_t list_size, int32_t max_neigh
 }
 
 int pn_pre_create(const pn_config* cfg, int32_t max_neighbors, pn_precomputed** out) {
+  PN_NVTX_RANGE("pn_pre_create");
   return pre_create(cfg, 0, max_neighbors, out);
 }
 
 int pn_pre_create_spatial_hashing(const pn_config* cfg, int64_t list_size,
                                   int32_t max_neighbors, pn_precomputed** out) {
+  PN_NVTX_RANGE("pn_pre_create_spatial_hashing");
   if (list_size < 1) return PN_ERR_INVALID_ARG;
   return pre_create(cfg, list_size, max_neighbors, out);
 }
@@ -252,6 +254,7 @@ int pn_pre_destroy(pn_precomputed* s) {
 int pn_pre_initialize(pn_precomputed* s, const void* x, int64_t n_x, const void* y,
                       int64_t n_y, const int32_t* eachindex_y, int64_t n_eachindex_y,
                       pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_pre_initialize");
   if (!s) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   // "this neighborhood search does not support inactive points" (nhs_precomputed.jl:136)
@@ -267,6 +270,7 @@ int pn_pre_initialize(pn_precomputed* s, const void* x, int64_t n_x, const void*
 int pn_pre_update(pn_precomputed* s, const void* x, int64_t n_x, const void* y, int64_t n_y,
                   const int32_t* eachindex_y, int64_t n_eachindex_y, int32_t points_moving_x,
                   int32_t points_moving_y, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_pre_update");
   if (!s) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (eachindex_y != nullptr && n_eachindex_y != n_y) return record(s, PN_ERR_INVALID_ARG, st);
@@ -284,6 +288,7 @@ int pn_pre_foreach_point_neighbor(pn_precomputed* s, int32_t functor, const void
                                   int64_t n_x, const void* y, int64_t n_y,
                                   const int32_t* points, int64_t n_points, const void* params,
                                   pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_pre_foreach_point_neighbor");
   if (!s) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (!s->built) return record(s, PN_ERR_NOT_INITIALIZED, st);
@@ -299,6 +304,7 @@ int pn_pre_foreach_point_neighbor(pn_precomputed* s, int32_t functor, const void
 
 int pn_pre_neighbor_lists(pn_precomputed* s, int32_t sort, int64_t* offsets, int32_t* neighbors,
                           int64_t capacity, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_pre_neighbor_lists");
   if (!s || !offsets) return PN_ERR_INVALID_ARG;
   cudaStream_t st = (cudaStream_t)stream;
   if (!s->built) return record(s, PN_ERR_NOT_INITIALIZED, st);

@@ -929,6 +929,107 @@ struct MixedFastOf {
   using type = MixedFast<D, F<float, D>>;
 };
 
+// ------------------------------------------------------------------ Float64 via Float32
+// A Float64 search's cell-sorted queries (x is y) are traversed in Float32: over the
+// coordinates rounded to Float32 (d_pos32), with the radius widened past that rounding, so
+// the Float32 candidates hold every Float64 neighbour and few others (a shell of relative
+// width ~1e-4).  Exact64<D, F> then redoes the reference's Float64 geometry and test for
+// each candidate from the Float64 coordinates -- pos_diff = xi - yj, d2 = dot, the periodic
+// image when d2 > r^2, accepted when d2 <= r^2 -- and hands the accepted ones to the
+// Float64 pair function F.  The candidate tests run on the Float32 units; only the
+// neighbours' arithmetic runs on GB300's Float64 units, whose rate is 1/64 of Float32's.
+// Neighbour sets, pos_diff and d2 are the Float64 traversal's exactly.
+struct Exact64Geom {
+  GridDev<double> g;    // the search's Float64 geometry (r^2, periodic box)
+  const double* pos;    // cell-sorted Float64 coordinates
+  const double* state;  // 3D force / adjoint-backward sweeps: candidates and aux, or null
+  int32_t per;          // periodic box
+  int32_t pad_;
+};
+template <class PF>
+struct Exact64Params {
+  PF f;
+  Exact64Geom m;
+};
+
+template <int D, class F>
+struct Exact64 {
+  static constexpr bool kCountOnly = false;  // every candidate is decided in Float64
+  static constexpr bool kInline = false;     // compacted: the pair step is Float64 work
+  static constexpr bool kRowHook = has_row_hook<F>::value;  // a pair cache records F's pairs
+  using Params = Exact64Params<typename F::Params>;  // the same type for every D
+  struct Acc { typename F::Acc f; double x[D]; };
+  static __device__ __forceinline__ Query<double, D> wide(const Query<float, D>& q,
+                                                          const double* x) {
+    Query<double, D> r;
+    r.i = q.i;
+    r.q = q.q;
+    r.k = q.k;
+#pragma unroll
+    for (int k = 0; k < D; ++k) r.x[k] = x[k];
+    return r;
+  }
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
+  static __device__ __forceinline__ void fail(const Params& p, const Query<float, D>& q) {
+    const double z[D] = {};
+    F::fail(p.f, wide(q, z));
+  }
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<float, D>& q) {
+    load_pos<double, D>(p.m.pos, q.k, a.x);
+    F::init(a.f, p.f, wide(q, a.x));
+  }
+  static __device__ __forceinline__ void row_begin(Acc& a, const Params& p,
+                                                   const Query<float, D>& q, int ri, int32_t b0,
+                                                   int32_t e0) {
+    if constexpr (kRowHook) F::row_begin(a.f, p.f, wide(q, a.x), ri, b0, e0);
+  }
+  static __device__ __forceinline__ void no_rows(Acc& a) {
+    if constexpr (kRowHook) F::no_rows(a.f);
+  }
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<float, D>& q,
+                                              int32_t js, const float*, float, float) {
+    double yj[D], pd[D];
+    const double aux = load_cand<double, D>(p.m.state != nullptr ? p.m.state : p.m.pos, js, yj);
+    const double d2 = p.m.per ? pair_geom<double, D, true>(p.m.g, a.x, yj, pd)
+                              : pair_geom<double, D, false>(p.m.g, a.x, yj, pd);
+    if (!(d2 <= p.m.g.r2)) return;
+    F::pair(a.f, p.f, wide(q, a.x), js, pd, d2, aux);
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<float, D>& q) {
+    F::finish(a.f, p.f, wide(q, a.x));
+  }
+};
+
+template <template <typename, int> class F>
+struct Exact64Of {
+  template <typename T, int D>
+  using type = Exact64<D, F<double, D>>;
+};
+
+template <class F>
+struct is_exact64 { static constexpr bool value = false; };
+template <int D, class G>
+struct is_exact64<Exact64<D, G>> { static constexpr bool value = true; };
+
+// The Float64 pair functions that take the Float32 traversal (the others keep the Float64
+// one): those of the WCSPH, n-body, count and adjoint sweeps, with or without a pair cache.
+template <class F>
+struct exact64_ok { static constexpr bool value = false; };
+template <int D>
+struct exact64_ok<FCount<double, D>> { static constexpr bool value = true; };
+template <int D>
+struct exact64_ok<FNBody<double, D>> { static constexpr bool value = true; };
+template <int D>
+struct exact64_ok<FDensity<double, D>> { static constexpr bool value = true; };
+template <int D>
+struct exact64_ok<FForce<double, D>> { static constexpr bool value = true; };
+template <int D>
+struct exact64_ok<FAdjointForward<double, D>> { static constexpr bool value = true; };
+template <int D>
+struct exact64_ok<FAdjointBackward<double, D>> { static constexpr bool value = true; };
+template <int D, class G>
+struct exact64_ok<WithMask<double, D, G>> { static constexpr bool value = exact64_ok<G>::value; };
+
 
 // ------------------------------------------------------------------ candidate scan
 // Candidates are classified without branches.  The exact path (classify, kExact) gives
@@ -1255,8 +1356,16 @@ __device__ __forceinline__ void sorted_query(const TravArgs<T>& a, const typenam
   traverse_query<T, D, PER, F>(a, p, q, c, valid);
 }
 
+// Resident blocks per SM the traversal is compiled for: 8 (64 registers a thread), and 5
+// for the Float64 pair functions behind the Float32 traversal, whose Float64 values take
+// register pairs (and whose sweeps are bound by the Float64 units, not by occupancy).
+template <class F>
+struct trav_blocks { static constexpr int value = 8; };
+template <int D, class G>
+struct trav_blocks<Exact64<D, G>> { static constexpr int value = 5; };
+
 template <typename T, int D, bool PER, class F>
-__global__ void __launch_bounds__(TRAV_THREADS, 8)
+__global__ void __launch_bounds__(TRAV_THREADS, trav_blocks<F>::value)
 k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];

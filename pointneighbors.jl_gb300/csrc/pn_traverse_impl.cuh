@@ -155,7 +155,14 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
   const int key = s->ndims * 2 + (s->periodic ? 1 : 0);
 #define PN_TRAV_CASE(KEY, DD, PP)                                                       \
   case KEY:                                                                             \
-    if constexpr (sorted_only<F<T, DD>>::value) {                                       \
+    if constexpr (is_exact64<F<T, DD>>::value) {                                        \
+      if constexpr (DD >= 2) {                                                          \
+        k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);      \
+        count_launch();                                                                 \
+      } else {                                                                          \
+        return PN_ERR_INVALID_ARG;                                                      \
+      }                                                                                 \
+    } else if constexpr (sorted_only<F<T, DD>>::value) {                                \
       if (a.pc_mask != nullptr)                                                         \
         k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
       else                                                                              \
@@ -198,7 +205,7 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
     default: return PN_ERR_INVALID_ARG;
   }
 #undef PN_TRAV_CASE
-  if constexpr (never_cached<F<T, 1>>::value) {
+  if constexpr (never_cached<F<T, 1>>::value || is_exact64<F<T, 1>>::value) {
     return cuda_status(cudaGetLastError());
   } else if ((a.nb != nullptr || a.pc_mask != nullptr) && a.nb_fallback && sorted) {
     // queries the pair cache or the lists could not hold: the stencil traversal, for
@@ -318,13 +325,27 @@ static MixedGeom mixed_geom(const pn_search* s, TravArgs<double>* a) {
 
 // Launch pair function F: F<T, D> itself, or, with Float32 pair arithmetic over Float64
 // coordinates, Mixed<D, F<float, D>> with the geometry m.
+// Float64 sorted queries without a pair cache to walk take the Float32 traversal `fast64`
+// with Exact64<F> when `g64` is given and F is one of exact64_ok's.
 template <typename T, typename V, template <typename, int> class F>
 static int launch_pair(const pn_search* s, const TravArgs<T>& a, const typename F<V, 1>::Params& p,
                        const MixedGeom& m, bool sorted, int64_t n_launch, cudaStream_t st,
-                       const TravArgs<float>* fast = nullptr) {
+                       const TravArgs<float>* fast = nullptr,
+                       const TravArgs<float>* fast64 = nullptr,
+                       const Exact64Geom* g64 = nullptr) {
   if constexpr (std::is_same<T, V>::value) {
     (void)m;
     (void)fast;
+    if constexpr (std::is_same<T, double>::value && exact64_ok<F<double, 3>>::value) {
+      if (fast64 != nullptr && g64 != nullptr && a.pc_mask == nullptr && sorted &&
+          s->ndims >= 2) {
+        const Exact64Params<typename F<double, 1>::Params> ep{p, *g64};
+        return launch_trav<float, Exact64Of<F>::template type>(s, *fast64, ep, sorted,
+                                                               n_launch, st);
+      }
+    }
+    (void)fast64;
+    (void)g64;
     return launch_trav<T, F>(s, a, p, sorted, n_launch, st);
   } else {
     const MixedParams<typename F<V, 1>::Params> mp{p, m};
@@ -372,6 +393,10 @@ struct TravCall {
   bool fast;               // mixed precision, sorted queries: the Float32 traversal a32
   TravArgs<float> a32;
   const TravArgs<float>* fast_args() const { return fast ? &a32 : nullptr; }
+  bool fast64;             // Float64, sorted queries: the Float32 traversal a32 + Exact64
+  Exact64Geom g64;
+  const TravArgs<float>* fast64_args() const { return fast64 ? &a32 : nullptr; }
+  const Exact64Geom* geom64() const { return fast64 ? &g64 : nullptr; }
 };
 
 // In 3D the WCSPH / adjoint state (x, y, z, aux) has the coordinates' layout: the force and
@@ -384,6 +409,7 @@ static void use_state(const pn_search* s, TravArgs<T>& a, MixedGeom& m, TravCall
   if (s->ndims != 3) return;
   if constexpr (std::is_same<T, V>::value) {
     a.pos = state;
+    if constexpr (std::is_same<T, double>::value) c.g64.state = state;
   } else if (c.fast) {
     c.a32.pos = state;
   } else {
@@ -433,6 +459,15 @@ static int prepare_call(pn_search* s, const T* x, int64_t n_x, const T* y, int64
   c.n_sorted = s->ovf_active ? s->n_binned + s->cap : s->n_binned;
   c.n_launch = c.sorted ? c.n_sorted : c.n_q;
   c.fast = kMixed && c.sorted && lists == nullptr && s->d_pos32 != nullptr && !s->hashed;
+  c.fast64 = false;
+  if constexpr (!kMixed && std::is_same<T, double>::value) {
+    c.fast64 = c.sorted && lists == nullptr && s->d_pos32 != nullptr && !s->hashed;
+    if (c.fast64) {
+      c.a32 = mixed_fast_args(s, c.n_q);  // Float32 coordinates, radius widened past them
+      c.g64 = Exact64Geom{c.a.g, static_cast<const double*>(s->d_pos), nullptr,
+                          s->periodic, 0};
+    }
+  }
   // the pair cache, on the Float32 traversal for a mixed search
   c.cache_on = (!kMixed || c.fast) && (!s->hashed || s->hash_dense) && lists == nullptr &&
                c.sorted && s->pc_cap > 0;
@@ -474,13 +509,13 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
     case PN_F_COUNT: {
       const auto* u = static_cast<const pn_count_params*>(params);
       CountParams<V> p{u->counts, 0};
-      return launch_pair<T, V, FCount>(s, a, p, m, sorted, n_launch, st, c.fast_args());
+      return launch_pair<T, V, FCount>(s, a, p, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
     }
     case PN_F_INDEX_SUM: {
       const auto* u = static_cast<const pn_index_sum_params*>(params);
       IndexSumParams<V> p{u->sums, s->d_perm};
       return launch_pair<T, V, FIndexSum>(s, a, p, m, sorted, n_launch, st,
-                                           c.fast_args());
+                                           c.fast_args(), c.fast64_args(), c.geom64());
     }
     case PN_F_NEIGHBOR_LIST: {
       const auto* u = static_cast<const pn_neighbor_list_params*>(params);
@@ -492,7 +527,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
         counts = s->d_qcount;
       }
       CountParams<V> pc{counts, 1};
-      int rc = launch_pair<T, V, FCount>(s, a, pc, m, sorted, n_launch, st, c.fast_args());
+      int rc = launch_pair<T, V, FCount>(s, a, pc, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
       if (rc != PN_OK) return rc;
       rc = scan64(s, counts, n_q, u->offsets, st);
       if (rc != PN_OK) return rc;
@@ -501,7 +536,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
       if (u->neighbors == nullptr || u->capacity <= 0) return cuda_status(cudaGetLastError());
       k_check_capacity<<<1, 1, 0, st>>>(u->offsets + n_q, u->capacity, s->d_err); count_launch();
       EmitParams<V> pe{u->offsets, u->neighbors, s->d_perm, u->capacity, n_q};
-      rc = launch_pair<T, V, FEmit>(s, a, pe, m, sorted, n_launch, st, c.fast_args());
+      rc = launch_pair<T, V, FEmit>(s, a, pe, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
       if (rc != PN_OK) return rc;
       if (u->sort_rows) rc = sort_rows(s, u->offsets, n_q, u->neighbors, u->capacity, st);
       return rc;
@@ -511,7 +546,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
       const V eps_v = std::numeric_limits<V>::epsilon();
       NBodyParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->G, std::sqrt(eps_v),
                        static_cast<V*>(u->accel)};
-      return launch_pair<T, V, FNBody>(s, a, p, m, sorted, n_launch, st, c.fast_args());
+      return launch_pair<T, V, FNBody>(s, a, p, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
     }
     case PN_F_POTENTIAL: {
       const auto* u = static_cast<const pn_potential_params*>(params);
@@ -519,7 +554,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
       PotentialParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->cutoff,
                            (V)(1.0 / u->cutoff), static_cast<V*>(u->energy)};
       return launch_pair<T, V, FPotential>(s, a, p, m, sorted, n_launch, st,
-                                            c.fast_args());
+                                            c.fast_args(), c.fast64_args(), c.geom64());
     }
     default:
       return foreach_sph<T, V>(s, functor, n_x, params, c, st);

@@ -42,7 +42,16 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
             rc = launch_trav<float, MixedFastOf<FDensityMask>::template type>(
                 s, c.a32, mp, sorted, n_launch, st);
           } else {
-            rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
+            bool via32 = false;  // Float64: the Float32 traversal, each candidate in Float64
+            if constexpr (std::is_same<T, double>::value) {
+              if (c.fast64 && s->ndims >= 2) {
+                const Exact64Params<MaskPairParams<DensityParams<V>>> ep{pp, c.g64};
+                rc = launch_trav<float, Exact64Of<FDensityMask>::template type>(
+                    s, c.a32, ep, sorted, n_launch, st);
+                via32 = true;
+              }
+            }
+            if (!via32) rc = launch_trav<T, FDensityMask>(s, a, pp, sorted, n_launch, st);
           }
         }
         if (rc == PN_OK) {
@@ -51,12 +60,12 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
         }
         done = true;
       }
-      if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st, c.fast_args());
+      if (!done) rc = launch_pair<T, V, FDensity>(s, a, p, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
       if (rc != PN_OK || !step) return rc;
       ForceParams<V> pf{p.c, static_cast<const V*>(s->d_pa), static_cast<const V*>(s->d_pb),
                         static_cast<V*>(u->accel)};
       use_state(s, a, m, c, pf.pa);
-      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st, c.fast_args());
+      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
     }
     case PN_F_WCSPH_FORCE: {
       const auto* u = static_cast<const pn_wcsph_params*>(params);
@@ -79,7 +88,7 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
       }
       ForceParams<V> pf{sph_const<V>(s, u), pa, pb, static_cast<V*>(u->accel)};
       use_state(s, a, m, c, pf.pa);
-      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st, c.fast_args());
+      return launch_pair<T, V, FForce>(s, a, pf, m, sorted, n_launch, st, c.fast_args(), c.fast64_args(), c.geom64());
     }
     case PN_F_ADJOINT_FORWARD:
     case PN_F_ADJOINT_BACKWARD: {
@@ -111,7 +120,16 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
               rc = launch_trav<float, MixedFastOf<FAdjointForwardMask>::template type>(
                   s, c.a32, mp, sorted, n_launch, st);
             } else {
-              rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
+              bool via32 = false;
+              if constexpr (std::is_same<T, double>::value) {
+                if (c.fast64 && s->ndims >= 2) {
+                  const Exact64Params<MaskPairParams<AdjointParams<V>>> ep{pp, c.g64};
+                  rc = launch_trav<float, Exact64Of<FAdjointForwardMask>::template type>(
+                      s, c.a32, ep, sorted, n_launch, st);
+                  via32 = true;
+                }
+              }
+              if (!via32) rc = launch_trav<T, FAdjointForwardMask>(s, a, pp, sorted, n_launch, st);
             }
           }
           if (rc == PN_OK) s->pc_valid = true;
@@ -119,7 +137,7 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
         }
         if (!done)
           rc = launch_pair<T, V, FAdjointForward>(s, a, p, m, sorted, n_launch, st,
-                                                  c.fast_args());
+                                                  c.fast_args(), c.fast64_args(), c.geom64());
         if (rc != PN_OK) return rc;
         k_sum_partials<V><<<SUM_BLOCKS, 256, 0, st>>>(p.terms, n_x, s->d_sum_part); count_launch();
         k_sum_final<<<1, 256, 0, st>>>(s->d_sum_part, SUM_BLOCKS, u->loss); count_launch();
@@ -144,7 +162,7 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
       p.scale = u->grad_scale;
       use_state(s, a, m, c, static_cast<const V*>(p.pa));
       return launch_pair<T, V, FAdjointBackward>(s, a, p, m, sorted, n_launch, st,
-                                                 c.fast_args());
+                                                 c.fast_args(), c.fast64_args(), c.geom64());
     }
     default:
       return PN_ERR_UNSUPPORTED_FUNCTOR;
