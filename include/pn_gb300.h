@@ -373,11 +373,13 @@ int pn_pre_requires_update(const pn_precomputed* s, int32_t out[2]);
  * concatenated in order; outputs are indexed by the same global point index. */
 typedef struct pn_batch pn_batch;
 
-/* Tile schedule of one batched traversal: block size (64, 128 or 256 query slots per
- * tile), tile order (0: cloud order, 1: costliest clouds first, by radius^3), and
- * persistent (1: one wave of blocks pulling tiles from a device queue; 0: one block per
- * tile). */
-typedef struct { int32_t block, order, persistent, pad_; } pn_batch_schedule;
+/* Tile schedule of one batched traversal: block size (64, 128 or 256 threads), tile order
+ * (0: cloud order, 1: costliest clouds first, by radius^3), persistent (1: one wave of
+ * blocks pulling tiles from a device queue; 0: one block per tile), and points per thread
+ * (1 or 2; 0 reads as 1): a tile holds block x points_per_thread consecutive query slots,
+ * which the block walks in rounds of `block`.  (No staging depth: the traversal reads its
+ * candidates through L1 and stages nothing in shared memory.) */
+typedef struct { int32_t block, order, persistent, points_per_thread; } pn_batch_schedule;
 
 int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_clouds,
                     pn_batch** out);
@@ -391,11 +393,28 @@ int pn_batch_update(pn_batch* b, const void* y, pn_stream_t stream);
  * cloud, the array pointers must be the same global arrays for all clouds). */
 int pn_batch_foreach_point_neighbor(pn_batch* b, int32_t functor, const void* y,
                                     const void* params, pn_stream_t stream);
-/* Time every schedule on this batch (reps launches each, CUDA events) and keep the
- * fastest for `functor` (PN_F_COUNT, PN_F_WCSPH_DENSITY or PN_F_WCSPH_FORCE); results do
- * not depend on the schedule. */
+/* Time every schedule (3 blocks x 2 orders x 2 persistence x 2 points per thread) on this
+ * batch (reps launches each, CUDA events) and keep the fastest for `functor` (PN_F_COUNT,
+ * PN_F_WCSPH_DENSITY or PN_F_WCSPH_FORCE); results do not depend on the schedule. */
 int pn_batch_autotune(pn_batch* b, int32_t functor, const void* y, const void* params,
                       int32_t reps, pn_stream_t stream);
+/* The same with a schedule cache file: when `cache_path` holds this batch's key
+ * (pn_batch_tune_key) the cached schedule is taken untimed, else the batch is autotuned and
+ * the winner stored under the key.  The file is text, one line per key:
+ * "<key> <block> <order> <persistent> <points_per_thread> <ms>". */
+int pn_batch_autotune_cached(pn_batch* b, int32_t functor, const void* y, const void* params,
+                             int32_t reps, const char* cache_path, pn_stream_t stream);
+/* The cache key of this batch and pair function: element type and dimension, the clouds'
+ * median radius (steps of 0.25), log2 of the points and of the clouds.  PN_ERR_CAPACITY when
+ * key_size bytes do not hold it. */
+int pn_batch_tune_key(const pn_batch* b, int32_t functor, char* key, int32_t key_size);
+/* Host-only access to a schedule cache file (no device is touched): look a key up
+ * (*found = 1 and *out when present), or store a schedule under it, replacing an older
+ * entry (the file is rewritten through a temporary file and a rename). */
+int pn_tune_cache_lookup(const char* path, const char* key, pn_batch_schedule* out,
+                         int32_t* found);
+int pn_tune_cache_store(const char* path, const char* key, const pn_batch_schedule* sched,
+                        double ms);
 int pn_batch_get_schedule(const pn_batch* b, int32_t functor, pn_batch_schedule* out);
 int pn_batch_set_schedule(pn_batch* b, int32_t functor, const pn_batch_schedule* sched);
 /* Capture update!(y) + WCSPH density + force of every cloud into a CUDA graph (the

@@ -107,7 +107,7 @@ class pn_adjoint_params(C.Structure):
 
 class pn_batch_schedule(C.Structure):
     _fields_ = [("block", C.c_int32), ("order", C.c_int32), ("persistent", C.c_int32),
-                ("pad_", C.c_int32)]
+                ("points_per_thread", C.c_int32)]
 
 
 _P = C.c_void_p
@@ -157,6 +157,12 @@ _SIGNATURES = {
     "pn_batch_update": (C.c_int, [_P, _P, _P]),
     "pn_batch_foreach_point_neighbor": (C.c_int, [_P, C.c_int32, _P, _P, _P]),
     "pn_batch_autotune": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int32, _P]),
+    "pn_batch_autotune_cached": (C.c_int, [_P, C.c_int32, _P, _P, C.c_int32, C.c_char_p, _P]),
+    "pn_batch_tune_key": (C.c_int, [_P, C.c_int32, C.c_char_p, C.c_int32]),
+    "pn_tune_cache_lookup": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(pn_batch_schedule),
+                                       C.POINTER(C.c_int32)]),
+    "pn_tune_cache_store": (C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(pn_batch_schedule),
+                                      C.c_double]),
     "pn_batch_get_schedule": (C.c_int, [_P, C.c_int32, C.POINTER(pn_batch_schedule)]),
     "pn_batch_set_schedule": (C.c_int, [_P, C.c_int32, C.POINTER(pn_batch_schedule)]),
     "pn_batch_capture_step": (C.c_int, [_P, _P, _P]),

@@ -129,24 +129,40 @@ class BatchedNeighborhoodSearch:
                                                            _stream()), check,
                     "foreach_point_neighbor")
 
-    def autotune(self, f, x, reps=3):
-        """Time the 12 tile schedules for `f`'s sweep and keep the fastest; returns it."""
+    def autotune(self, f, x, reps=3, cache=None):
+        """Time the 24 tile schedules for `f`'s sweep and keep the fastest; returns it.  With
+        `cache` (a file path) a schedule stored there for this batch's key is taken untimed,
+        and a newly timed winner is stored."""
         x = self._coords(x)
         p = _batch_params(f, self.searches, x, self.n_total)
         functor = f.functor
-        self._check(lib().pn_batch_autotune(self._h, functor, C.c_void_p(x.data_ptr()), p,
-                                            int(reps), _stream()), True, "autotune")
+        if cache is None:
+            rc = lib().pn_batch_autotune(self._h, functor, C.c_void_p(x.data_ptr()), p,
+                                         int(reps), _stream())
+        else:
+            rc = lib().pn_batch_autotune_cached(self._h, functor, C.c_void_p(x.data_ptr()), p,
+                                                int(reps), str(cache).encode(), _stream())
+        self._check(rc, True, "autotune")
         return self.schedule(functor)
+
+    def tune_key(self, functor):
+        buf = C.create_string_buffer(256)
+        rc = lib().pn_batch_tune_key(self._h, int(functor), buf, 256)
+        if rc != _lib.PN_OK:
+            _raise(rc, "tune_key")
+        return buf.value.decode()
 
     def schedule(self, functor):
         s = _lib.pn_batch_schedule()
         rc = lib().pn_batch_get_schedule(self._h, int(functor), C.byref(s))
         if rc != _lib.PN_OK:
             _raise(rc, "schedule")
-        return {"block": s.block, "order": s.order, "persistent": s.persistent}
+        return {"block": s.block, "order": s.order, "persistent": s.persistent,
+                "points_per_thread": max(1, s.points_per_thread)}
 
-    def set_schedule(self, functor, block, order, persistent):
-        s = _lib.pn_batch_schedule(int(block), int(order), int(persistent), 0)
+    def set_schedule(self, functor, block, order, persistent, points_per_thread=1):
+        s = _lib.pn_batch_schedule(int(block), int(order), int(persistent),
+                                   int(points_per_thread))
         rc = lib().pn_batch_set_schedule(self._h, int(functor), C.byref(s))
         if rc != _lib.PN_OK:
             _raise(rc, "set_schedule")

@@ -15,7 +15,9 @@
 // costliest first (radius^3) so the long ones start early.  No block waits on another.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <limits>
 #include <map>
 #include <new>
@@ -154,7 +156,9 @@ k_trav_batch(const TravArgs<float>* __restrict__ args,
     if (threadIdx.x == 0 && pos_override != nullptr) sa.pos = pos_override;
     __syncthreads();
 
-    const int32_t k = tile.begin + (int32_t)threadIdx.x;
+    // a tile holds points_per_thread rounds of BS consecutive slots (the bound is uniform)
+    for (int32_t k0 = tile.begin; k0 < tile.end; k0 += BS) {
+    const int32_t k = k0 + (int32_t)threadIdx.x;
     Query<float, 3> q;
     bool valid = k < tile.end;
     q.i = valid ? sa.perm[k] : -1;
@@ -172,6 +176,7 @@ k_trav_batch(const TravArgs<float>* __restrict__ args,
       q.x[0] = q.x[1] = q.x[2] = 0.0f;
     }
     traverse_query<float, 3, false, F>(sa, sp, q, c, valid);
+    }
     if (!PERSIST) return;
     __syncthreads();  // the shared copies are re-used by the next tile
   }
@@ -187,14 +192,19 @@ int kind_of(int32_t functor) {
   }
 }
 
+// points_per_thread 0 reads as 1 (the field was padding before it was a dimension)
+int ppt_of(const pn_batch_schedule& s) { return s.points_per_thread == 2 ? 2 : 1; }
+
 bool valid_schedule(const pn_batch_schedule& s) {
   return (s.block == 64 || s.block == 128 || s.block == 256) && (s.order == 0 || s.order == 1) &&
-         (s.persistent == 0 || s.persistent == 1);
+         (s.persistent == 0 || s.persistent == 1) &&
+         (s.points_per_thread >= 0 && s.points_per_thread <= 2);
 }
 
-int tile_key(const pn_batch_schedule& s) { return s.block * 2 + s.order; }
+int tile_key(const pn_batch_schedule& s) { return (s.block * 2 + s.order) * 4 + ppt_of(s); }
 
-// Tiles of `block` slots per cloud, in cloud order or costliest first (radius^3, stable).
+// Tiles of block x points_per_thread slots per cloud, in cloud order or costliest first
+// (radius^3, stable).
 int ensure_tiles(pn_batch* b, const pn_batch_schedule& s) {
   const int key = tile_key(s);
   if (b->d_tiles.count(key)) return PN_OK;
@@ -206,8 +216,9 @@ int ensure_tiles(pn_batch* b, const pn_batch_schedule& s) {
     });
   std::vector<BatchTile> tiles;
   for (int32_t c : order)
-    for (int32_t k = b->pt_off[c]; k < b->pt_off[c + 1]; k += s.block)
-      tiles.push_back({c, k, std::min(k + s.block, b->pt_off[c + 1]), b->cell_off[c]});
+    for (int32_t k = b->pt_off[c]; k < b->pt_off[c + 1]; k += s.block * ppt_of(s))
+      tiles.push_back({c, k, std::min(k + s.block * ppt_of(s), b->pt_off[c + 1]),
+                       b->cell_off[c]});
   BatchTile* d = nullptr;
   if (!tiles.empty()) {
     if (cudaMalloc(&d, sizeof(BatchTile) * tiles.size()) != cudaSuccess) {
@@ -393,6 +404,77 @@ int record(pn_batch* b, int rc, cudaStream_t st) {
 }
 
 }  // namespace
+
+// ------------------------------------------------------------------ schedule cache
+// The autotuner's winners persist in a text file, one line per key:
+//   <key> <block> <order> <persistent> <points_per_thread> <ms>
+// The key names what decides the best schedule -- the pair function, element type and
+// dimension, the clouds' radius (median, in steps of 0.25) and the sizes (log2 of the points
+// and of the clouds) -- so a later batch of the same kind reuses the schedule untimed.
+// Unreadable lines are skipped; a store rewrites the file through a temporary and a rename.
+struct CacheEntry {
+  std::string key;
+  pn_batch_schedule s;
+  double ms;
+};
+
+bool valid_key(const std::string& k) {
+  if (k.empty() || k.size() > 200) return false;
+  for (char c : k)
+    if (c <= ' ' || c > '~') return false;
+  return true;
+}
+
+std::vector<CacheEntry> read_cache(const char* path) {
+  std::vector<CacheEntry> out;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return out;
+  char line[512];
+  while (std::fgets(line, sizeof line, f)) {
+    char key[256];
+    pn_batch_schedule s{};
+    double ms = 0.0;
+    if (std::sscanf(line, "%255s %d %d %d %d %lf", key, &s.block, &s.order, &s.persistent,
+                    &s.points_per_thread, &ms) == 6 &&
+        valid_schedule(s) && valid_key(key))
+      out.push_back(CacheEntry{key, s, ms});
+  }
+  std::fclose(f);
+  return out;
+}
+
+bool write_cache(const char* path, const std::vector<CacheEntry>& es) {
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE* f = std::fopen(tmp.c_str(), "w");
+  if (!f) return false;
+  bool ok = true;
+  for (const auto& e : es)
+    ok = ok && std::fprintf(f, "%s %d %d %d %d %.6f\n", e.key.c_str(), e.s.block, e.s.order,
+                            e.s.persistent, ppt_of(e.s), e.ms) > 0;
+  ok = (std::fclose(f) == 0) && ok;
+  if (ok) ok = std::rename(tmp.c_str(), path) == 0;
+  if (!ok) std::remove(tmp.c_str());
+  return ok;
+}
+
+std::string tune_key(const pn_batch* b, int32_t functor) {
+  std::vector<double> r(b->radius.begin(), b->radius.end());
+  std::sort(r.begin(), r.end());
+  const double med = r.empty() ? 0.0 : r[r.size() / 2];
+  const int64_t n_pts = b->pt_off[b->n_clouds];
+  const char* f = functor == PN_F_COUNT ? "count" : functor == PN_F_WCSPH_DENSITY ? "density"
+                                                                                   : "force";
+  char buf[160];
+  std::snprintf(buf, sizeof buf, "batch/%s/f32/d3/r%.2f/n2^%d/c2^%d", f,
+                std::round(med * 4.0) / 4.0,
+                (int)std::lround(std::log2((double)std::max<int64_t>(n_pts, 1))),
+                (int)std::lround(std::log2((double)std::max(b->n_clouds, 1))));
+  return buf;
+}
+
+int autotune(pn_batch* b, int32_t functor, const void* y, const void* params, int32_t reps,
+             cudaStream_t st, float* best_ms);
+
 }  // namespace pn
 
 extern "C" {
@@ -568,8 +650,76 @@ int pn_batch_foreach_point_neighbor(pn_batch* b, int32_t functor, const void* y,
 int pn_batch_autotune(pn_batch* b, int32_t functor, const void* y, const void* params,
                       int32_t reps, pn_stream_t stream) {
   PN_NVTX_RANGE("pn_batch_autotune");
+  float best = 0.f;
+  return autotune(b, functor, y, params, reps, (cudaStream_t)stream, &best);
+}
+
+int pn_batch_tune_key(const pn_batch* b, int32_t functor, char* key, int32_t key_size) {
+  if (!b || !key || key_size <= 0 || kind_of(functor) < 0) return PN_ERR_INVALID_ARG;
+  const std::string k = tune_key(b, functor);
+  if ((int64_t)k.size() + 1 > key_size) return PN_ERR_CAPACITY;
+  std::memcpy(key, k.c_str(), k.size() + 1);
+  return PN_OK;
+}
+
+int pn_tune_cache_lookup(const char* path, const char* key, pn_batch_schedule* out,
+                         int32_t* found) {
+  if (!path || !key || !out || !found) return PN_ERR_INVALID_ARG;
+  *found = 0;
+  double ms = 0.0;
+  for (const auto& e : read_cache(path))
+    if (e.key == key) {
+      *out = e.s;
+      ms = e.ms;
+      *found = 1;
+    }
+  (void)ms;
+  return PN_OK;
+}
+
+int pn_tune_cache_store(const char* path, const char* key, const pn_batch_schedule* sched,
+                        double ms) {
+  if (!path || !key || !sched || !valid_schedule(*sched) || !valid_key(key))
+    return PN_ERR_INVALID_ARG;
+  std::vector<CacheEntry> es = read_cache(path);
+  bool replaced = false;
+  for (auto& e : es)
+    if (e.key == key) {
+      e.s = *sched;
+      e.ms = ms;
+      replaced = true;
+    }
+  if (!replaced) es.push_back(CacheEntry{key, *sched, ms});
+  return write_cache(path, es) ? PN_OK : PN_ERR_INVALID_ARG;
+}
+
+int pn_batch_autotune_cached(pn_batch* b, int32_t functor, const void* y, const void* params,
+                             int32_t reps, const char* cache_path, pn_stream_t stream) {
+  PN_NVTX_RANGE("pn_batch_autotune_cached");
+  if (!b || !cache_path) return PN_ERR_INVALID_ARG;
+  const int kind = kind_of(functor);
+  if (kind < 0) return PN_ERR_UNSUPPORTED_FUNCTOR;
+  const std::string key = tune_key(b, functor);
+  pn_batch_schedule s{};
+  int32_t found = 0;
+  if (pn_tune_cache_lookup(cache_path, key.c_str(), &s, &found) == PN_OK && found &&
+      valid_schedule(s)) {
+    b->sched[kind] = s;
+    return PN_OK;
+  }
+  float best = 0.f;
+  const int rc = autotune(b, functor, y, params, reps, (cudaStream_t)stream, &best);
+  if (rc != PN_OK) return rc;
+  return pn_tune_cache_store(cache_path, key.c_str(), &b->sched[kind], (double)best);
+}
+
+}  // extern "C"
+
+namespace pn {
+
+int autotune(pn_batch* b, int32_t functor, const void* y, const void* params, int32_t reps,
+             cudaStream_t st, float* best_ms) {
   if (!b || !params || !y || reps <= 0) return PN_ERR_INVALID_ARG;
-  cudaStream_t st = (cudaStream_t)stream;
   const int kind = kind_of(functor);
   if (kind < 0) return record(b, PN_ERR_UNSUPPORTED_FUNCTOR, st);
   if (!b->initialized) return record(b, PN_ERR_NOT_INITIALIZED, st);
@@ -584,8 +734,8 @@ int pn_batch_autotune(pn_batch* b, int32_t functor, const void* y, const void* p
   float best = std::numeric_limits<float>::infinity();
   pn_batch_schedule best_s = b->sched[kind];
   static const int kBlocks[3] = {64, 128, 256};
-  for (int v = 0; v < 12 && rc == PN_OK; ++v) {
-    const pn_batch_schedule s{kBlocks[v / 4], (v / 2) % 2, v % 2, 0};
+  for (int v = 0; v < 24 && rc == PN_OK; ++v) {
+    const pn_batch_schedule s{kBlocks[v / 8], (v / 4) % 2, (v / 2) % 2, 1 + v % 2};
     rc = launch_kind(b, kind, s, kind, st);  // warm-up (and the tiles of this schedule)
     std::vector<float> t;
     for (int r = 0; r < reps && rc == PN_OK; ++r) {
@@ -607,9 +757,16 @@ int pn_batch_autotune(pn_batch* b, int32_t functor, const void* y, const void* p
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (rc == PN_OK) b->sched[kind] = best_s;
+  if (rc == PN_OK) {
+    b->sched[kind] = best_s;
+    *best_ms = best;
+  }
   return record(b, rc, st);
 }
+
+}  // namespace pn
+
+extern "C" {
 
 int pn_batch_get_schedule(const pn_batch* b, int32_t functor, pn_batch_schedule* out) {
   const int kind = kind_of(functor);

@@ -204,7 +204,12 @@ template <typename T> struct EmitParams {
   const int64_t* offsets; int32_t* nbrs; const int32_t* perm; int64_t capacity; int64_t n_rows;
 };
 template <typename T> struct NBodyParams { const T* masses; const int32_t* perm; T G; T sqrt_eps; T* accel; };
-template <typename T> struct PotentialParams { const T* masses; const int32_t* perm; T cutoff, inv_cutoff; T* energy; };
+// cutoff2 = cutoff^2: the truncation 0 < d < cutoff is decided as 0 < d^2 < cutoff^2, the
+// same decision as a correctly rounded square root gives, without depending on the
+// approximate root the pair arithmetic uses
+template <typename T> struct PotentialParams {
+  const T* masses; const int32_t* perm; T cutoff, inv_cutoff; T* energy; T cutoff2;
+};
 
 template <typename T, int D>
 struct FCount {
@@ -428,9 +433,8 @@ struct FPotential {
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T*, T d2, T) {
-    const T r = fsqrt(d2);
-    if (r > (T)0 && r < p.cutoff)
-      a.e += __ldg(&p.masses[__ldg(&p.perm[js])]) * (fdiv((T)1, r) - p.inv_cutoff);
+    if (d2 > (T)0 && d2 < p.cutoff2)
+      a.e += __ldg(&p.masses[__ldg(&p.perm[js])]) * (fdiv((T)1, fsqrt(d2)) - p.inv_cutoff);
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     p.energy[q.i] = a.mi * a.e;
@@ -581,6 +585,7 @@ template <typename T>
 struct AdjointParams {
   SphConst<T> c;         // mass, inv_h, sigma, dw_coef = -5 sigma / h^2
   T cutoff, inv_cutoff, lambda;
+  T cutoff2;             // cutoff^2: the truncation is decided on d^2 (see PotentialParams)
   T* density;            // forward: out, original order
   T* terms;              // forward: out, original order
   T* pa;                 // sorted state (x, y, z, g): forward writes, backward reads
@@ -609,7 +614,7 @@ struct FAdjointForward {
     const T t = fmax((T)1 - (T)0.5 * q, (T)0);
     const T t2 = t * t;
     a.w += t2 * t2 * ((T)2 * q + (T)1);
-    if (r > (T)0 && r < p.cutoff) a.e += fdiv((T)1, r) - p.inv_cutoff;
+    if (d2 > (T)0 && d2 < p.cutoff2) a.e += fdiv((T)1, r) - p.inv_cutoff;
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     const T rho = p.c.mass * p.c.sigma * a.w;
@@ -648,7 +653,7 @@ struct FAdjointBackward {
     const T q = r * p.c.inv_h;
     const T t = fmax((T)1 - (T)0.5 * q, (T)0);
     T s = (a.gk + gj) * p.c.mass * p.c.dw_coef * (t * t * t);
-    if (r < p.cutoff) s -= fdiv(p.lambda * p.c.mass * p.c.mass, d2 * r);
+    if (d2 < p.cutoff2) s -= fdiv(p.lambda * p.c.mass * p.c.mass, d2 * r);
 #pragma unroll
     for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
   }

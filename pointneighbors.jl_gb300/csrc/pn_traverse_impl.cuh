@@ -552,7 +552,7 @@ static int foreach_t(pn_search* s, int32_t functor, const T* x, int64_t n_x, con
       const auto* u = static_cast<const pn_potential_params*>(params);
       if ((const void*)x != (const void*)y) return PN_ERR_INVALID_ARG;
       PotentialParams<V> p{static_cast<const V*>(u->masses), s->d_perm, (V)u->cutoff,
-                           (V)(1.0 / u->cutoff), static_cast<V*>(u->energy)};
+                           (V)(1.0 / u->cutoff), static_cast<V*>(u->energy), (V)u->cutoff * (V)u->cutoff};
       return launch_pair<T, V, FPotential>(s, a, p, m, sorted, n_launch, st,
                                             c.fast_args(), c.fast64_args(), c.geom64());
     }

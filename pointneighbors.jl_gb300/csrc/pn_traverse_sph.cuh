@@ -102,6 +102,7 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
       p.c = sph_const<V>(s, &w);
       p.cutoff = (V)u->cutoff;
       p.inv_cutoff = (V)(1.0 / u->cutoff);
+      p.cutoff2 = p.cutoff * p.cutoff;
       p.lambda = (V)u->lambda_pot;
       p.pa = static_cast<V*>(s->d_pa);
       if (functor == PN_F_ADJOINT_FORWARD) {

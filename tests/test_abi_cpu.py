@@ -317,3 +317,39 @@ def test_periodic_argument_errors(pkg):
                                search_radius=1.0)
     with pytest.raises(P.ArgumentError, match="must cover the periodic box"):
         P.GridNeighborhoodSearch(2, search_radius=1.0, periodic_box=box, cell_list=small)
+
+
+def test_tune_cache_round_trip(L, tmp_path):
+    """The batched autotuner's schedule cache (pn_tune_cache_store / _lookup) on the host:
+    stored schedules come back by key, a store replaces the key's entry, unreadable lines
+    and invalid schedules are ignored or rejected."""
+    lib = L.load()
+    path = str(tmp_path / "schedules.txt").encode()
+    s = L.pn_batch_schedule(256, 1, 0, 2)
+    found = C.c_int32(-1)
+    out = L.pn_batch_schedule()
+    assert lib.pn_tune_cache_lookup(path, b"batch/force/f32/d3/r2.75/n2^24/c2^9", C.byref(out),
+                                    C.byref(found)) == 0 and found.value == 0
+    assert lib.pn_tune_cache_store(path, b"batch/force/f32/d3/r2.75/n2^24/c2^9", C.byref(s),
+                                   3.25) == 0
+    assert lib.pn_tune_cache_store(path, b"batch/density/f32/d3/r2.75/n2^24/c2^9",
+                                   C.byref(L.pn_batch_schedule(64, 0, 1, 1)), 2.5) == 0
+    assert lib.pn_tune_cache_lookup(path, b"batch/force/f32/d3/r2.75/n2^24/c2^9", C.byref(out),
+                                    C.byref(found)) == 0 and found.value == 1
+    assert (out.block, out.order, out.persistent, out.points_per_thread) == (256, 1, 0, 2)
+    # a store replaces the entry of its key and keeps the others
+    assert lib.pn_tune_cache_store(path, b"batch/force/f32/d3/r2.75/n2^24/c2^9",
+                                   C.byref(L.pn_batch_schedule(128, 0, 0, 1)), 1.0) == 0
+    lines = open(path.decode()).read().splitlines()
+    assert len(lines) == 2 and lines[0].startswith("batch/force/") and " 128 0 0 1 " in lines[0]
+    lib.pn_tune_cache_lookup(path, b"batch/density/f32/d3/r2.75/n2^24/c2^9", C.byref(out),
+                             C.byref(found))
+    assert found.value == 1 and (out.block, out.persistent) == (64, 1)
+    # unreadable lines are skipped; invalid schedules and keys are rejected
+    with open(path.decode(), "a") as f:
+        f.write("garbage\nbatch/count 7 0 0 1 1.0\n")
+    lib.pn_tune_cache_lookup(path, b"batch/count", C.byref(out), C.byref(found))
+    assert found.value == 0
+    assert lib.pn_tune_cache_store(path, b"k", C.byref(L.pn_batch_schedule(96, 0, 0, 1)),
+                                   1.0) == L.PN_ERR_INVALID_ARG
+    assert lib.pn_tune_cache_store(path, b"bad key", C.byref(s), 1.0) == L.PN_ERR_INVALID_ARG

@@ -95,14 +95,16 @@ def test_batch_equals_per_cloud_searches(P):
     for block in (64, 128, 256):
         for order in (0, 1):
             for persistent in (0, 1):
-                for fn in (P._lib.PN_F_COUNT, P._lib.PN_F_WCSPH_DENSITY, P._lib.PN_F_WCSPH_FORCE):
-                    batch.set_schedule(fn, block, order, persistent)
-                res = _batched(P, clouds, batch, xs, vs)
-                for a, b in zip(res, want):
-                    assert torch.equal(a, b), (block, order, persistent)
+                for ppt in (1, 2):
+                    for fn in (P._lib.PN_F_COUNT, P._lib.PN_F_WCSPH_DENSITY,
+                               P._lib.PN_F_WCSPH_FORCE):
+                        batch.set_schedule(fn, block, order, persistent, ppt)
+                    res = _batched(P, clouds, batch, xs, vs)
+                    for a, b in zip(res, want):
+                        assert torch.equal(a, b), (block, order, persistent, ppt)
 
 
-def test_batch_update_autotune_and_graph(P):
+def test_batch_update_autotune_and_graph(P, tmp_path):
     clouds = _clouds(P, n_clouds=40, seed=5)
     searches = _searches(P, clouds)
     x0 = torch.as_tensor(_concat(clouds, "x"), device="cuda")
@@ -117,11 +119,18 @@ def test_batch_update_autotune_and_graph(P):
     h = [c["radius"] / 2 for c in clouds]
     step = P.WCSPHStep(density=rho, pressure=prs, velocity=vs.reshape(-1), accel=acc,
                        **dict(W, h=h))
+    cache = tmp_path / "schedules.txt"
     for f in (P.WCSPHDensity(density=rho, pressure=prs, velocity=vs.reshape(-1), **dict(W, h=h)),
               P.WCSPHForce(density=rho, pressure=prs, velocity=vs.reshape(-1), accel=acc,
                            reuse_state=True, **dict(W, h=h))):
-        sched = batch.autotune(f, x1.T, reps=2)
-        assert sched["block"] in (64, 128, 256)
+        sched = batch.autotune(f, x1.T, reps=2, cache=cache)
+        assert sched["block"] in (64, 128, 256) and sched["points_per_thread"] in (1, 2)
+        # a second batch of the same kind takes the stored schedule untimed
+        other = P.BatchedNeighborhoodSearch(searches)
+        other.initialize(x1.T)
+        other.set_schedule(f.functor, 64, 0, 0, 1)
+        assert other.autotune(f, x1.T, reps=2, cache=cache) == sched
+        assert batch.tune_key(f.functor) in cache.read_text()
     got = _batched(P, clouds, batch, x1, vs)
     assert torch.equal(got[1], want[1]) and torch.equal(got[2], want[2])
     # the captured graph: update!(xbuf) + density + force, replayed after xbuf moved
