@@ -178,6 +178,22 @@ __device__ __forceinline__ uint64_t mul_f32x2(uint64_t a, uint64_t b) {
   asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
   return r;
 }
+__device__ __forceinline__ uint64_t fma_f32x2(uint64_t a, uint64_t b, uint64_t c) {
+  uint64_t r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+
+// Candidate groups: an inline pair function that needs only d^2 (the WCSPH density) takes
+// the candidates of a stencil run GROUP at a time: their exact d^2 and a word of the
+// accepted ones, and it accumulates its contribution over the whole group without a
+// branch, so the lanes of a warp stay converged while their runs differ in length.
+constexpr int GROUP = 4;
+
+template <class F, class = void>
+struct has_group { static constexpr bool value = false; };
+template <class F>
+struct has_group<F, decltype((void)F::kGroup)> { static constexpr bool value = F::kGroup; };
 
 // Pair-function math (only the sums are compared with the FP64 oracle, within tolerance):
 // FP32 uses the approximate hardware square root and divide; FP64 stays IEEE.
@@ -381,6 +397,15 @@ struct WithMask {
     if (off < 64) a.lo |= 1ull << off;
     else if (off < 128) a.hi |= 1ull << (off - 64);
   }
+  // a group of GROUP candidates from slot js0 (a multiple of GROUP past the row's start)
+  static constexpr bool kGroup = has_group<F>::value;
+  static __device__ __forceinline__ void group(Acc& a, const Params& p, const Query<T, D>& q,
+                                               int32_t js0, const float* d2, uint32_t hits) {
+    F::group(a.f, p.f, q, js0, d2, hits);
+    const uint32_t off = (uint32_t)(js0 - a.b0);
+    if (off < 64) a.lo |= (uint64_t)hits << off;
+    else if (off < 128) a.hi |= (uint64_t)hits << (off - 64);
+  }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     F::finish(a.f, p.f, q);
     flush(a, p, q);
@@ -497,15 +522,39 @@ struct FDensity {
   static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
   struct Acc { T w; };
   static __device__ __forceinline__ void init(Acc& a, const Params&, const Query<T, D>&) { a.w = (T)0; }
+  // Every operation explicitly rounded (or an explicit fma), so that group()'s packed form
+  // gives the same bits: a density does not depend on whether its pairs were found by the
+  // stencil or walked from the pair cache.
   static __device__ __forceinline__ T kernel(const Params& p, T d2) {
-    const T q = fsqrt(d2) * p.c.inv_h;
-    const T t = fmax((T)1 - (T)0.5 * q, (T)0);  // zero beyond the support 2h
-    const T t2 = t * t;
-    return t2 * t2 * ((T)2 * q + (T)1);
+    const T q = xmul(fsqrt(d2), p.c.inv_h);
+    const T t = fmax(fma(q, (T)-0.5, (T)1), (T)0);  // zero beyond the support 2h
+    const T t2 = xmul(t, t);
+    return xmul(xmul(t2, t2), fma(q, (T)2, (T)1));
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t,
                                               const T*, T d2, T) {
-    a.w += kernel(p, d2);
+    a.w = xadd(a.w, kernel(p, d2));
+  }
+  // Float32 groups: the kernel of GROUP candidates two per packed instruction, then added in
+  // candidate order, a rejected candidate adding an exact zero: pair()'s sum bit for bit.
+  static constexpr bool kGroup = sizeof(T) == 4;
+  static __device__ __forceinline__ void group(Acc& a, const Params& p, const Query<T, D>&,
+                                               int32_t, const float* d2, uint32_t hits) {
+    const uint64_t inv_h = pack_f32x2(p.c.inv_h, p.c.inv_h);
+    const uint64_t m_half = pack_f32x2(-0.5f, -0.5f), one = pack_f32x2(1.0f, 1.0f);
+    const uint64_t two = pack_f32x2(2.0f, 2.0f);
+#pragma unroll
+    for (int u = 0; u < GROUP; u += 2) {
+      const uint64_t q = mul_f32x2(pack_f32x2(fsqrt(d2[u]), fsqrt(d2[u + 1])), inv_h);
+      float t0, t1;
+      unpack_f32x2(fma_f32x2(q, m_half, one), t0, t1);
+      const uint64_t t = pack_f32x2(fmaxf(t0, 0.0f), fmaxf(t1, 0.0f));
+      const uint64_t t2 = mul_f32x2(t, t);
+      float w0, w1;
+      unpack_f32x2(mul_f32x2(mul_f32x2(t2, t2), fma_f32x2(q, two, one)), w0, w1);
+      a.w = xadd(a.w, (hits >> u) & 1u ? (T)w0 : (T)0);
+      a.w = xadd(a.w, (hits >> (u + 1)) & 1u ? (T)w1 : (T)0);
+    }
   }
 
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
@@ -551,9 +600,11 @@ struct FForce {
   }
   // In 3D the traversal reads the candidates from the state (x, y, z, p/rho^2), and `aux`
   // is the candidate's p/rho^2; otherwise it is loaded here.
+  // Without branches: every term is finite for any accepted pair (d2 + eps h^2 > 0, the
+  // density sum > 0), and the pairs closer than r_min (the point itself) contribute an
+  // exact zero through the final select.
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T* pd, T d2, T aux) {
-    if (d2 < p.c.r_min2) return;
     const T Pj = D == 3 ? aux : load4(p.pa, js).w;
     const V4<T> sb = load4(p.pb, js);
     const T vj[3] = {sb.x, sb.y, sb.z};
@@ -565,8 +616,10 @@ struct FForce {
     for (int k = 0; k < D; ++k) vr += (a.vi[k] - vj[k]) * pd[k];
     // Monaghan: Pi = -alpha c0 mu / rho_mean for approaching pairs (v.x < 0), else 0
     const T mu = fdiv(p.c.h * vr, d2 + p.c.eps_h2);
-    const T visc = vr < (T)0 ? fdiv(-p.c.alpha * p.c.c0 * mu, (T)0.5 * (a.rhoi + sb.w)) : (T)0;
-    const T s = -p.c.mass * (a.Pi + Pj + visc) * gw;
+    const T pi_ij = fdiv(-p.c.alpha * p.c.c0 * mu, (T)0.5 * (a.rhoi + sb.w));
+    const T visc = vr < (T)0 ? pi_ij : (T)0;
+    T s = -p.c.mass * (a.Pi + Pj + visc) * gw;
+    s = d2 < p.c.r_min2 ? (T)0 : s;
 #pragma unroll
     for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
   }
@@ -1168,7 +1221,30 @@ __device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F:
   if constexpr (F::kInline) {
     // one candidate at a time with the exact test and the pair function applied in place
     // on the registers just loaded (a cheap pair function needs no compaction)
-    if constexpr (sizeof(T) == 4 && D == 3 && !WRAP) {
+    if constexpr (sizeof(T) == 4 && D == 3 && !WRAP && has_group<F>::value) {
+      // GROUP candidates per step, each d^2 formed exactly as in the loop below; the last
+      // group reads up to GROUP - 1 slots past the run (the slot arrays' padding holds
+      // them) and masks them off
+      const uint64_t qxy = pack_f32x2(q.x[0], q.x[1]);
+      const float r2 = a.g.r2;
+      const int32_t n = end - beg;
+      for (int32_t e = 0; e < n; e += GROUP) {
+        float d2[GROUP];
+        uint32_t hits = 0u;
+#pragma unroll
+        for (int u = 0; u < GROUP; ++u) {
+          const float4 cj = __ldg(reinterpret_cast<const float4*>(a.pos) + beg + e + u);
+          const uint64_t dxy = sub_f32x2(qxy, pack_f32x2(cj.x, cj.y));
+          float sx, sy;
+          unpack_f32x2(mul_f32x2(dxy, dxy), sx, sy);
+          const float dz = __fsub_rn(q.x[2], cj.z);
+          d2[u] = __fadd_rn(__fadd_rn(sx, sy), __fmul_rn(dz, dz));
+          hits |= d2[u] <= r2 ? 1u << u : 0u;  // false for NaN (vacated slots)
+        }
+        if (n - e < GROUP) hits &= (1u << (n - e)) - 1u;
+        F::group(acc, p, q, beg + e, d2, hits);
+      }
+    } else if constexpr (sizeof(T) == 4 && D == 3 && !WRAP) {
       // the x and y differences and squares as packed pairs (sub/mul.rn.f32x2: the same
       // correctly rounded operations as the scalar exact form, two per instruction)
       const uint64_t qxy = pack_f32x2(q.x[0], q.x[1]);
@@ -1633,43 +1709,48 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   typename F::Acc acc;
   F::init(acc, p, q);
   constexpr int NR = D == 3 ? 9 : (D == 2 ? 3 : 1);
-  // One loop over all the query's neighbours (row by row, low then high word): a lane moves
-  // to its next mask word when it has used up the current one, so lanes with different
-  // counts per row do not wait for one another row by row.
-  // wi = 2 row + half indexes the query's 2 NR mask words.  The next row's start and mask
-  // are loaded when a row is entered, so a lane that moves to the next row finds them in
-  // registers instead of stalling its warp on the load.
+  // One loop over all the query's neighbours (row by row, word by word): a lane moves to
+  // its next mask word when it has used up the current one, so lanes with different counts
+  // per row do not wait for one another row by row.  The mask is walked in 32-bit words
+  // (wi = 4 row + word): a word's lowest set bit and its removal are single 32-bit
+  // operations; the row's remaining words shift down (m.x <- m.y <- m.z <- m.w).  The next
+  // row's start and mask are loaded when a row is entered, so a lane that moves to the next
+  // row finds them in registers instead of stalling its warp on the load.
+  const uint4* masks = reinterpret_cast<const uint4*>(a.pc_mask);
   int wi = 0;
   int32_t rb0 = __ldg(&a.pc_b0[k]);
-  ulonglong2 m = __ldg(&a.pc_mask[k]);
+  uint4 m = __ldg(&masks[k]);
   int32_t nb0 = 0;
-  ulonglong2 nm = make_ulonglong2(0ull, 0ull);
+  uint4 nm = make_uint4(0u, 0u, 0u, 0u);
   if (NR > 1) {
     nb0 = __ldg(&a.pc_b0[a.pc_stride + k]);
-    nm = __ldg(&a.pc_mask[a.pc_stride + k]);
+    nm = __ldg(&masks[a.pc_stride + k]);
   }
-  uint64_t w = m.x;
+  uint32_t w = m.x;
   for (;;) {
     while (w == 0) {
-      if (++wi >= 2 * NR) break;
-      if (wi & 1) {
-        w = m.y;
+      if (++wi >= 4 * NR) break;
+      if (wi & 3) {
+        m.x = m.y;
+        m.y = m.z;
+        m.z = m.w;
+        w = m.x;
       } else {
         rb0 = nb0;
         m = nm;
         w = m.x;
-        const int nr = (wi >> 1) + 1;
+        const int nr = (wi >> 2) + 1;
         if (nr < NR) {
           const int64_t o = (int64_t)nr * a.pc_stride + k;
           nb0 = __ldg(&a.pc_b0[o]);
-          nm = __ldg(&a.pc_mask[o]);
+          nm = __ldg(&masks[o]);
         }
       }
     }
     if (w == 0) break;
-    const int e = __ffsll((long long)w) - 1;
+    const int e = __ffs(w) - 1;
     w &= w - 1;
-    const int32_t js = rb0 + 64 * (wi & 1) + e;
+    const int32_t js = rb0 + 32 * (wi & 3) + e;
     T yj[D], pd[D];
     const T aux = load_cand<T, D>(a.pos, js, yj);
     const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
