@@ -185,9 +185,10 @@ __device__ __forceinline__ uint64_t fma_f32x2(uint64_t a, uint64_t b, uint64_t c
 }
 
 // Candidate groups: an inline pair function that needs only d^2 (the WCSPH density) takes
-// the candidates of a stencil run GROUP at a time: their exact d^2 and a word of the
-// accepted ones, and it accumulates its contribution over the whole group without a
-// branch, so the lanes of a warp stay converged while their runs differ in length.
+// the candidates of a stencil run GROUP at a time, with their exact d^2 (the accepted ones
+// are those with d^2 <= r^2), and it accumulates its contribution over the whole group
+// without a branch, so the lanes of a warp stay converged while their runs differ in
+// length.
 constexpr int GROUP = 4;
 
 template <class F, class = void>
@@ -397,11 +398,15 @@ struct WithMask {
     if (off < 64) a.lo |= 1ull << off;
     else if (off < 128) a.hi |= 1ull << (off - 64);
   }
-  // a group of GROUP candidates from slot js0 (a multiple of GROUP past the row's start)
+  // a group of GROUP candidates from slot js0 (a multiple of GROUP past the row's start);
+  // the accepted ones are those with d2[u] <= r2
   static constexpr bool kGroup = has_group<F>::value;
   static __device__ __forceinline__ void group(Acc& a, const Params& p, const Query<T, D>& q,
-                                               int32_t js0, const float* d2, uint32_t hits) {
-    F::group(a.f, p.f, q, js0, d2, hits);
+                                               int32_t js0, const float* d2, float r2) {
+    F::group(a.f, p.f, q, js0, d2, r2);
+    uint32_t hits = 0u;
+#pragma unroll
+    for (int u = 0; u < GROUP; ++u) hits |= d2[u] <= r2 ? 1u << u : 0u;
     const uint32_t off = (uint32_t)(js0 - a.b0);
     if (off < 64) a.lo |= (uint64_t)hits << off;
     else if (off < 128) a.hi |= (uint64_t)hits << (off - 64);
@@ -539,7 +544,7 @@ struct FDensity {
   // candidate order, a rejected candidate adding an exact zero: pair()'s sum bit for bit.
   static constexpr bool kGroup = sizeof(T) == 4;
   static __device__ __forceinline__ void group(Acc& a, const Params& p, const Query<T, D>&,
-                                               int32_t, const float* d2, uint32_t hits) {
+                                               int32_t, const float* d2, float r2) {
     const uint64_t inv_h = pack_f32x2(p.c.inv_h, p.c.inv_h);
     const uint64_t m_half = pack_f32x2(-0.5f, -0.5f), one = pack_f32x2(1.0f, 1.0f);
     const uint64_t two = pack_f32x2(2.0f, 2.0f);
@@ -552,8 +557,8 @@ struct FDensity {
       const uint64_t t2 = mul_f32x2(t, t);
       float w0, w1;
       unpack_f32x2(mul_f32x2(mul_f32x2(t2, t2), fma_f32x2(q, two, one)), w0, w1);
-      a.w = xadd(a.w, (hits >> u) & 1u ? (T)w0 : (T)0);
-      a.w = xadd(a.w, (hits >> (u + 1)) & 1u ? (T)w1 : (T)0);
+      a.w = xadd(a.w, d2[u] <= r2 ? (T)w0 : (T)0);  // false for NaN and the tail's +inf
+      a.w = xadd(a.w, d2[u + 1] <= r2 ? (T)w1 : (T)0);
     }
   }
 
@@ -600,11 +605,9 @@ struct FForce {
   }
   // In 3D the traversal reads the candidates from the state (x, y, z, p/rho^2), and `aux`
   // is the candidate's p/rho^2; otherwise it is loaded here.
-  // Without branches: every term is finite for any accepted pair (d2 + eps h^2 > 0, the
-  // density sum > 0), and the pairs closer than r_min (the point itself) contribute an
-  // exact zero through the final select.
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T* pd, T d2, T aux) {
+    if (d2 < p.c.r_min2) return;
     const T Pj = D == 3 ? aux : load4(p.pa, js).w;
     const V4<T> sb = load4(p.pb, js);
     const T vj[3] = {sb.x, sb.y, sb.z};
@@ -616,10 +619,8 @@ struct FForce {
     for (int k = 0; k < D; ++k) vr += (a.vi[k] - vj[k]) * pd[k];
     // Monaghan: Pi = -alpha c0 mu / rho_mean for approaching pairs (v.x < 0), else 0
     const T mu = fdiv(p.c.h * vr, d2 + p.c.eps_h2);
-    const T pi_ij = fdiv(-p.c.alpha * p.c.c0 * mu, (T)0.5 * (a.rhoi + sb.w));
-    const T visc = vr < (T)0 ? pi_ij : (T)0;
-    T s = -p.c.mass * (a.Pi + Pj + visc) * gw;
-    s = d2 < p.c.r_min2 ? (T)0 : s;
+    const T visc = vr < (T)0 ? fdiv(-p.c.alpha * p.c.c0 * mu, (T)0.5 * (a.rhoi + sb.w)) : (T)0;
+    const T s = -p.c.mass * (a.Pi + Pj + visc) * gw;
 #pragma unroll
     for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
   }
@@ -1230,19 +1231,22 @@ __device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F:
       const int32_t n = end - beg;
       for (int32_t e = 0; e < n; e += GROUP) {
         float d2[GROUP];
-        uint32_t hits = 0u;
+        const float4* cg = reinterpret_cast<const float4*>(a.pos) + beg + e;
 #pragma unroll
         for (int u = 0; u < GROUP; ++u) {
-          const float4 cj = __ldg(reinterpret_cast<const float4*>(a.pos) + beg + e + u);
+          const float4 cj = __ldg(cg + u);
           const uint64_t dxy = sub_f32x2(qxy, pack_f32x2(cj.x, cj.y));
           float sx, sy;
           unpack_f32x2(mul_f32x2(dxy, dxy), sx, sy);
           const float dz = __fsub_rn(q.x[2], cj.z);
           d2[u] = __fadd_rn(__fadd_rn(sx, sy), __fmul_rn(dz, dz));
-          hits |= d2[u] <= r2 ? 1u << u : 0u;  // false for NaN (vacated slots)
         }
-        if (n - e < GROUP) hits &= (1u << (n - e)) - 1u;
-        F::group(acc, p, q, beg + e, d2, hits);
+        if (n - e < GROUP) {  // the last group: the slots past the run are never accepted
+#pragma unroll
+          for (int u = 1; u < GROUP; ++u)
+            if (u >= n - e) d2[u] = __int_as_float(0x7f800000);
+        }
+        F::group(acc, p, q, beg + e, d2, r2);  // accepted: d2 <= r2 (false for NaN)
       }
     } else if constexpr (sizeof(T) == 4 && D == 3 && !WRAP) {
       // the x and y differences and squares as packed pairs (sub/mul.rn.f32x2: the same
@@ -1709,48 +1713,43 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   typename F::Acc acc;
   F::init(acc, p, q);
   constexpr int NR = D == 3 ? 9 : (D == 2 ? 3 : 1);
-  // One loop over all the query's neighbours (row by row, word by word): a lane moves to
-  // its next mask word when it has used up the current one, so lanes with different counts
-  // per row do not wait for one another row by row.  The mask is walked in 32-bit words
-  // (wi = 4 row + word): a word's lowest set bit and its removal are single 32-bit
-  // operations; the row's remaining words shift down (m.x <- m.y <- m.z <- m.w).  The next
-  // row's start and mask are loaded when a row is entered, so a lane that moves to the next
-  // row finds them in registers instead of stalling its warp on the load.
-  const uint4* masks = reinterpret_cast<const uint4*>(a.pc_mask);
+  // One loop over all the query's neighbours (row by row, low then high word): a lane moves
+  // to its next mask word when it has used up the current one, so lanes with different
+  // counts per row do not wait for one another row by row.
+  // wi = 2 row + half indexes the query's 2 NR mask words.  The next row's start and mask
+  // are loaded when a row is entered, so a lane that moves to the next row finds them in
+  // registers instead of stalling its warp on the load.
   int wi = 0;
   int32_t rb0 = __ldg(&a.pc_b0[k]);
-  uint4 m = __ldg(&masks[k]);
+  ulonglong2 m = __ldg(&a.pc_mask[k]);
   int32_t nb0 = 0;
-  uint4 nm = make_uint4(0u, 0u, 0u, 0u);
+  ulonglong2 nm = make_ulonglong2(0ull, 0ull);
   if (NR > 1) {
     nb0 = __ldg(&a.pc_b0[a.pc_stride + k]);
-    nm = __ldg(&masks[a.pc_stride + k]);
+    nm = __ldg(&a.pc_mask[a.pc_stride + k]);
   }
-  uint32_t w = m.x;
+  uint64_t w = m.x;
   for (;;) {
     while (w == 0) {
-      if (++wi >= 4 * NR) break;
-      if (wi & 3) {
-        m.x = m.y;
-        m.y = m.z;
-        m.z = m.w;
-        w = m.x;
+      if (++wi >= 2 * NR) break;
+      if (wi & 1) {
+        w = m.y;
       } else {
         rb0 = nb0;
         m = nm;
         w = m.x;
-        const int nr = (wi >> 2) + 1;
+        const int nr = (wi >> 1) + 1;
         if (nr < NR) {
           const int64_t o = (int64_t)nr * a.pc_stride + k;
           nb0 = __ldg(&a.pc_b0[o]);
-          nm = __ldg(&masks[o]);
+          nm = __ldg(&a.pc_mask[o]);
         }
       }
     }
     if (w == 0) break;
-    const int e = __ffs(w) - 1;
+    const int e = __ffsll((long long)w) - 1;
     w &= w - 1;
-    const int32_t js = rb0 + 32 * (wi & 3) + e;
+    const int32_t js = rb0 + 64 * (wi & 1) + e;
     T yj[D], pd[D];
     const T aux = load_cand<T, D>(a.pos, js, yj);
     const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
