@@ -502,8 +502,10 @@ def run_gpu(args, rank, world, local):
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = cpu_baseline(x1, v, args, dt)
 
+    metric = METRIC if args.dtype == "float32" else METRIC.replace(
+        "FP32", "FP64" if args.dtype == "float64" else "FP64 coordinates, FP32 radius")
     out = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
+        "metric": metric, "value": value, "unit": UNIT, "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": 1e3 * max_s / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None,
         "dtype": {"float32": "f32", "float64": "f64",
