@@ -51,8 +51,10 @@ typedef enum {
   PN_ERR_BOUNDS = 9,         /* a query point whose neighbouring cells are outside the grid
                                 (the reference's BoundsError in points_in_cell)             */
   PN_ERR_CAPACITY = 10,      /* neighbour-list output buffer too small                      */
-  PN_ERR_SCRATCH_LIMIT = 11  /* problem larger than pn_count_neighbors_noalloc's fixed
+  PN_ERR_SCRATCH_LIMIT = 11, /* problem larger than pn_count_neighbors_noalloc's fixed
                                 scratch (PN_NOALLOC_SCRATCH_BYTES)                          */
+  PN_ERR_INDEX = 12          /* a device index out of range (bounds-checked library only,
+                                see pn_bounds_failure)                                      */
 } pn_status;
 
 typedef enum { PN_FLOAT32 = 0, PN_FLOAT64 = 1 } pn_dtype;
@@ -459,6 +461,17 @@ int pn_abi_version(void);
 
 /* Number of CUDA kernels the library has launched in this process (all searches). */
 unsigned long long pn_launch_count(void);
+
+/* Bounds-checked build (libpn_gb300_bc.so, compiled with -DPN_BOUNDS_CHECK): every device
+ * index of the cell-list build and of the traversals is checked before it reaches memory
+ * (cell indices, slots, candidate runs, point indices read from the permutation, pair-cache
+ * entries); the first index out of range sets PN_ERR_INDEX and the access goes to element 0
+ * instead.  pn_build_flags() has bit 0 set in that build.  pn_bounds_failure reports the
+ * first failure of a search: site (1 query slot, 2 cell, 3 candidate run, 4 point index,
+ * 5 pair-cache entry, 6 slot written by the build, 7 neighbour slot of the pair cache; 0
+ * none) and the index, truncated to 32 bits. */
+int32_t pn_build_flags(void);
+int pn_bounds_failure(pn_search* s, int32_t* site, int32_t* index);
 
 /* Measurement aid (no counterpart in the reference): one launch of a kernel whose every
  * thread runs `iters` rounds of 8 independent Float32 FMA chains (152 x 8 blocks of 256

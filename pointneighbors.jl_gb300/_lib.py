@@ -10,7 +10,9 @@ import ctypes as C
 import os
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libpn_gb300.so")
+# PN_GB300_LIB names another build of the library (the bounds-checked
+# _build/libpn_gb300_bc.so, for instance); by default the in-tree libpn_gb300.so.
+LIB_PATH = os.environ.get("PN_GB300_LIB") or os.path.join(HERE, "_build", "libpn_gb300.so")
 
 PN_OK = 0
 PN_ERR_OUT_OF_DOMAIN = 1
@@ -24,6 +26,7 @@ PN_ERR_OUT_OF_MEMORY = 8
 PN_ERR_BOUNDS = 9
 PN_ERR_CAPACITY = 10
 PN_ERR_SCRATCH_LIMIT = 11
+PN_ERR_INDEX = 12
 PN_NOALLOC_SCRATCH_BYTES = 4 * 1024 * 1024
 PN_FMA_PROBE_THREADS = 152 * 8 * 256
 
@@ -114,6 +117,8 @@ _P = C.c_void_p
 _SIGNATURES = {
     "pn_abi_version": (C.c_int, []),
     "pn_launch_count": (C.c_ulonglong, []),
+    "pn_build_flags": (C.c_int32, []),
+    "pn_bounds_failure": (C.c_int, [_P, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "pn_fma_probe": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "pn_selftest_bounded_wait": (C.c_int, [C.c_void_p]),
     "pn_create": (C.c_int, [C.POINTER(pn_config), C.POINTER(_P)]),

@@ -17,6 +17,9 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libpn_gb300.so")
+# the bounds-checked variant (-DPN_BOUNDS_CHECK), built on request into its own folder
+BC_DIR = os.path.join(OUT_DIR, "bounds_check")
+LIB_BC = os.path.join(OUT_DIR, "libpn_gb300_bc.so")
 SOURCES = ["pn_api.cu", "pn_build.cu", "pn_traverse_f32.cu", "pn_traverse_f64.cu",
            "pn_traverse_mixed.cu", "pn_traverse_mixed_lists.cu", "pn_traverse_f32_sph.cu",
            "pn_traverse_f64_sph.cu", "pn_traverse_mixed_sph.cu", "pn_noalloc.cu",
@@ -40,17 +43,20 @@ def _deps() -> list[str]:
     return files
 
 
-def stale() -> bool:
-    if not os.path.exists(LIB):
+def stale(lib: str = LIB) -> bool:
+    if not os.path.exists(lib):
         return True
-    t = os.path.getmtime(LIB)
+    t = os.path.getmtime(lib)
     return any(os.path.getmtime(f) > t for f in _deps())
 
 
-def _compile(src: str, verbose_ptxas: bool) -> str:
-    obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + ".o")
+def _compile(src: str, verbose_ptxas: bool, bounds_check: bool = False) -> str:
+    out = BC_DIR if bounds_check else OUT_DIR
+    obj = os.path.join(out, os.path.splitext(src)[0] + ".o")
     cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-I", os.path.join(ROOT, "include"), "-c",
            os.path.join(CSRC, src), "-o", obj]
+    if bounds_check:
+        cmd[1:1] = ["-DPN_BOUNDS_CHECK"]
     if verbose_ptxas:
         cmd[1:1] = ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)
@@ -61,22 +67,25 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
     return obj
 
 
-def build(force: bool = False, verbose_ptxas: bool = False) -> str:
-    """Compile the library if any source changed; return its path."""
-    if not force and not stale():
-        return LIB
-    os.makedirs(OUT_DIR, exist_ok=True)
+def build(force: bool = False, verbose_ptxas: bool = False, bounds_check: bool = False) -> str:
+    """Compile the library if any source changed; return its path.  bounds_check: the
+    variant that checks every device index (libpn_gb300_bc.so, PN_BOUNDS_CHECK)."""
+    lib = LIB_BC if bounds_check else LIB
+    if not force and not stale(lib):
+        return lib
+    os.makedirs(BC_DIR if bounds_check else OUT_DIR, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas), SOURCES))
-    tmp = LIB + ".tmp"
+        objs = list(ex.map(lambda s: _compile(s, verbose_ptxas, bounds_check), SOURCES))
+    tmp = lib + ".tmp"
     cmd = [nvcc(), *ARCH, "-shared", "-o", tmp, *objs, "-lcudart_static", "-lrt", "-ldl",
            "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv,
+                bounds_check="--bounds-check" in sys.argv))

@@ -254,9 +254,11 @@ static int create(const pn_config* cfg, int64_t list_size, pn_search** out,
     return rc;
   }
   // d_err: [0] sticky error, [1] a point outside the periodic box, [2] incremental-update
-  // decision, [3] cells not sorted by x, [4] some query needs the pair cache's fallback
-  bool ok = cudaMalloc(&s->d_err, sizeof(int32_t) * 8) == cudaSuccess;
-  ok = ok && cudaMemset(s->d_err, 0, sizeof(int32_t) * 8) == cudaSuccess;
+  // decision, [3] cells not sorted by x, [4] some query needs the pair cache's fallback,
+  // [5] largest cell of the last build, [6] max_points_per_cell exceeded, [8] [9] site and
+  // index of the first bounds failure (bounds-checked build)
+  bool ok = cudaMalloc(&s->d_err, sizeof(int32_t) * pn::ERR_WORDS) == cudaSuccess;
+  ok = ok && cudaMemset(s->d_err, 0, sizeof(int32_t) * pn::ERR_WORDS) == cudaSuccess;
   ok = ok && cudaMallocHost(&s->h_ovf_n, sizeof(int32_t)) == cudaSuccess;
   ok = ok && cudaEventCreateWithFlags(&s->ev_ovf, cudaEventDisableTiming) == cudaSuccess;
   if (ok && !s->is_template) {
@@ -467,6 +469,25 @@ int pn_foreach_point_neighbor(pn_search* s, int32_t functor, const void* x, int6
   return record(s, rc, st);
 }
 
+int32_t pn_build_flags(void) {
+#ifdef PN_BOUNDS_CHECK
+  return 1;
+#else
+  return 0;
+#endif
+}
+
+int pn_bounds_failure(pn_search* s, int32_t* site, int32_t* index) {
+  if (!s || !site || !index) return PN_ERR_INVALID_ARG;
+  int32_t w[2] = {0, 0};
+  if (cudaMemcpy(w, s->d_err + pn::ERR_BC_SITE, sizeof(w), cudaMemcpyDeviceToHost) !=
+      cudaSuccess)
+    return PN_ERR_CUDA;
+  *site = w[0];
+  *index = w[1];
+  return PN_OK;
+}
+
 int pn_get_error(pn_search* s, int32_t clear) {
   if (!s) return PN_ERR_INVALID_ARG;
   int32_t e = 0;
@@ -504,6 +525,7 @@ const char* pn_status_string(int32_t status) {
     case PN_ERR_SCRATCH_LIMIT:
       return "the problem needs more than the 4 MiB fixed scratch of the no-allocation entry "
              "point (4 bytes per grid cell + 12 bytes per point + 20 bytes)";
+    case PN_ERR_INDEX: return "a device index out of range (bounds-checked build)";
     default: return "unknown status";
   }
 }

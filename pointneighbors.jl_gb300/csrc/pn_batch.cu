@@ -535,7 +535,7 @@ int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_cl
   bool ok = cudaMalloc(&b->d_grids, sizeof(GridDev<float>) * n_clouds) == cudaSuccess &&
             cudaMalloc(&b->d_pt_off, sizeof(int32_t) * (n_clouds + 1)) == cudaSuccess &&
             cudaMalloc(&b->d_cell_off, sizeof(int32_t) * (n_clouds + 1)) == cudaSuccess &&
-            cudaMalloc(&b->d_err, sizeof(int32_t) * 4) == cudaSuccess &&
+            cudaMalloc(&b->d_err, sizeof(int32_t) * ERR_WORDS) == cudaSuccess &&
             cudaMalloc(&b->d_counts, sizeof(int32_t) * (nc + 8)) == cudaSuccess &&
             cudaMalloc(&b->d_start, sizeof(int32_t) * (nc + 1)) == cudaSuccess &&
             cudaMalloc(&b->d_scan_state, sizeof(unsigned long long) * (b->scan_tiles + 1)) ==
@@ -553,7 +553,7 @@ int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_cl
             cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) == cudaSuccess;
   if (ok) {
     // spare slots: never a neighbour (NaN coordinates), never a query (perm -1)
-    ok = cudaMemset(b->d_err, 0, sizeof(int32_t) * 4) == cudaSuccess &&
+    ok = cudaMemset(b->d_err, 0, sizeof(int32_t) * ERR_WORDS) == cudaSuccess &&
          cudaMemset(b->d_perm + np, 0xff, sizeof(int32_t) * SLOT_PAD) == cudaSuccess &&
          cudaMemset(b->d_pos, 0xff, sizeof(float) * 4 * slots) == cudaSuccess &&
          cudaMemset(b->d_pa, 0xff, sizeof(float) * 4 * slots) == cudaSuccess;
@@ -569,6 +569,8 @@ int pn_batch_create(const pn_config* cfgs, const int64_t* n_points, int32_t n_cl
       a.cell_of_slot = b->d_cell_of_slot;
       a.pos = b->d_pos;
       a.err = b->d_err;
+      a.bc_slots = slots;
+      a.bc_points = np;
       a.outside = b->d_err + 1;
       a.unsorted = nullptr;  // the batch always re-bins: every cell sorted by x
       for (int k = 0; k < 3; ++k) {

@@ -74,7 +74,8 @@ k_bin(const GridDev<T> g, const T* __restrict__ y, int64_t n_y, const int32_t* _
       const unsigned peers = __match_any_sync(valid, cell);
       const int leader = __ffs(peers) - 1;
       int32_t b = 0;
-      if (lane == leader) b = atomicAdd(&counts[cell], __popc(peers));
+      if (lane == leader) b = atomicAdd(&counts[PN_IDX(err, BC_CELL, cell, g.n_total)],
+                                         __popc(peers));
       b = __shfl_sync(peers, b, leader);
       slot_of[t] = b + __popc(peers & lanemask_lt());
     }
@@ -190,13 +191,15 @@ __global__ void __launch_bounds__(256)
 k_scatter(const int32_t* __restrict__ cell_of, const int32_t* __restrict__ slot_of,
           const int32_t* __restrict__ idx, int32_t m, const int32_t* __restrict__ start,
           int32_t* __restrict__ tmp_perm, int32_t* __restrict__ cell_of_slot,
-          const int32_t* __restrict__ gate) {
+          const int32_t* __restrict__ gate, int32_t* __restrict__ err = nullptr,
+          int32_t n_cells = INT32_MAX, int64_t n_slots = INT64_MAX) {
   if (gate && *gate != GATE_REBUILD) return;
   const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= m) return;
-  const int32_t c = cell_of[t];
-  if (c < 0) return;
-  const int32_t p = start[c] + slot_of[t];
+  const int32_t c0 = cell_of[t];
+  if (c0 < 0) return;
+  const int32_t c = PN_IDX(err, BC_CELL, c0, n_cells);
+  const int32_t p = PN_IDX(err, BC_SLOT, start[c] + slot_of[t], n_slots);
   tmp_perm[p] = idx ? idx[t] : (int32_t)t;
   cell_of_slot[p] = c;
 }
@@ -449,13 +452,14 @@ __global__ void __launch_bounds__(256)
 k_scatter_movers(const int32_t* __restrict__ ovf_n, const int32_t* __restrict__ ovf_list,
                  const int32_t* __restrict__ ovf_cell, const int32_t* __restrict__ ovf_slot,
                  const int32_t* __restrict__ ovf_start, int32_t* __restrict__ tmp_perm,
-                 int32_t* __restrict__ cell_of_slot, const int32_t* __restrict__ gate) {
+                 int32_t* __restrict__ cell_of_slot, const int32_t* __restrict__ gate,
+                 int32_t* __restrict__ err, int32_t n_cells, int64_t n_slots) {
   if (*gate != GATE_OVERFLOW) return;
   const int32_t n = *ovf_n;
   for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < n;
        m += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t c = ovf_cell[m];
-    const int32_t p = ovf_start[c] + ovf_slot[m];
+    const int32_t c = PN_IDX(err, BC_CELL, ovf_cell[m], n_cells);
+    const int32_t p = PN_IDX(err, BC_SLOT, ovf_start[c] + ovf_slot[m], n_slots);
     tmp_perm[p] = ovf_list[m];
     cell_of_slot[p] = c;
   }
@@ -603,7 +607,8 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
   if (m > 0) {
     k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
                                               s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
-                                              nullptr); count_launch();
+                                              nullptr, s->d_err, s->n_total, slot_capacity(s));
+    count_launch();
     // Points rejected by the bounds check are not binned; every kernel that walks the
     // slots bounds itself by start[n_total], read on the device.
     launch_finalize<T>(s, y, (int32_t)m, st);
@@ -804,7 +809,8 @@ template <int D>
 __global__ void __launch_bounds__(BIN_THREADS)
 k_hash_dense_bin(const int4* __restrict__ key_of, int32_t m, int3 off, int3 n,
                  int32_t* __restrict__ cell_of, int32_t* __restrict__ slot_of,
-                 int32_t* __restrict__ counts) {
+                 int32_t* __restrict__ counts, int32_t* __restrict__ err) {
+  const int64_t n_cells = (int64_t)n.x * (D >= 2 ? n.y : 1) * (D == 3 ? n.z : 1);
   const int lane = threadIdx.x & 31;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < m;
        base += (int64_t)gridDim.x * blockDim.x) {
@@ -821,7 +827,8 @@ k_hash_dense_bin(const int4* __restrict__ key_of, int32_t m, int3 off, int3 n,
       const unsigned peers = __match_any_sync(valid, cell);
       const int leader = __ffs(peers) - 1;
       int32_t b = 0;
-      if (lane == leader) b = atomicAdd(&counts[cell], __popc(peers));
+      if (lane == leader) b = atomicAdd(&counts[PN_IDX(err, BC_CELL, cell, n_cells)],
+                                         __popc(peers));
       b = __shfl_sync(peers, b, leader);
       slot_of[t] = b + __popc(peers & lanemask_lt());
     }
@@ -942,9 +949,9 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
     const int3 off = make_int3(s->hash_off[0], s->hash_off[1], s->hash_off[2]);
     const int3 n = make_int3((int32_t)dims[0], (int32_t)dims[1], (int32_t)dims[2]);
     switch (s->ndims) {
-      case 1: k_hash_dense_bin<1><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
-      case 2: k_hash_dense_bin<2><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
-      default: k_hash_dense_bin<3><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts); break;
+      case 1: k_hash_dense_bin<1><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts, s->d_err); break;
+      case 2: k_hash_dense_bin<2><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts, s->d_err); break;
+      default: k_hash_dense_bin<3><<<blocks, BIN_THREADS, 0, st>>>(s->d_hkey_t, (int32_t)m, off, n, s->d_cell_of, s->d_slot_of, s->d_counts, s->d_err); break;
     }
     count_launch();
     // (the search's scan state has room for the tiles of list_size >= cells counts)
@@ -952,7 +959,9 @@ int build_hash(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_
                 scan_tile_count(cells), s->d_err, st, build_stats(s));
     k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, idx, (int32_t)m,
                                               s->d_start, s->d_tmp_perm, s->d_cell_of_slot,
-                                              nullptr); count_launch();
+                                              nullptr, s->d_err, (int32_t)cells,
+                                              slot_capacity(s));
+    count_launch();
     launch_finalize<T>(s, y, (int32_t)m, st);
   } else if (m > 0) {
     // 4. the lists: each list's points ranked by (cell, x, index), one entry per cell
@@ -1088,7 +1097,8 @@ static void launch_movers(pn_search* s, const T* y, cudaStream_t st) {
   const int32_t* gate = s->d_err + 2;
   k_scatter_movers<<<152 * 4, 256, 0, st>>>(s->d_ovf_n, s->d_ovf_list, s->d_ovf_cell,
                                              s->d_ovf_slot, s->d_ovf_start, s->d_tmp_perm,
-                                             s->d_cell_of_slot, gate); count_launch();
+                                             s->d_cell_of_slot, gate, s->d_err, s->n_total,
+                                             slot_capacity(s)); count_launch();
   k_finalize_movers<T, D><<<152 * 4, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot,
                                                    s->d_ovf_start, s->d_start + s->n_total,
                                                    s->n_total, y, s->d_perm,
@@ -1135,7 +1145,8 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell, gate,
              GATE_REBUILD);
   k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, nullptr, m, s->d_start,
-                                            s->d_tmp_perm, s->d_cell_of_slot, gate); count_launch();
+                                            s->d_tmp_perm, s->d_cell_of_slot, gate, s->d_err,
+                                            s->n_total, slot_capacity(s)); count_launch();
   launch_finalize<T>(s, y, m, st, gate);
   k_reset_overflow<<<152 * 4, 256, 0, st>>>(s->d_start, s->n_total, s->d_perm, s->d_main_perm,
                                             s->d_ovf_start, s->d_ovf_n, gate); count_launch();

@@ -139,6 +139,9 @@ struct NvtxRange {
 // Spare slots at the end of the slot arrays (candidate scans read up to 7 past a run).
 constexpr int64_t SLOT_PAD = 64;
 
+// Slots allocated in the slot arrays (main, overflow and the spare slots).
+inline int64_t slot_capacity(const pn_search* s) { return 2 * s->cap + SLOT_PAD; }
+
 // Host-side count of kernel launches made by the library (pn_launch_count()).
 void count_launch();
 

@@ -178,6 +178,55 @@ __device__ __forceinline__ void set_error(int32_t* err, int32_t code) {
   if (*(volatile int32_t*)err == 0) atomicCAS(err, 0, code);
 }
 
+// Bounds-checked builds (-DPN_BOUNDS_CHECK, libpn_gb300_bc.so): PN_IDX(err, site, i, n)
+// checks 0 <= i < n before an index reaches memory.  Outside that range the first failure's
+// site and index are kept in err[ERR_BC_SITE] and err[ERR_BC_INDEX], the sticky error
+// becomes PN_ERR_INDEX, and the access goes to element 0 instead (every checked array has an
+// element 0), so a checked run reports the bad index rather than faulting.  In the normal
+// build PN_IDX is the index itself.
+enum BoundsSite : int32_t {
+  BC_QUERY_SLOT = 1,     // a cell-sorted query slot
+  BC_CELL = 2,           // a linear cell index (cell starts, counts)
+  BC_RUN = 3,            // a candidate run [begin, end) of slots
+  BC_POINT = 4,          // a point index read from perm (outputs, per-point inputs)
+  BC_PAIR_CACHE = 5,     // a pair-cache entry (row, slot)
+  BC_SLOT = 6,           // a slot written by the build (scatter, movers)
+  BC_NEIGHBOUR = 7,      // a neighbour slot taken from the pair cache
+};
+constexpr int ERR_BC_SITE = 8, ERR_BC_INDEX = 9, ERR_WORDS = 16;
+
+static __device__ __noinline__ void bounds_failure(int32_t* err, int32_t site, int64_t i) {
+  if (err == nullptr) return;  // a kernel launched without an error word
+  if (atomicCAS(err + ERR_BC_SITE, 0, site) == 0) err[ERR_BC_INDEX] = (int32_t)i;
+  set_error(err, PN_ERR_INDEX);
+}
+
+template <typename I>
+__device__ __forceinline__ I bc_index(int32_t* err, int32_t site, I i, int64_t n) {
+  if ((int64_t)i < 0 || (int64_t)i >= n) {
+    bounds_failure(err, site, (int64_t)i);
+    return (I)0;
+  }
+  return i;
+}
+
+#ifdef PN_BOUNDS_CHECK
+#define PN_IDX(err, site, i, n) ::pn::bc_index((err), (site), (i), (int64_t)(n))
+// a run [b, e) of an array of n elements: an empty run when it does not fit
+#define PN_RUN(err, b, e, n)                                                         \
+  do {                                                                               \
+    if ((e) > (b) && ((int64_t)(b) < 0 || (int64_t)(e) > (int64_t)(n))) {           \
+      ::pn::bounds_failure((err), ::pn::BC_RUN, (int64_t)(b));                       \
+      (e) = (b);                                                                     \
+    }                                                                                \
+  } while (0)
+#else
+#define PN_IDX(err, site, i, n) (i)
+#define PN_RUN(err, b, e, n) \
+  do {                       \
+  } while (0)
+#endif
+
 __device__ __forceinline__ unsigned lanemask_lt() {
   unsigned m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));

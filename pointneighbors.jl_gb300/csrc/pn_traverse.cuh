@@ -41,6 +41,9 @@ struct TravArgs {
   T r2_lo, r2_hi;               // r^2 (1 -+ 32 eps): the FMA distance test decides outside
   const int32_t* outside;       // device flag: some binned point lies outside the periodic box
   int32_t* err;
+  // bounds-checked builds: slots allocated (main, overflow and padding) and points a query
+  // or a slot's permutation entry may name
+  int64_t bc_slots, bc_points;
   // Row clipping: inside every cell the points are sorted by their first coordinate, so a
   // stencil row's three cells are one x-sorted run and a query only scans the part of it
   // within x +- sqrt(r^2 - dy^2 - dz^2) (dy, dz: distance to the row's band).  `unsorted`
@@ -348,6 +351,7 @@ struct MaskParams {
   ulonglong2* mask;
   int64_t stride;
   int32_t* any_fallback;
+  int32_t* err;
 };
 template <class PF>
 struct MaskPairParams {
@@ -378,7 +382,8 @@ struct WithMask {
   }
   static __device__ __forceinline__ void flush(Acc& a, const Params& p, const Query<T, D>& q) {
     if (a.ri < 0) return;
-    const int64_t o = (int64_t)a.ri * p.m.stride + q.k;
+    const int64_t o =
+        (int64_t)a.ri * p.m.stride + PN_IDX(p.m.err, BC_PAIR_CACHE, q.k, p.m.stride);
     p.m.b0[o] = a.b0;
     p.m.mask[o] = make_ulonglong2(a.lo, a.hi);
   }
@@ -415,7 +420,9 @@ struct WithMask {
     F::finish(a.f, p.f, q);
     flush(a, p, q);
     if (a.fb) {
-      p.m.b0[q.k] = -1;  // row 0's entry marks the query for the stencil fallback
+      p.m.b0[PN_IDX(p.m.err, BC_PAIR_CACHE, q.k, p.m.stride)] = -1;  // row 0's entry marks
+                                                                      // the query for the
+                                                                      // stencil fallback
       if (*(volatile int32_t*)p.m.any_fallback == 0) atomicExch(p.m.any_fallback, 1);
     }
   }
@@ -1386,8 +1393,9 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
       if (D == 3) row = ((PER ? pwrap(c[2] + oz, g.ncell[2]) : c[2] + oz) - 1) * g.n[0] * g.n[1];
       if (D >= 2) row += ((PER ? pwrap(c[1] + oy, g.ncell[1]) : c[1] + oy) - 1) * g.n[0];
       if (!PER || (c[0] >= 3 && c[0] <= g.ncell[0])) {
-        const int32_t l0 = row + c[0] - 2;
+        const int32_t l0 = PN_IDX(a.err, BC_CELL, row + c[0] - 2, (int64_t)g.n_total - 2);
         int32_t b0 = __ldg(&a.start[l0]), e0 = __ldg(&a.start[l0 + 3]);
+        PN_RUN(a.err, b0, e0, a.bc_slots);
         if (clip) {
           clip_row<T, D>(a, q, below, above, oy, oz, b0, e0);
           if constexpr (has_row_hook<F>::value)
@@ -1395,17 +1403,25 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
           if (b0 >= e0) continue;  // no point of this row is within r
         }
         scan_any<T, D, PER, F>(a, p, acc, q, wrap, b0, e0);
-        if (a.ovf_start)
-          scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.ovf_start[l0]),
-                                 __ldg(&a.ovf_start[l0 + 3]));
+        if (a.ovf_start) {
+          int32_t ob = __ldg(&a.ovf_start[l0]), oe = __ldg(&a.ovf_start[l0 + 3]);
+          PN_RUN(a.err, ob, oe, a.bc_slots);
+          scan_any<T, D, PER, F>(a, p, acc, q, wrap, ob, oe);
+        }
       } else {
 #pragma unroll 1
         for (int ox = -1; ox <= 1; ++ox) {
-          const int32_t l = row + pwrap(c[0] + ox, g.ncell[0]) - 1;
-          scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.start[l]), __ldg(&a.start[l + 1]));
-          if (a.ovf_start)
-            scan_any<T, D, PER, F>(a, p, acc, q, wrap, __ldg(&a.ovf_start[l]),
-                                   __ldg(&a.ovf_start[l + 1]));
+          const int32_t l =
+              PN_IDX(a.err, BC_CELL, row + pwrap(c[0] + ox, g.ncell[0]) - 1, g.n_total);
+          int32_t b = __ldg(&a.start[l]), e = __ldg(&a.start[l + 1]);
+          PN_RUN(a.err, b, e, a.bc_slots);
+          scan_any<T, D, PER, F>(a, p, acc, q, wrap, b, e);
+          if (a.ovf_start) {
+            b = __ldg(&a.ovf_start[l]);
+            e = __ldg(&a.ovf_start[l + 1]);
+            PN_RUN(a.err, b, e, a.bc_slots);
+            scan_any<T, D, PER, F>(a, p, acc, q, wrap, b, e);
+          }
         }
       }
     }
@@ -1421,16 +1437,17 @@ __device__ __forceinline__ void sorted_query(const TravArgs<T>& a, const typenam
                                              int64_t k, int32_t n_slots) {
   Query<T, D> q;
   bool valid = k < n_slots;
-  q.i = valid ? a.perm[k] : -1;
+  q.i = valid ? a.perm[PN_IDX(a.err, BC_QUERY_SLOT, k, a.bc_slots)] : -1;
   if (valid && q.i < 0) F::vacant(p, (int32_t)k);
   valid = valid && q.i >= 0;
+  if (valid) q.i = PN_IDX(a.err, BC_POINT, q.i, a.bc_points);
   if (a.nb_len != nullptr && valid) valid = __ldg(&a.nb_len[k]) < 0;  // pair-cache rows only
   q.q = q.i;
   q.k = (int32_t)k;
   int32_t c[3] = {1, 1, 1};
   if (valid) {
     load_pos<T, D>(a.pos, k, q.x);
-    const int32_t lin = a.cell_of_slot[k];
+    const int32_t lin = PN_IDX(a.err, BC_CELL, a.cell_of_slot[k], a.g.n_total);
     c[0] = lin % a.g.n[0] + 1;
     if (D >= 2) c[1] = (lin / a.g.n[0]) % a.g.n[1] + 1;
     if (D == 3) c[2] = lin / (a.g.n[0] * a.g.n[1]) + 1;
@@ -1581,6 +1598,7 @@ __device__ __forceinline__ void traverse_query_hash(const TravArgs<T>& a,
         }
         int32_t b, e;
         hash_run<D>(a.hash_list, a.hash_cell, a.hash_mod, cc, b, e);
+        PN_RUN(a.err, b, e, a.bc_slots);
         scan_any<T, D, PER, F>(a, p, acc, q, PER, b, e);
       }
     }
@@ -1596,7 +1614,9 @@ k_trav_hash_sorted(const TravArgs<T> a, const typename F::Params p) {
   if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
   Query<T, D> q;
   const bool valid = k < n_slots;
-  q.i = valid ? a.perm[k] : -1;
+  q.i = valid ? PN_IDX(a.err, BC_POINT, a.perm[PN_IDX(a.err, BC_QUERY_SLOT, k, a.bc_slots)],
+                       a.bc_points)
+              : -1;
   q.q = q.i;
   q.k = (int32_t)k;
   int32_t c[3] = {0, 0, 0};
@@ -1662,7 +1682,7 @@ __device__ __forceinline__ void list_query(const TravArgs<T>& a, const typename 
 #pragma unroll
     for (int e = 0; e < 4; ++e) {
       if (e < m) {
-        const int32_t js = js4[e];
+        const int32_t js = PN_IDX(a.err, BC_NEIGHBOUR, js4[e], a.bc_slots);
         T yj[D], pd[D];
         const T aux = load_cand<T, D>(a.pos, js, yj);
         const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
@@ -1682,9 +1702,10 @@ k_lists_sorted(const TravArgs<T> a, const typename F::Params p) {
   if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
   Query<T, D> q;
   bool valid = k < n_slots;
-  q.i = valid ? a.perm[k] : -1;
+  q.i = valid ? a.perm[PN_IDX(a.err, BC_QUERY_SLOT, k, a.bc_slots)] : -1;
   if (valid && q.i < 0) F::vacant(p, (int32_t)k);
   valid = valid && q.i >= 0;
+  if (valid) q.i = PN_IDX(a.err, BC_POINT, q.i, a.bc_points);
   q.q = q.i;
   q.k = (int32_t)k;
   if (valid) load_pos<T, D>(a.pos, k, q.x);
@@ -1703,10 +1724,11 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
   Query<T, D> q;
   bool valid = k < n_slots;
-  q.i = valid ? a.perm[k] : -1;
+  q.i = valid ? a.perm[PN_IDX(a.err, BC_QUERY_SLOT, k, a.bc_slots)] : -1;
   if (valid && q.i < 0) F::vacant(p, (int32_t)k);
   valid = valid && q.i >= 0;
-  if (!valid || __ldg(&a.pc_b0[k]) < 0) return;
+  if (!valid || __ldg(&a.pc_b0[PN_IDX(a.err, BC_PAIR_CACHE, k, a.pc_stride)]) < 0) return;
+  q.i = PN_IDX(a.err, BC_POINT, q.i, a.bc_points);
   q.q = q.i;
   q.k = (int32_t)k;
   load_pos<T, D>(a.pos, k, q.x);
@@ -1749,7 +1771,7 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
     if (w == 0) break;
     const int e = __ffsll((long long)w) - 1;
     w &= w - 1;
-    const int32_t js = rb0 + 64 * (wi & 1) + e;
+    const int32_t js = PN_IDX(a.err, BC_NEIGHBOUR, rb0 + 64 * (wi & 1) + e, a.bc_slots);
     T yj[D], pd[D];
     const T aux = load_cand<T, D>(a.pos, js, yj);
     const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);

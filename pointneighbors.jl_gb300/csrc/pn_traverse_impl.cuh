@@ -128,7 +128,7 @@ static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m, cudaStream_t 
   if (rc != PN_OK) return rc;
   cudaMemsetAsync(s->d_err + 4, 0, sizeof(int32_t), st);
   *m = MaskParams{s->d_pc_b0, reinterpret_cast<ulonglong2*>(s->d_pc_mask), n_rows,
-                  s->d_err + 4};
+                  s->d_err + 4, s->d_err};
   s->pc_rows = n_rows;
   return PN_OK;
 }
@@ -272,6 +272,8 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
   a.n_q = n_q;
   a.n_x = n_x;
   a.err = s->d_err;
+  a.bc_slots = slot_capacity(s);
+  a.bc_points = s->n_y;
   a.outside = s->d_err + 1;
   a.unsorted = s->d_err + 3;
   if (s->hashed && !s->hash_dense) {  // the hash lists' traversal

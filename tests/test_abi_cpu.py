@@ -191,6 +191,13 @@ def test_geometry_known_values(L):
     assert rc == L.PN_ERR_INVALID_ARG
 
 
+def test_normal_build_is_not_bounds_checked(L):
+    """The in-tree library is the normal build; the checked one (PN_BOUNDS_CHECK) is a
+    separate file with bit 0 of pn_build_flags set."""
+    assert L.load().pn_build_flags() == 0
+    assert L.status_string(L.PN_ERR_INDEX) == "a device index out of range (bounds-checked build)"
+
+
 def test_status_strings_are_the_references(L):
     assert L.status_string(L.PN_ERR_OUT_OF_DOMAIN) == \
         "particle coordinates are NaN or outside the domain bounds of the cell list"
