@@ -1098,7 +1098,9 @@ def extra_records(args, rank, world, local):
     rec["update_paths"] = {
         "overflow": _path_record(run_gpu(sub(rebuild_fraction=1.0), rank, world, local)),
         "note": "rebuild_fraction 1.0: update! keeps the movers in overflow lists (never "
-                "rebuilds), whose queries the pair cache leaves to the stencil traversal"}
+                "rebuilds) and moves the other points in place; the rows are clipped by the "
+                "sort keys widened by the largest in-place move, and the pair cache also "
+                "holds each row's overflow run"}
     rec["batched"] = run_gpu_batched(sub(steps=min(K, 10), warmup=min(Wm, 3)), rank, world, local)
     rec["adjoint"] = run_gpu_adjoint(sub(dtype="float32"), rank, world, local)
     rec["fp64"] = _path_record(run_gpu(sub(dtype="float64", steps=min(K, 5),

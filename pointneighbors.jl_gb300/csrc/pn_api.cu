@@ -32,9 +32,10 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 static void free_points(pn_search* s) {
   void* ptrs[] = {s->d_cell_of, s->d_slot_of, s->d_tmp_perm, s->d_perm, s->d_cell_of_slot,
                   s->d_pos,     s->d_pa,      s->d_pb,       s->d_main_perm, s->d_ovf_list,
-                  s->d_ovf_cell, s->d_ovf_slot, s->d_pos32, s->d_pos32lo};
+                  s->d_ovf_cell, s->d_ovf_slot, s->d_pos32, s->d_pos32lo, s->d_xkey};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  s->d_xkey = nullptr;
   s->d_cell_of = s->d_slot_of = s->d_tmp_perm = s->d_perm = s->d_cell_of_slot = nullptr;
   s->d_main_perm = s->d_ovf_list = s->d_ovf_cell = s->d_ovf_slot = nullptr;
   s->d_pos = s->d_pa = s->d_pb = nullptr;
@@ -69,6 +70,9 @@ int ensure_capacity(pn_search* s, int64_t n) {
   if (s->mixed || (s->dtype == PN_FLOAT64 && !s->hashed))
     alloc((void**)&s->d_pos32, sizeof(float) * 4 * slots);
   if (s->mixed) alloc((void**)&s->d_pos32lo, sizeof(float) * 4 * slots);
+  if (s->dtype == PN_FLOAT32 && !s->mixed && !s->hashed &&
+      s->cfg.update_strategy == PN_PARALLEL_INCREMENTAL_UPDATE)
+    alloc((void**)&s->d_xkey, sizeof(float) * slots);
   alloc((void**)&s->d_main_perm, i4 * cap);
   alloc((void**)&s->d_ovf_list, i4 * cap);
   alloc((void**)&s->d_ovf_cell, i4 * cap);
@@ -389,7 +393,8 @@ int pn_destroy(pn_search* s) {
   void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
                   s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_b0,
-                  s->d_pc_mask,    s->d_hkey_t,     s->d_hkey_tmp,  s->d_hkey,
+                  s->d_pc_mask,    s->d_pc_ob0,     s->d_pc_omask,  s->d_hkey_t,
+                  s->d_hkey_tmp,   s->d_hkey,
                   s->d_hcellidx,   s->d_hcell,      s->d_hbucket,   s->d_hscan_state,
                   s->d_hbbox};
   for (void* p : ptrs)

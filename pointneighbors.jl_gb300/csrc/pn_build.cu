@@ -226,7 +226,8 @@ __device__ __forceinline__ void finalize_slot(const int32_t* __restrict__ tmp_pe
                                               const int32_t* __restrict__ start, int64_t k,
                                               const T* __restrict__ y, int32_t* __restrict__ perm,
                                               T* __restrict__ pos,
-                                              const int32_t* __restrict__ stats = nullptr) {
+                                              const int32_t* __restrict__ stats = nullptr,
+                                              float* __restrict__ xkey = nullptr) {
   const int32_t c = cell_of_slot[k];
   const int32_t s = start[c], e = start[c + 1];
   const int32_t v = tmp_perm[k];
@@ -250,6 +251,9 @@ __device__ __forceinline__ void finalize_slot(const int32_t* __restrict__ tmp_pe
 #pragma unroll
   for (int d = 0; d < D; ++d) p[d] = y[(int64_t)v * D + d];
   store_pos<T, D>(pos, dst, p);
+  if constexpr (std::is_same<T, float>::value) {
+    if (xkey != nullptr) xkey[dst] = p[0];  // the sort key: x when the cell was sorted
+  }
 }
 
 template <typename T, int D>
@@ -257,13 +261,13 @@ __global__ void __launch_bounds__(256)
 k_finalize(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
            const int32_t* __restrict__ start, int32_t n_total, const T* __restrict__ y,
            int32_t* __restrict__ perm, T* __restrict__ pos, const int32_t* __restrict__ gate,
-           const int32_t* __restrict__ stats = nullptr) {
+           const int32_t* __restrict__ stats = nullptr, float* __restrict__ xkey = nullptr) {
   if (gate && *gate != GATE_REBUILD) return;
   // Only start[n_total] slots were filled: points that failed the bounds check were not
   // binned, so the slot count is read on the device.
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= start[n_total]) return;
-  finalize_slot<T, D>(tmp_perm, cell_of_slot, start, k, y, perm, pos, stats);
+  finalize_slot<T, D>(tmp_perm, cell_of_slot, start, k, y, perm, pos, stats, xkey);
 }
 
 // The in-cell rank of the slots of cells above LARGE_CELL points (cells, or hash lists with
@@ -279,7 +283,7 @@ k_finalize_large(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict
                  const int4* __restrict__ key_tmp, const int32_t* __restrict__ start,
                  int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
                  T* __restrict__ pos, int4* __restrict__ key, const int32_t* __restrict__ stats,
-                 const int32_t* __restrict__ gate) {
+                 const int32_t* __restrict__ gate, float* __restrict__ xkey = nullptr) {
   if (gate && *gate != GATE_REBUILD) return;
   if (stats[0] <= LARGE_CELL || stats[1] != 0) return;
   __shared__ T s_x[LARGE_TILE];
@@ -349,6 +353,9 @@ k_finalize_large(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict
 #pragma unroll
       for (int d = 0; d < D; ++d) p[d] = y[(int64_t)v * D + d];
       store_pos<T, D>(pos, dst, p);
+      if constexpr (std::is_same<T, float>::value) {
+        if (xkey != nullptr) xkey[dst] = p[0];
+      }
     }
     __syncthreads();  // every thread has read s_lo / s_hi before they are reset
   }
@@ -373,10 +380,11 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
               int32_t* __restrict__ ovf_counts, int32_t* __restrict__ ovf_n,
               int32_t* __restrict__ ovf_list, int32_t* __restrict__ ovf_cell,
               int32_t* __restrict__ ovf_slot, int32_t* __restrict__ outside,
-              int32_t* __restrict__ err) {
+              int32_t* __restrict__ err, const float* __restrict__ xkey) {
   const int lane = threadIdx.x & 31;
   const int32_t nm = *n_main;
   int32_t ovf_max = 0;  // the largest overflow list this thread has seen grow
+  float dmax = 0.0f;    // the largest |x - xkey| of a slot refreshed in place
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nm;
        base += (int64_t)gridDim.x * blockDim.x) {
     const int64_t k = base + threadIdx.x;
@@ -403,6 +411,9 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
       } else if (lin == cell_of_slot[k]) {
         perm[k] = i;
         store_pos<T, D>(pos, k, p);
+        if constexpr (std::is_same<T, float>::value) {
+          if (xkey != nullptr) dmax = fmaxf(dmax, fabsf(__fsub_rn(p[0], xkey[k])));
+        }
       } else {
         moved = true;
         cell = lin;
@@ -437,14 +448,18 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
       }
     }
   }
-  // one atomic per block: the block's loop bounds are uniform, so every thread gets here
-  __shared__ int32_t s_max;
-  if (threadIdx.x == 0) s_max = 0;
+  // one atomic per block: the block's loop bounds are uniform, so every thread gets here.
+  // dmax >= 0, so its bits order like the values.
+  __shared__ int32_t s_max, s_dmax;
+  if (threadIdx.x == 0) s_max = s_dmax = 0;
   __syncthreads();
   const int32_t wmax = __reduce_max_sync(0xffffffffu, ovf_max);
+  const int32_t wd = __reduce_max_sync(0xffffffffu, __float_as_int(dmax));
   if (lane == 0 && wmax > 0) atomicMax(&s_max, wmax);
+  if (lane == 0 && wd > 0) atomicMax(&s_dmax, wd);
   __syncthreads();
   if (threadIdx.x == 0 && s_max > 0) atomicMax(&ovf_n[1], s_max);
+  if (threadIdx.x == 0 && s_dmax > 0) atomicMax(&err[ERR_DELTA], s_dmax);
 }
 
 // Movers -> their overflow slots (ovf_start is absolute: it starts after the main slots).
@@ -471,12 +486,13 @@ __global__ void __launch_bounds__(256)
 k_finalize_movers(const int32_t* __restrict__ tmp_perm, const int32_t* __restrict__ cell_of_slot,
                   const int32_t* __restrict__ ovf_start, const int32_t* __restrict__ n_main,
                   int32_t n_total, const T* __restrict__ y, int32_t* __restrict__ perm,
-                  T* __restrict__ pos, const int32_t* __restrict__ gate) {
+                  T* __restrict__ pos, const int32_t* __restrict__ gate,
+                  float* __restrict__ xkey) {
   if (*gate != GATE_OVERFLOW) return;
   const int32_t k0 = *n_main, k1 = ovf_start[n_total];
   for (int64_t k = k0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < k1;
        k += (int64_t)gridDim.x * blockDim.x)
-    finalize_slot<T, D>(tmp_perm, cell_of_slot, ovf_start, k, y, perm, pos);
+    finalize_slot<T, D>(tmp_perm, cell_of_slot, ovf_start, k, y, perm, pos, nullptr, xkey);
 }
 
 // The decision: rebuild when the points outside their main cell exceed `fraction` of the
@@ -509,7 +525,7 @@ __global__ void __launch_bounds__(256)
 k_reset_overflow(const int32_t* __restrict__ start, int32_t n_total,
                  const int32_t* __restrict__ perm, int32_t* __restrict__ main_perm,
                  int32_t* __restrict__ ovf_start, int32_t* __restrict__ ovf_n,
-                 const int32_t* __restrict__ gate) {
+                 const int32_t* __restrict__ gate, int32_t* __restrict__ delta) {
   if (*gate != GATE_REBUILD) return;
   const int32_t nm = start[n_total];
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
@@ -517,7 +533,10 @@ k_reset_overflow(const int32_t* __restrict__ start, int32_t n_total,
     ovf_start[c] = nm;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nm; k += stride)
     main_perm[k] = perm[k];
-  if (blockIdx.x == 0 && threadIdx.x == 0) *ovf_n = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *ovf_n = 0;
+    *delta = 0;  // every slot holds its sort key again
+  }
 }
 
 // ---------------------------------------------------------------- host side
@@ -560,16 +579,16 @@ static void launch_finalize(pn_search* s, const T* y, int32_t m, cudaStream_t st
   const int lb = std::min(blocks, 152 * 4);
   switch (s->ndims) {
     case 1:
-      k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats);
-      k_finalize_large<T, 1, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate);
+      k_finalize<T, 1><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats, s->d_xkey);
+      k_finalize_large<T, 1, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate, s->d_xkey);
       break;
     case 2:
-      k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats);
-      k_finalize_large<T, 2, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate);
+      k_finalize<T, 2><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats, s->d_xkey);
+      k_finalize_large<T, 2, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate, s->d_xkey);
       break;
     default:
-      k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats);
-      k_finalize_large<T, 3, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate);
+      k_finalize<T, 3><<<blocks, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, s->d_start, nt, y, s->d_perm, pos, gate, stats, s->d_xkey);
+      k_finalize_large<T, 3, false><<<lb, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot, nullptr, s->d_start, nt, y, s->d_perm, pos, nullptr, stats, gate, s->d_xkey);
       break;
   }
   count_launch();
@@ -613,6 +632,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
     // slots bounds itself by start[n_total], read on the device.
     launch_finalize<T>(s, y, (int32_t)m, st);
   }
+  cudaMemsetAsync(s->d_err + ERR_DELTA, 0, sizeof(int32_t), st);
   s->n_binned = m;
   s->pc_valid = false;
   s->ovf_active = false;
@@ -1089,7 +1109,7 @@ static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {
   k_mark_movers<T, D, PER><<<blocks, 256, 0, st>>>(
       make_grid<T>(s), s->d_main_perm, s->d_cell_of_slot, s->d_start + s->n_total, y,
       s->d_perm, static_cast<T*>(s->d_pos), s->d_ovf_counts, s->d_ovf_n, s->d_ovf_list,
-      s->d_ovf_cell, s->d_ovf_slot, s->d_err + 1, s->d_err); count_launch();
+      s->d_ovf_cell, s->d_ovf_slot, s->d_err + 1, s->d_err, s->d_xkey); count_launch();
 }
 
 template <typename T, int D>
@@ -1102,7 +1122,8 @@ static void launch_movers(pn_search* s, const T* y, cudaStream_t st) {
   k_finalize_movers<T, D><<<152 * 4, 256, 0, st>>>(s->d_tmp_perm, s->d_cell_of_slot,
                                                    s->d_ovf_start, s->d_start + s->n_total,
                                                    s->n_total, y, s->d_perm,
-                                                   static_cast<T*>(s->d_pos), gate); count_launch();
+                                                   static_cast<T*>(s->d_pos), gate, s->d_xkey);
+  count_launch();
 }
 
 template <typename T>
@@ -1117,6 +1138,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   cudaMemsetAsync(s->d_ovf_n, 0, 2 * sizeof(int32_t), st);  // movers, largest overflow cell
   cudaMemsetAsync(build_stats(s), 0, 2 * sizeof(int32_t), st);
   cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
+  cudaMemsetAsync(s->d_err + ERR_DELTA, 0, sizeof(int32_t), st);
   const bool per = s->periodic != 0;
   switch (s->ndims * 2 + (per ? 1 : 0)) {
     case 2: launch_mark<T, 1, false>(s, y, st); break;
@@ -1149,7 +1171,8 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
                                             s->n_total, slot_capacity(s)); count_launch();
   launch_finalize<T>(s, y, m, st, gate);
   k_reset_overflow<<<152 * 4, 256, 0, st>>>(s->d_start, s->n_total, s->d_perm, s->d_main_perm,
-                                            s->d_ovf_start, s->d_ovf_n, gate); count_launch();
+                                            s->d_ovf_start, s->d_ovf_n, gate,
+                                            s->d_err + ERR_DELTA); count_launch();
   s->ovf_active = true;
   s->pc_valid = false;
   refresh_pos32(s, st);

@@ -78,6 +78,11 @@ struct pn_search {
   bool ovf_pending = false;
   int64_t n_ovf = 0;                   // movers after the last update (host view)
   bool ovf_active = false;             // overflow lists in use
+  // Float32 incremental searches: each slot's first coordinate when its cell was last
+  // sorted (main slots: the last full build; overflow slots: the last update), the key the
+  // rows are clipped by while the positions of the main slots move in place; the largest
+  // distance of a main slot's x from its key is err word ERR_DELTA
+  float* d_xkey = nullptr;             // [slots]
   bool main_perm_valid = false;
   double rebuild_fraction = 0.01;      // full rebuild when movers exceed this fraction
   int32_t updates_since_build = 0;
@@ -91,6 +96,13 @@ struct pn_search {
   int64_t pc_b0_cap = 0;
   unsigned long long* d_pc_mask = nullptr;  // [rows][slots] x 2 words
   int64_t pc_mask_cap = 0;
+  // while overflow lists are in use: per row the start of the clipped overflow run (-1: no
+  // neighbour in it) and a 64-bit mask of its neighbours
+  int32_t* d_pc_ob0 = nullptr;              // [rows][slots]
+  int64_t pc_ob0_cap = 0;
+  unsigned long long* d_pc_omask = nullptr;  // [rows][slots]
+  int64_t pc_omask_cap = 0;
+  bool pc_ovf = false;                      // the last recording wrote the overflow masks
   int64_t pc_rows = 0;
 
   // SpatialHashingCellList: the slots of a hash list are sorted by cell, then by first

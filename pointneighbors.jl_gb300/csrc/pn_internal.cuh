@@ -194,6 +194,9 @@ enum BoundsSite : int32_t {
   BC_NEIGHBOUR = 7,      // a neighbour slot taken from the pair cache
 };
 constexpr int ERR_BC_SITE = 8, ERR_BC_INDEX = 9, ERR_WORDS = 16;
+// err word (as Float32 bits): the largest |x - xkey| of a main slot after an incremental
+// update that kept overflow lists (0 after a build or rebuild)
+constexpr int ERR_DELTA = 10;
 
 static __device__ __noinline__ void bounds_failure(int32_t* err, int32_t site, int64_t i) {
   if (err == nullptr) return;  // a kernel launched without an error word

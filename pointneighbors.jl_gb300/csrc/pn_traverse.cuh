@@ -52,6 +52,13 @@ struct TravArgs {
   // rounding of the cell edges, so the clipped run is always a superset of the neighbours.
   const int32_t* unsorted;
   T clip_m[3];
+  // Float32 incremental searches with overflow lists (or null): the rows are clipped by the
+  // sorted key xkey (each slot's x when its cell was last sorted) with the window widened by
+  // *delta, the largest distance of a main slot's x from its key, so the clipped runs stay
+  // supersets of the neighbours while the positions move in place; overflow runs are
+  // clipped by their keys (their x: they are re-sorted at every update).
+  const float* xkey;
+  const float* delta;
   // Precomputed neighbour lists (or null: the grid traversal).  Groups of 32 rows are stored
   // transposed in quads: row r's entries 4k..4k+3 are the int4 at
   // nb[nb_grp[r / 32] + 128 k + 4 (r % 32)], so a warp reads its rows' k-th quads in one
@@ -69,6 +76,8 @@ struct TravArgs {
   const int32_t* pc_b0;
   const ulonglong2* pc_mask;
   int64_t pc_stride;
+  const int32_t* pc_ob0;                 // overflow runs (or null), see MaskParams
+  const unsigned long long* pc_omask;
   const int32_t* pc_any_fallback;  // device flag: some query was marked for the fallback
   // SpatialHashingCellList (or null): list h's cells are the entries hash_cell[hash_list[h]
   // .. hash_list[h + 1]), each (x, y, z, first slot), a cell's run ending at the next
@@ -352,6 +361,13 @@ struct MaskParams {
   int64_t stride;
   int32_t* any_fallback;
   int32_t* err;
+  // overflow lists in use (or null): per row the start of the clipped overflow run (-1: no
+  // neighbour in it) and a 64-bit mask of its neighbours; written only when some point is
+  // in an overflow list (*ovf_end > *main_end), which the cache's walk checks the same way
+  int32_t* ob0;
+  unsigned long long* omask;
+  const int32_t* ovf_end;
+  const int32_t* main_end;
 };
 template <class PF>
 struct MaskPairParams {
@@ -370,15 +386,23 @@ struct WithMask {
   static constexpr bool kInline = F::kInline;
   static constexpr bool kRowHook = true;
   using Params = MaskPairParams<typename F::Params>;  // the same type for every D
-  struct Acc { typename F::Acc f; int32_t ri, b0; uint64_t lo, hi; bool fb; };
+  // lo, hi: the row's main run from b0; om: its overflow run from ob0 (ovf: the row's
+  // candidates now come from the overflow run); ovf_any: the overflow masks are written
+  struct Acc {
+    typename F::Acc f;
+    int32_t ri, b0, ob0;
+    uint64_t lo, hi, om;
+    bool fb, ovf, ovf_any;
+  };
   static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
   static __device__ __forceinline__ void fail(const Params& p, const Query<T, D>& q) { F::fail(p.f, q); }
   static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
     F::init(a.f, p.f, q);
     a.ri = -1;
-    a.b0 = 0;
-    a.lo = a.hi = 0;
-    a.fb = false;
+    a.b0 = a.ob0 = 0;
+    a.lo = a.hi = a.om = 0;
+    a.fb = a.ovf = false;
+    a.ovf_any = p.m.ob0 != nullptr && __ldg(p.m.ovf_end) > __ldg(p.m.main_end);
   }
   static __device__ __forceinline__ void flush(Acc& a, const Params& p, const Query<T, D>& q) {
     if (a.ri < 0) return;
@@ -386,19 +410,35 @@ struct WithMask {
         (int64_t)a.ri * p.m.stride + PN_IDX(p.m.err, BC_PAIR_CACHE, q.k, p.m.stride);
     p.m.b0[o] = a.b0;
     p.m.mask[o] = make_ulonglong2(a.lo, a.hi);
+    if (a.ovf_any) {
+      p.m.ob0[o] = a.om != 0 ? a.ob0 : -1;
+      if (a.om != 0) p.m.omask[o] = a.om;
+    }
   }
   static __device__ __forceinline__ void row_begin(Acc& a, const Params& p, const Query<T, D>& q,
                                                    int ri, int32_t b0, int32_t e0) {
     flush(a, p, q);
     a.ri = ri;
     a.b0 = b0;
-    a.lo = a.hi = 0;
+    a.lo = a.hi = a.om = 0;
+    a.ovf = false;
     if (e0 - b0 > 128) a.fb = true;
+  }
+  // the row's overflow run [ob0, oe0) follows its main run
+  static __device__ __forceinline__ void ovf_begin(Acc& a, int32_t ob0, int32_t oe0) {
+    a.ovf = true;
+    a.ob0 = ob0;
+    if (oe0 > ob0 && (!a.ovf_any || oe0 - ob0 > 64)) a.fb = true;
   }
   static __device__ __forceinline__ void no_rows(Acc& a) { a.fb = true; }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>& q,
                                               int32_t js, const T* pd, T d2, T aux) {
     F::pair(a.f, p.f, q, js, pd, d2, aux);
+    if (a.ovf) {
+      const uint32_t off = (uint32_t)(js - a.ob0);
+      if (off < 64) a.om |= 1ull << off;
+      return;
+    }
     const uint32_t off = (uint32_t)(js - a.b0);
     if (off < 64) a.lo |= 1ull << off;
     else if (off < 128) a.hi |= 1ull << (off - 64);
@@ -412,7 +452,7 @@ struct WithMask {
     uint32_t hits = 0u;
 #pragma unroll
     for (int u = 0; u < GROUP; ++u) hits |= d2[u] <= r2 ? 1u << u : 0u;
-    const uint32_t off = (uint32_t)(js0 - a.b0);
+    const uint32_t off = (uint32_t)(js0 - a.b0);  // main runs only (overflow runs: pair())
     if (off < 64) a.lo |= (uint64_t)hits << off;
     else if (off < 128) a.hi |= (uint64_t)hits << (off - 64);
   }
@@ -931,6 +971,9 @@ struct MixedFast {
   static __device__ __forceinline__ void no_rows(Acc& a) {
     if constexpr (kRowHook) F::no_rows(a.f);
   }
+  static __device__ __forceinline__ void ovf_begin(Acc& a, int32_t ob0, int32_t oe0) {
+    if constexpr (kRowHook) F::ovf_begin(a.f, ob0, oe0);
+  }
   // The exact Float32(Float64(xi - yj)) from the hi/lo split (q.x holds the query's hi
   // part), in Float64 where the split cannot decide the rounding.
   static __device__ __forceinline__ void exact_diff(const Acc& a, const Params& p,
@@ -1051,6 +1094,9 @@ struct Exact64 {
   }
   static __device__ __forceinline__ void no_rows(Acc& a) {
     if constexpr (kRowHook) F::no_rows(a.f);
+  }
+  static __device__ __forceinline__ void ovf_begin(Acc& a, int32_t ob0, int32_t oe0) {
+    if constexpr (kRowHook) F::ovf_begin(a.f, ob0, oe0);
   }
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<float, D>& q,
                                               int32_t js, const float*, float, float) {
@@ -1222,14 +1268,15 @@ __device__ __forceinline__ void chunk_done(const TravArgs<T>& a, const typename 
 // where they reconverge.
 constexpr int CHUNK_WORDS = 2;
 
-template <typename T, int D, bool PER, bool WRAP, class F>
+// NOGROUP: one candidate at a time even for a group functor (the overflow runs).
+template <typename T, int D, bool PER, bool WRAP, class F, bool NOGROUP = false>
 __device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F::Params& p,
                                          typename F::Acc& acc, const Query<T, D>& q,
                                          int32_t beg, int32_t end) {
   if constexpr (F::kInline) {
     // one candidate at a time with the exact test and the pair function applied in place
     // on the registers just loaded (a cheap pair function needs no compaction)
-    if constexpr (sizeof(T) == 4 && D == 3 && !WRAP && has_group<F>::value) {
+    if constexpr (sizeof(T) == 4 && D == 3 && !WRAP && has_group<F>::value && !NOGROUP) {
       // GROUP candidates per step, each d^2 formed exactly as in the loop below; the last
       // group reads up to GROUP - 1 slots past the run (the slot arrays' padding holds
       // them) and masks them off
@@ -1295,26 +1342,26 @@ __device__ __forceinline__ void scan_run(const TravArgs<T>& a, const typename F:
   }
 }
 
-template <typename T, int D, bool PER, class F>
+template <typename T, int D, bool PER, class F, bool NOGROUP = false>
 __device__ __forceinline__ void scan_any(const TravArgs<T>& a, const typename F::Params& p,
                                          typename F::Acc& acc, const Query<T, D>& q,
                                          bool wrap, int32_t beg, int32_t end) {
-  if (PER && wrap) scan_run<T, D, PER, PER, F>(a, p, acc, q, beg, end);
-  else scan_run<T, D, PER, false, F>(a, p, acc, q, beg, end);
+  if (PER && wrap) scan_run<T, D, PER, PER, F, NOGROUP>(a, p, acc, q, beg, end);
+  else scan_run<T, D, PER, false, F, NOGROUP>(a, p, acc, q, beg, end);
 }
 
 // Rows this short are scanned whole: the two binary searches would cost more than the
 // candidates they skip.
 constexpr int32_t CLIP_MIN_RUN = 32;
 
-// First slot of the x-sorted run [b, e) with x >= v (lower) or x > v (upper).
-template <typename T, int D, bool UPPER>
-__device__ __forceinline__ int32_t bound_x(const T* __restrict__ pos, int32_t b, int32_t e, T v) {
-  constexpr int S = PS<D>::value;
+// First slot of the x-sorted run [b, e) with key >= v (lower) or key > v (upper); the key
+// of slot k is key[k * S].
+template <typename T, int S, bool UPPER>
+__device__ __forceinline__ int32_t bound_x(const T* __restrict__ key, int32_t b, int32_t e, T v) {
   int32_t n = e - b;
   while (n > 0) {
     const int32_t h = n >> 1;
-    const T xk = __ldg(&pos[(int64_t)(b + h) * S]);
+    const T xk = __ldg(&key[(int64_t)(b + h) * S]);
     if (UPPER ? !(v < xk) : (xk < v)) {
       b += h + 1;
       n -= h + 1;
@@ -1327,11 +1374,12 @@ __device__ __forceinline__ int32_t bound_x(const T* __restrict__ pos, int32_t b,
 
 // Clip the x-sorted run [b0, e0) of the stencil row (oy, oz) to the query's reach
 // x +- sqrt(r^2 - dy^2 - dz^2); an unreachable row becomes empty.  below/above: the query's
-// distance (less the margin) to the lower/upper edge of its cell in y and z.
+// distance (less the margin) to the lower/upper edge of its cell in y and z.  keyed: the
+// run is searched by its sort keys (xkey) with the reach widened by `margin`.
 template <typename T, int D>
 __device__ __forceinline__ void clip_row(const TravArgs<T>& a, const Query<T, D>& q,
                                          const T* below, const T* above, int oy, int oz,
-                                         int32_t& b0, int32_t& e0) {
+                                         int32_t& b0, int32_t& e0, T margin, bool keyed) {
   if (e0 - b0 <= CLIP_MIN_RUN) return;
   const T dy = oy < 0 ? below[1] : (oy > 0 ? above[1] : (T)0);
   const T dz = oz < 0 ? below[2] : (oz > 0 ? above[2] : (T)0);
@@ -1341,9 +1389,16 @@ __device__ __forceinline__ void clip_row(const TravArgs<T>& a, const Query<T, D>
     e0 = b0;
     return;
   }
-  const T w = fsqrt(rem) * (T)1.00001 + a.clip_m[0];
-  b0 = bound_x<T, D, false>(a.pos, b0, e0, q.x[0] - w);
-  e0 = bound_x<T, D, true>(a.pos, b0, e0, q.x[0] + w);
+  const T w = fsqrt(rem) * (T)1.00001 + a.clip_m[0] + margin;
+  if constexpr (std::is_same<T, float>::value) {
+    if (keyed) {
+      b0 = bound_x<float, 1, false>(a.xkey, b0, e0, q.x[0] - w);
+      e0 = bound_x<float, 1, true>(a.xkey, b0, e0, q.x[0] + w);
+      return;
+    }
+  }
+  b0 = bound_x<T, PS<D>::value, false>(a.pos, b0, e0, q.x[0] - w);
+  e0 = bound_x<T, PS<D>::value, true>(a.pos, b0, e0, q.x[0] + w);
 }
 
 // One query per thread.  A warp holds consecutive queries (in sorted mode: consecutive
@@ -1369,7 +1424,16 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
   }
   // row clipping (see TravArgs): the query's distance to the lower and upper edge of its
   // cell in y and z, reduced by the margin; rows near a periodic face are not clipped
-  const bool clip = valid && !(PER && wrap) && (a.unsorted == nullptr || *a.unsorted == 0);
+  // the sort keys stand in for the positions while main slots have moved in place or been
+  // vacated (overflow lists hold points); after a rebuild the positions are the keys
+  T margin = (T)0;
+  bool keyed = false;
+  if (std::is_same<T, float>::value && a.xkey != nullptr) {
+    margin = (T)__ldg(a.delta);
+    keyed = margin > (T)0 || __ldg(&a.ovf_start[g.n_total]) > __ldg(&a.start[g.n_total]);
+  }
+  const bool clip = valid && !(PER && wrap) &&
+                    (keyed || a.unsorted == nullptr || *a.unsorted == 0);
   if constexpr (has_row_hook<F>::value) {
     if (valid && !clip) F::no_rows(acc);  // rows are not single clipped runs here
   }
@@ -1397,16 +1461,19 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
         int32_t b0 = __ldg(&a.start[l0]), e0 = __ldg(&a.start[l0 + 3]);
         PN_RUN(a.err, b0, e0, a.bc_slots);
         if (clip) {
-          clip_row<T, D>(a, q, below, above, oy, oz, b0, e0);
+          clip_row<T, D>(a, q, below, above, oy, oz, b0, e0, margin, keyed);
           if constexpr (has_row_hook<F>::value)
             F::row_begin(acc, p, q, (oz + OZ) * (2 * OY + 1) + (oy + OY), b0, e0);
-          if (b0 >= e0) continue;  // no point of this row is within r
         }
-        scan_any<T, D, PER, F>(a, p, acc, q, wrap, b0, e0);
+        if (b0 < e0) scan_any<T, D, PER, F>(a, p, acc, q, wrap, b0, e0);
         if (a.ovf_start) {
           int32_t ob = __ldg(&a.ovf_start[l0]), oe = __ldg(&a.ovf_start[l0 + 3]);
           PN_RUN(a.err, ob, oe, a.bc_slots);
-          scan_any<T, D, PER, F>(a, p, acc, q, wrap, ob, oe);
+          if (clip && keyed) clip_row<T, D>(a, q, below, above, oy, oz, ob, oe, (T)0, true);
+          if constexpr (has_row_hook<F>::value) {
+            if (clip) F::ovf_begin(acc, ob, oe);
+          }
+          if (ob < oe) scan_any<T, D, PER, F, true>(a, p, acc, q, wrap, ob, oe);
         }
       } else {
 #pragma unroll 1
@@ -1713,15 +1780,135 @@ k_lists_sorted(const TravArgs<T> a, const typename F::Params p) {
   list_query<T, D, PER, F>(a, p, q, (int32_t)k, valid);
 }
 
+// One loop over all the query's neighbours, row by row: the main run's low and high mask
+// word, then (OVF) the overflow run's word.  A lane moves to its next word when it has used
+// up the current one, so lanes with different counts per row do not wait for one another
+// row by row.  The next row's starts and masks are loaded when a row is entered, so a lane
+// that moves on finds them in registers instead of stalling its warp on the load.  A
+// neighbour's slot is the word's base slot plus its bit.
+template <typename T, int D, bool PER, class F, bool OVF>
+__device__ __forceinline__ void walk_masks(const TravArgs<T>& a, const typename F::Params& p,
+                                           typename F::Acc& acc, const Query<T, D>& q,
+                                           int64_t k) {
+  constexpr int NR = D == 3 ? 9 : (D == 2 ? 3 : 1);
+  if constexpr (!OVF) {
+    // wi = 2 row + half indexes the query's 2 NR mask words
+    int wi = 0;
+    int32_t rb0 = __ldg(&a.pc_b0[k]);
+    ulonglong2 m = __ldg(&a.pc_mask[k]);
+    int32_t nb0 = 0;
+    ulonglong2 nm = make_ulonglong2(0ull, 0ull);
+    if (NR > 1) {
+      nb0 = __ldg(&a.pc_b0[a.pc_stride + k]);
+      nm = __ldg(&a.pc_mask[a.pc_stride + k]);
+    }
+    uint64_t w = m.x;
+    for (;;) {
+      while (w == 0) {
+        if (++wi >= 2 * NR) break;
+        if (wi & 1) {
+          w = m.y;
+        } else {
+          rb0 = nb0;
+          m = nm;
+          w = m.x;
+          const int nr = (wi >> 1) + 1;
+          if (nr < NR) {
+            const int64_t o = (int64_t)nr * a.pc_stride + k;
+            nb0 = __ldg(&a.pc_b0[o]);
+            nm = __ldg(&a.pc_mask[o]);
+          }
+        }
+      }
+      if (w == 0) break;
+      const int e = __ffsll((long long)w) - 1;
+      w &= w - 1;
+      const int32_t js = PN_IDX(a.err, BC_NEIGHBOUR, rb0 + 64 * (wi & 1) + e, a.bc_slots);
+      T yj[D], pd[D];
+      const T aux = load_cand<T, D>(a.pos, js, yj);
+      const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
+      F::pair(acc, p, q, js, pd, d2, aux);
+    }
+    return;
+  }
+  constexpr int NP = 3;  // mask words per row: main low, main high, overflow
+  int32_t rb0 = __ldg(&a.pc_b0[k]), nb0 = 0;
+  ulonglong2 m = __ldg(&a.pc_mask[k]), nm = make_ulonglong2(0ull, 0ull);
+  int32_t rob0 = -1, nob0 = -1;
+  uint64_t om = 0ull, nom = 0ull;
+  if constexpr (OVF) {
+    rob0 = __ldg(&a.pc_ob0[k]);
+    if (rob0 >= 0) om = __ldg(&a.pc_omask[k]);
+  }
+  if (NR > 1) {
+    const int64_t o = a.pc_stride + k;
+    nb0 = __ldg(&a.pc_b0[o]);
+    nm = __ldg(&a.pc_mask[o]);
+    if constexpr (OVF) {
+      nob0 = __ldg(&a.pc_ob0[o]);
+      if (nob0 >= 0) nom = __ldg(&a.pc_omask[o]);
+    }
+  }
+  int row = 0, part = 0;
+  int32_t base = rb0;
+  uint64_t w = m.x;
+  for (;;) {
+    while (w == 0) {
+      if (++part < NP) {
+        if (part == 1) {
+          w = m.y;
+          base = rb0 + 64;
+        } else {
+          w = om;
+          base = rob0;
+        }
+        continue;
+      }
+      if (++row >= NR) break;
+      part = 0;
+      rb0 = nb0;
+      m = nm;
+      w = m.x;
+      base = rb0;
+      if constexpr (OVF) {
+        rob0 = nob0;
+        om = nom;
+      }
+      if (row + 1 < NR) {
+        const int64_t o = (int64_t)(row + 1) * a.pc_stride + k;
+        nb0 = __ldg(&a.pc_b0[o]);
+        nm = __ldg(&a.pc_mask[o]);
+        if constexpr (OVF) {
+          nob0 = __ldg(&a.pc_ob0[o]);
+          nom = nob0 >= 0 ? __ldg(&a.pc_omask[o]) : 0ull;
+        }
+      }
+    }
+    if (w == 0) break;
+    const int e = __ffsll((long long)w) - 1;
+    w &= w - 1;
+    const int32_t js = PN_IDX(a.err, BC_NEIGHBOUR, base + e, a.bc_slots);
+    T yj[D], pd[D];
+    const T aux = load_cand<T, D>(a.pos, js, yj);
+    const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
+    F::pair(acc, p, q, js, pd, d2, aux);
+  }
+}
+
 // Cell-sorted queries over the pair cache's hit masks: for every stencil row, the accepted
 // candidates of the row's clipped run, in slot order; queries marked for the fallback are
 // left to the stencil launch after this one.
-template <typename T, int D, bool PER, class F>
+// OVF: the instance for a cache with overflow masks while overflow lists hold points; the
+// other instance returns at once then (each reads the same two words), so the common case
+// keeps the smaller walk and its registers.
+template <typename T, int D, bool PER, class F, bool OVF = false>
 __global__ void __launch_bounds__(TRAV_THREADS, 8)
 k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
   if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
+  const bool ovf_walk = a.pc_ob0 != nullptr && n_slots > __ldg(&a.start[a.g.n_total]);
+  if (ovf_walk != OVF) return;
   Query<T, D> q;
   bool valid = k < n_slots;
   q.i = valid ? a.perm[PN_IDX(a.err, BC_QUERY_SLOT, k, a.bc_slots)] : -1;
@@ -1734,49 +1921,7 @@ k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   load_pos<T, D>(a.pos, k, q.x);
   typename F::Acc acc;
   F::init(acc, p, q);
-  constexpr int NR = D == 3 ? 9 : (D == 2 ? 3 : 1);
-  // One loop over all the query's neighbours (row by row, low then high word): a lane moves
-  // to its next mask word when it has used up the current one, so lanes with different
-  // counts per row do not wait for one another row by row.
-  // wi = 2 row + half indexes the query's 2 NR mask words.  The next row's start and mask
-  // are loaded when a row is entered, so a lane that moves to the next row finds them in
-  // registers instead of stalling its warp on the load.
-  int wi = 0;
-  int32_t rb0 = __ldg(&a.pc_b0[k]);
-  ulonglong2 m = __ldg(&a.pc_mask[k]);
-  int32_t nb0 = 0;
-  ulonglong2 nm = make_ulonglong2(0ull, 0ull);
-  if (NR > 1) {
-    nb0 = __ldg(&a.pc_b0[a.pc_stride + k]);
-    nm = __ldg(&a.pc_mask[a.pc_stride + k]);
-  }
-  uint64_t w = m.x;
-  for (;;) {
-    while (w == 0) {
-      if (++wi >= 2 * NR) break;
-      if (wi & 1) {
-        w = m.y;
-      } else {
-        rb0 = nb0;
-        m = nm;
-        w = m.x;
-        const int nr = (wi >> 1) + 1;
-        if (nr < NR) {
-          const int64_t o = (int64_t)nr * a.pc_stride + k;
-          nb0 = __ldg(&a.pc_b0[o]);
-          nm = __ldg(&a.pc_mask[o]);
-        }
-      }
-    }
-    if (w == 0) break;
-    const int e = __ffsll((long long)w) - 1;
-    w &= w - 1;
-    const int32_t js = PN_IDX(a.err, BC_NEIGHBOUR, rb0 + 64 * (wi & 1) + e, a.bc_slots);
-    T yj[D], pd[D];
-    const T aux = load_cand<T, D>(a.pos, js, yj);
-    const T d2 = pair_geom<T, D, PER>(a.g, q.x, yj, pd);
-    F::pair(acc, p, q, js, pd, d2, aux);
-  }
+  walk_masks<T, D, PER, F, OVF>(a, p, acc, q, k);
   F::finish(acc, p, q);
 }
 

@@ -126,10 +126,20 @@ static int pc_prepare(pn_search* s, int64_t n_rows, MaskParams* m, cudaStream_t 
   int rc = pc_grow(&s->d_pc_b0, &s->pc_b0_cap, nr * n_rows + 1);
   if (rc == PN_OK) rc = pc_grow(&s->d_pc_mask, &s->pc_mask_cap, 2 * (nr * n_rows + 1));
   if (rc != PN_OK) return rc;
+  // overflow lists of a Float32 incremental search: the overflow runs' masks as well
+  const bool ovf = s->ovf_active && s->d_xkey != nullptr;
+  if (ovf) {
+    rc = pc_grow(&s->d_pc_ob0, &s->pc_ob0_cap, nr * n_rows + 1);
+    if (rc == PN_OK) rc = pc_grow(&s->d_pc_omask, &s->pc_omask_cap, nr * n_rows + 1);
+    if (rc != PN_OK) return rc;
+  }
   cudaMemsetAsync(s->d_err + 4, 0, sizeof(int32_t), st);
   *m = MaskParams{s->d_pc_b0, reinterpret_cast<ulonglong2*>(s->d_pc_mask), n_rows,
-                  s->d_err + 4, s->d_err};
+                  s->d_err + 4, s->d_err,
+                  ovf ? s->d_pc_ob0 : nullptr, ovf ? s->d_pc_omask : nullptr,
+                  s->d_ovf_start + s->n_total, s->d_start + s->n_total};
   s->pc_rows = n_rows;
+  s->pc_ovf = ovf;
   return PN_OK;
 }
 
@@ -146,6 +156,18 @@ template <class F>
 struct never_cached { static constexpr bool value = false; };
 template <int D, class G>
 struct never_cached<Mixed<D, G>> { static constexpr bool value = true; };
+
+// The pair cache's walk: with overflow masks, also the instance that walks them (each
+// instance returns at once unless the device state is its case).
+template <typename T, int D, bool PER, class F>
+static void launch_masks(const TravArgs<T>& a, const typename F::Params& p, int blocks,
+                         cudaStream_t st) {
+  k_masks_sorted<T, D, PER, F, false><<<blocks, TRAV_THREADS, 0, st>>>(a, p);
+  if (a.pc_ob0 != nullptr) {
+    k_masks_sorted<T, D, PER, F, true><<<blocks, TRAV_THREADS, 0, st>>>(a, p);
+    count_launch();
+  }
+}
 
 template <typename T, template <typename, int> class F>
 static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename F<T, 1>::Params& p,
@@ -164,13 +186,13 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
       }                                                                                 \
     } else if constexpr (sorted_only<F<T, DD>>::value) {                                \
       if (a.pc_mask != nullptr)                                                         \
-        k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
+        launch_masks<T, DD, PP, F<T, DD>>(a, p, blocks, st);                            \
       else                                                                              \
         k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);      \
       count_launch();                                                                   \
     } else if (a.pc_mask != nullptr && sorted) {                                        \
       if constexpr (!never_cached<F<T, DD>>::value) {                                   \
-        k_masks_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);     \
+        launch_masks<T, DD, PP, F<T, DD>>(a, p, blocks, st);                            \
         count_launch();                                                                 \
       }                                                                                 \
     } else if (a.nb != nullptr) {                                                       \
@@ -276,6 +298,8 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
   a.bc_points = s->n_y;
   a.outside = s->d_err + 1;
   a.unsorted = s->d_err + 3;
+  a.xkey = s->ovf_active ? s->d_xkey : nullptr;
+  a.delta = reinterpret_cast<const float*>(s->d_err + ERR_DELTA);
   if (s->hashed && !s->hash_dense) {  // the hash lists' traversal
     a.hash_list = s->d_hbucket;
     a.hash_cell = s->d_hcell;
@@ -425,6 +449,8 @@ static void use_pair_cache(const pn_search* s, TravArgs<T>& a) {
   a.pc_b0 = s->d_pc_b0;
   a.pc_mask = reinterpret_cast<const ulonglong2*>(s->d_pc_mask);
   a.pc_stride = s->pc_rows;
+  a.pc_ob0 = s->pc_ovf ? s->d_pc_ob0 : nullptr;
+  a.pc_omask = s->pc_ovf ? s->d_pc_omask : nullptr;
   a.nb_len = s->d_pc_b0;  // row 0: negative marks the stencil fallback
   a.nb_fallback = 1;
   a.pc_any_fallback = s->d_err + 4;

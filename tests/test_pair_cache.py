@@ -47,8 +47,9 @@ def _step(P, nhs, x, v):
     return rho, prs, acc, cnt, lists
 
 
-# rebuild_fraction 1: update! keeps overflow lists, whose queries the cache cannot describe
-# (every query falls back to the stencil); periodic: queries near the faces fall back
+# rebuild_fraction 1: update! keeps overflow lists (positions moved in place, rows clipped
+# by the sort keys widened by the largest move; the cache also holds each row's overflow
+# run); periodic: queries near the faces fall back to the stencil
 @pytest.mark.parametrize("fraction,periodic", [(0.01, False), (1.0, False), (0.01, True)])
 def test_pair_cache_equals_stencil(P, O, fraction, periodic):
     W = P.workloads
