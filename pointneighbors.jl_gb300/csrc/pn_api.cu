@@ -32,10 +32,11 @@ void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 static void free_points(pn_search* s) {
   void* ptrs[] = {s->d_cell_of, s->d_slot_of, s->d_tmp_perm, s->d_perm, s->d_cell_of_slot,
                   s->d_pos,     s->d_pa,      s->d_pb,       s->d_main_perm, s->d_ovf_list,
-                  s->d_ovf_cell, s->d_ovf_slot, s->d_pos32, s->d_pos32lo, s->d_xkey};
+                  s->d_ovf_cell, s->d_ovf_slot, s->d_pos32, s->d_pos32lo, s->d_xkey,
+                  s->d_pos32lo2, s->d_sdf};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  s->d_xkey = nullptr;
+  s->d_xkey = s->d_pos32lo2 = s->d_sdf = nullptr;
   s->d_cell_of = s->d_slot_of = s->d_tmp_perm = s->d_perm = s->d_cell_of_slot = nullptr;
   s->d_main_perm = s->d_ovf_list = s->d_ovf_cell = s->d_ovf_slot = nullptr;
   s->d_pos = s->d_pa = s->d_pb = nullptr;
@@ -67,9 +68,13 @@ int ensure_capacity(pn_search* s, int64_t n) {
   alloc(&s->d_pos, tb * 4 * slots);
   alloc(&s->d_pa, tb * 4 * slots);
   alloc(&s->d_pb, tb * 4 * slots);
-  if (s->mixed || (s->dtype == PN_FLOAT64 && !s->hashed))
-    alloc((void**)&s->d_pos32, sizeof(float) * 4 * slots);
-  if (s->mixed) alloc((void**)&s->d_pos32lo, sizeof(float) * 4 * slots);
+  const bool split3 = s->dtype == PN_FLOAT64 && !s->hashed && !s->mixed;
+  if (s->mixed || split3) alloc((void**)&s->d_pos32, sizeof(float) * 4 * slots);
+  if (s->mixed || split3) alloc((void**)&s->d_pos32lo, sizeof(float) * 4 * slots);
+  if (split3 && s->ndims == 3) {
+    alloc((void**)&s->d_pos32lo2, sizeof(float) * 4 * slots);
+    alloc((void**)&s->d_sdf, sizeof(float) * 12 * slots);
+  }
   if (s->dtype == PN_FLOAT32 && !s->mixed && !s->hashed &&
       s->cfg.update_strategy == PN_PARALLEL_INCREMENTAL_UPDATE)
     alloc((void**)&s->d_xkey, sizeof(float) * slots);

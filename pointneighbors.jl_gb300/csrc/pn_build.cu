@@ -1184,28 +1184,34 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   return cuda_status(cudaGetLastError());
 }
 
-// The Float32 split of the cell-sorted coordinates: hi = fl32(x), lo = fl32(x - hi) (x - hi
-// is exact in Float64; lo only for a mixed-precision search, pos32lo null otherwise);
-// vacated slots keep NaN.
+// The Float32 split of the cell-sorted coordinates: hi = fl32(x), lo = fl32(x - hi), lo2 =
+// fl32(x - hi - lo) (each difference exact in Float64; lo2 has at most 5 significant bits,
+// so x = hi + lo + lo2 exactly unless a part underflows); pos32lo / pos32lo2 null when not
+// kept.  Vacated slots keep NaN.
 template <int D>
 __global__ void __launch_bounds__(256)
 k_to_pos32(const double* __restrict__ pos, const int32_t* __restrict__ n_slots,
-           int64_t n_max, float* __restrict__ pos32, float* __restrict__ pos32lo) {
+           int64_t n_max, float* __restrict__ pos32, float* __restrict__ pos32lo,
+           float* __restrict__ pos32lo2) {
   const int64_t n = min((int64_t)*n_slots, n_max);
   constexpr int S = PS<D>::value;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
        k += (int64_t)gridDim.x * blockDim.x) {
     float h[4] = {0.0f, 0.0f, 0.0f, 0.0f}, l[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    float l2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
     for (int d = 0; d < D; ++d) {
       const double x = pos[k * S + d];
       h[d] = __double2float_rn(x);
-      l[d] = __double2float_rn(__dsub_rn(x, (double)h[d]));
+      const double r = __dsub_rn(x, (double)h[d]);
+      l[d] = __double2float_rn(r);
+      l2[d] = __double2float_rn(__dsub_rn(r, (double)l[d]));
     }
 #pragma unroll
     for (int d = 0; d < S; ++d) {
       pos32[k * S + d] = h[d];
       if (pos32lo != nullptr) pos32lo[k * S + d] = l[d];
+      if (pos32lo2 != nullptr) pos32lo2[k * S + d] = l2[d];
     }
   }
 }
@@ -1219,9 +1225,9 @@ void refresh_pos32(pn_search* s, cudaStream_t st) {
   const int b = std::max(1, std::min(div_up(n_max, 256), 152 * 8));
   const double* pos = static_cast<const double*>(s->d_pos);
   switch (s->ndims) {
-    case 1: k_to_pos32<1><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo); break;
-    case 2: k_to_pos32<2><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo); break;
-    default: k_to_pos32<3><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo); break;
+    case 1: k_to_pos32<1><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo, nullptr); break;
+    case 2: k_to_pos32<2><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo, nullptr); break;
+    default: k_to_pos32<3><<<b, 256, 0, st>>>(pos, n_slots, n_max, s->d_pos32, s->d_pos32lo, s->d_pos32lo2); break;
   }
   count_launch();
 }

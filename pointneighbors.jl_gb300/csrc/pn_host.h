@@ -83,6 +83,11 @@ struct pn_search {
   // rows are clipped by while the positions of the main slots move in place; the largest
   // distance of a main slot's x from its key is err word ERR_DELTA
   float* d_xkey = nullptr;             // [slots]
+  // Float64 searches (not hashed): the third part of the coordinates' Float32 split
+  // (x = pos32 + pos32lo + pos32lo2 exactly) and the double-float WCSPH state, for the
+  // double-float sums of the 3D WCSPH sweeps
+  float* d_pos32lo2 = nullptr;         // [slots][4]
+  float* d_sdf = nullptr;              // [slots][12]
   bool main_perm_valid = false;
   double rebuild_fraction = 0.01;      // full rebuild when movers exceed this fraction
   int32_t updates_since_build = 0;

@@ -20,6 +20,7 @@
 // below size_k/2: round() is then 0 and the correction is exactly the identity.
 #pragma once
 
+#include "pn_df.cuh"
 #include "pn_internal.cuh"
 
 namespace pn {
@@ -375,6 +376,25 @@ struct MaskPairParams {
   MaskParams m;
 };
 
+// Double-float sums of the Float64 WCSPH sweeps (the DF64 wrapper): the constants, the
+// three-part Float32 split of the cell-sorted coordinates and the state the force reads.
+struct DFConst {
+  df inv_h, h, dw_coef, eps_h2, m_alpha_c0, m_mass, r_min2;
+  df r2_lo, r2_hi;  // r^2 (1 -+ 1e-12): outside, the double-float d^2 decides
+};
+struct DF64Geom {
+  const float* xa;  // x = xa + xb + xc exactly, cell-sorted, PS<D> floats per slot
+  const float* xb;
+  const float* xc;
+  float4* sdf;      // per slot (p/rho^2, rho), (vx, vy), (vz, -) as double-float pairs
+  DFConst k;
+};
+struct NoDF {};
+template <class F, class = void>
+struct df_acc { using type = NoDF; };
+template <class F>
+struct df_acc<F, std::void_t<typename F::AccDF>> { using type = typename F::AccDF; };
+
 template <class F, class = void>
 struct has_row_hook { static constexpr bool value = false; };
 template <class F>
@@ -387,24 +407,33 @@ struct WithMask {
   static constexpr bool kRowHook = true;
   using Params = MaskPairParams<typename F::Params>;  // the same type for every D
   // lo, hi: the row's main run from b0; om: its overflow run from ob0 (ovf: the row's
-  // candidates now come from the overflow run); ovf_any: the overflow masks are written
-  struct Acc {
-    typename F::Acc f;
+  // candidates now come from the overflow run); ovf_any: the overflow masks are written.
+  // FA: F's accumulator (F::Acc, or F::AccDF for the double-float sums of DF64).
+  template <class FA>
+  struct AccT {
+    FA f;
     int32_t ri, b0, ob0;
     uint64_t lo, hi, om;
     bool fb, ovf, ovf_any;
   };
+  using Acc = AccT<typename F::Acc>;
+  using AccDF = AccT<typename df_acc<F>::type>;
   static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
   static __device__ __forceinline__ void fail(const Params& p, const Query<T, D>& q) { F::fail(p.f, q); }
-  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
-    F::init(a.f, p.f, q);
+  template <class A>
+  static __device__ __forceinline__ void init_mask(A& a, const Params& p) {
     a.ri = -1;
     a.b0 = a.ob0 = 0;
     a.lo = a.hi = a.om = 0;
     a.fb = a.ovf = false;
     a.ovf_any = p.m.ob0 != nullptr && __ldg(p.m.ovf_end) > __ldg(p.m.main_end);
   }
-  static __device__ __forceinline__ void flush(Acc& a, const Params& p, const Query<T, D>& q) {
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<T, D>& q) {
+    F::init(a.f, p.f, q);
+    init_mask(a, p);
+  }
+  template <class A>
+  static __device__ __forceinline__ void flush(A& a, const Params& p, const Query<T, D>& q) {
     if (a.ri < 0) return;
     const int64_t o =
         (int64_t)a.ri * p.m.stride + PN_IDX(p.m.err, BC_PAIR_CACHE, q.k, p.m.stride);
@@ -415,7 +444,8 @@ struct WithMask {
       if (a.om != 0) p.m.omask[o] = a.om;
     }
   }
-  static __device__ __forceinline__ void row_begin(Acc& a, const Params& p, const Query<T, D>& q,
+  template <class A>
+  static __device__ __forceinline__ void row_begin(A& a, const Params& p, const Query<T, D>& q,
                                                    int ri, int32_t b0, int32_t e0) {
     flush(a, p, q);
     a.ri = ri;
@@ -425,15 +455,17 @@ struct WithMask {
     if (e0 - b0 > 128) a.fb = true;
   }
   // the row's overflow run [ob0, oe0) follows its main run
-  static __device__ __forceinline__ void ovf_begin(Acc& a, int32_t ob0, int32_t oe0) {
+  template <class A>
+  static __device__ __forceinline__ void ovf_begin(A& a, int32_t ob0, int32_t oe0) {
     a.ovf = true;
     a.ob0 = ob0;
     if (oe0 > ob0 && (!a.ovf_any || oe0 - ob0 > 64)) a.fb = true;
   }
-  static __device__ __forceinline__ void no_rows(Acc& a) { a.fb = true; }
-  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>& q,
-                                              int32_t js, const T* pd, T d2, T aux) {
-    F::pair(a.f, p.f, q, js, pd, d2, aux);
+  template <class A>
+  static __device__ __forceinline__ void no_rows(A& a) { a.fb = true; }
+  // the accepted candidate js: its bit in the row's mask
+  template <class A>
+  static __device__ __forceinline__ void record(A& a, int32_t js) {
     if (a.ovf) {
       const uint32_t off = (uint32_t)(js - a.ob0);
       if (off < 64) a.om |= 1ull << off;
@@ -442,6 +474,27 @@ struct WithMask {
     const uint32_t off = (uint32_t)(js - a.b0);
     if (off < 64) a.lo |= 1ull << off;
     else if (off < 128) a.hi |= 1ull << (off - 64);
+  }
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>& q,
+                                              int32_t js, const T* pd, T d2, T aux) {
+    F::pair(a.f, p.f, q, js, pd, d2, aux);
+    record(a, js);
+  }
+  // double-float sums (DF64): F's, and the same bits recorded
+  static __device__ __forceinline__ void init_df(AccDF& a, const Params& p,
+                                                 const Query<T, D>& q, const DF64Geom& d) {
+    F::init_df(a.f, p.f, q, d);
+    init_mask(a, p);
+  }
+  static __device__ __forceinline__ void pair_df(AccDF& a, const Params& p, int32_t js,
+                                                 const df* pd, df d2, const DF64Geom& d) {
+    F::pair_df(a.f, p.f, js, pd, d2, d);
+    record(a, js);
+  }
+  static __device__ __forceinline__ void finish_df(AccDF& a, const Params& p,
+                                                   const Query<T, D>& q, const DF64Geom& d) {
+    F::finish_df(a.f, p.f, q, d);
+    end_query(a, p, q);
   }
   // a group of GROUP candidates from slot js0 (a multiple of GROUP past the row's start);
   // the accepted ones are those with d2[u] <= r2
@@ -458,6 +511,10 @@ struct WithMask {
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     F::finish(a.f, p.f, q);
+    end_query(a, p, q);
+  }
+  template <class A>
+  static __device__ __forceinline__ void end_query(A& a, const Params& p, const Query<T, D>& q) {
     flush(a, p, q);
     if (a.fb) {
       p.m.b0[PN_IDX(p.m.err, BC_PAIR_CACHE, q.k, p.m.stride)] = -1;  // row 0's entry marks
@@ -628,6 +685,40 @@ struct FDensity {
       store4(p.pb, q.k, vb);
     }
   }
+
+  // Double-float sum (DF64): the kernel of the Float64 form in double-float arithmetic, the
+  // sum taken in candidate order; finish as the Float64 sum, and the double-float state for
+  // the force sweep.
+  struct AccDF { df w; };
+  static __device__ __forceinline__ void init_df(AccDF& a, const Params&, const Query<T, D>&,
+                                                 const DF64Geom&) {
+    a.w = df_make(0.0f);
+  }
+  static __device__ __forceinline__ void pair_df(AccDF& a, const Params&, int32_t, const df*,
+                                                 df d2, const DF64Geom& d) {
+    const df q = df_mul(df_sqrt(d2), d.k.inv_h);
+    const df t = df_add_f(df_make(__fmul_rn(-0.5f, q.hi), __fmul_rn(-0.5f, q.lo)), 1.0f);
+    if (!(t.hi > 0.0f)) return;  // beyond the support 2h: the Float64 form adds a zero
+    const df t2 = df_sqr(t);
+    const df u = df_add_f(df_make(__fmul_rn(2.0f, q.hi), __fmul_rn(2.0f, q.lo)), 1.0f);
+    a.w = df_add(a.w, df_mul(df_sqr(t2), u));
+  }
+  static __device__ __forceinline__ void finish_df(AccDF& a, const Params& p, const Query<T, D>& q,
+                                                   const DF64Geom& d) {
+    Acc t;
+    t.w = (T)df_to(a.w);
+    finish(t, p, q);
+    if (d.sdf != nullptr && q.k >= 0) {
+      const T rho = p.density[q.i], pr = p.pressure[q.i];
+      const df P = df_from((double)(pr / (rho * rho))), R = df_from((double)rho);
+      df v[3] = {df_make(0.0f), df_make(0.0f), df_make(0.0f)};
+#pragma unroll
+      for (int k = 0; k < D; ++k) v[k] = df_from((double)p.velocity[(int64_t)q.i * D + k]);
+      d.sdf[3 * (int64_t)q.k] = make_float4(P.hi, P.lo, R.hi, R.lo);
+      d.sdf[3 * (int64_t)q.k + 1] = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+      d.sdf[3 * (int64_t)q.k + 2] = make_float4(v[2].hi, v[2].lo, 0.0f, 0.0f);
+    }
+  }
 };
 
 template <typename T, int D>
@@ -674,6 +765,52 @@ struct FForce {
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
 #pragma unroll
     for (int k = 0; k < D; ++k) p.accel[(int64_t)q.i * D + k] = a.a[k];
+  }
+
+  // Double-float sum (DF64): the Float64 form's arithmetic in double-float, the neighbours'
+  // state (p/rho^2, rho, v) from the density sweep's double-float copy.
+  struct AccDF { df a[3], Pi, rhoi, vi[3]; };
+  static __device__ __forceinline__ void init_df(AccDF& a, const Params&, const Query<T, D>& q,
+                                                 const DF64Geom& d) {
+    const float4 s0 = d.sdf[3 * (int64_t)q.k], s1 = d.sdf[3 * (int64_t)q.k + 1],
+                 s2 = d.sdf[3 * (int64_t)q.k + 2];
+    a.Pi = df_make(s0.x, s0.y);
+    a.rhoi = df_make(s0.z, s0.w);
+    a.vi[0] = df_make(s1.x, s1.y);
+    a.vi[1] = df_make(s1.z, s1.w);
+    a.vi[2] = df_make(s2.x, s2.y);
+#pragma unroll
+    for (int k = 0; k < 3; ++k) a.a[k] = df_make(0.0f);
+  }
+  static __device__ __forceinline__ void pair_df(AccDF& a, const Params&, int32_t js,
+                                                 const df* pd, df d2, const DF64Geom& d) {
+    if (df_lt(d2, d.k.r_min2)) return;
+    const float4 s0 = __ldg(&d.sdf[3 * (int64_t)js]), s1 = __ldg(&d.sdf[3 * (int64_t)js + 1]),
+                 s2 = __ldg(&d.sdf[3 * (int64_t)js + 2]);
+    const df vj[3] = {df_make(s1.x, s1.y), df_make(s1.z, s1.w), df_make(s2.x, s2.y)};
+    const df q = df_mul(df_sqrt(d2), d.k.inv_h);
+    const df t = df_add_f(df_make(__fmul_rn(-0.5f, q.hi), __fmul_rn(-0.5f, q.lo)), 1.0f);
+    if (!(t.hi > 0.0f)) return;  // gw = 0: the Float64 form adds zeros
+    const df gw = df_mul(d.k.dw_coef, df_mul(df_sqr(t), t));
+    df vr = df_mul(df_sub(a.vi[0], vj[0]), pd[0]);
+#pragma unroll
+    for (int k = 1; k < D; ++k) vr = df_add(vr, df_mul(df_sub(a.vi[k], vj[k]), pd[k]));
+    // Monaghan: Pi = -alpha c0 mu / rho_mean for approaching pairs (v.x < 0), else 0
+    const df mu = df_div(df_mul(d.k.h, vr), df_add(d2, d.k.eps_h2));
+    df sum = df_add(a.Pi, df_make(s0.x, s0.y));
+    if (vr.hi < 0.0f) {
+      const df rm = df_add(a.rhoi, df_make(s0.z, s0.w));
+      sum = df_add(sum, df_div(df_mul(d.k.m_alpha_c0, mu),
+                               df_make(__fmul_rn(0.5f, rm.hi), __fmul_rn(0.5f, rm.lo))));
+    }
+    const df sc = df_mul(df_mul(d.k.m_mass, sum), gw);
+#pragma unroll
+    for (int k = 0; k < D; ++k) a.a[k] = df_add(a.a[k], df_mul(sc, pd[k]));
+  }
+  static __device__ __forceinline__ void finish_df(AccDF& a, const Params& p, const Query<T, D>& q,
+                                                   const DF64Geom&) {
+#pragma unroll
+    for (int k = 0; k < D; ++k) p.accel[(int64_t)q.i * D + k] = (T)df_to(a.a[k]);
   }
 };
 
@@ -1118,6 +1255,116 @@ struct Exact64Of {
   using type = Exact64<D, F<double, D>>;
 };
 
+// A Float64 search's WCSPH sweeps with their sums in double-float (3D, no periodic box).
+// Like Exact64, the Float32 traversal over the coordinates' Float32 roundings finds a
+// superset of the neighbours; each candidate's pos_diff is then formed from the three-part
+// Float32 splits of the two Float64 positions (df_diff3: the exact difference, kept to
+// double-float precision) and d^2 from it in double-float.  The neighbour test is the
+// Float64 one, decided by the double-float d^2 outside a band of 1e-12 r^2 around r^2 (its
+// error is below 1e-13 d^2) and by the Float64 geometry inside the band.  The accepted
+// pairs go to F's double-float pair function (pair_df).  Neighbour sets are the Float64
+// ones; the sums agree with Float64 ones to about 1e-14 of their terms.
+template <class PF>
+struct DF64Params {
+  PF f;
+  Exact64Geom m;
+  DF64Geom d;
+};
+
+template <int D, class F>
+struct DF64 {
+  static_assert(D == 3, "double-float sweeps are three-dimensional");
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
+  static constexpr bool kRowHook = has_row_hook<F>::value;
+  using Params = DF64Params<typename F::Params>;
+  struct Acc { typename df_acc<F>::type f; float xb[D], xc[D]; };
+  static __device__ __forceinline__ Query<double, D> wide(const Query<float, D>& q,
+                                                          const double* x) {
+    Query<double, D> r;
+    r.i = q.i;
+    r.q = q.q;
+    r.k = q.k;
+#pragma unroll
+    for (int k = 0; k < D; ++k) r.x[k] = x[k];
+    return r;
+  }
+  static __device__ __forceinline__ void vacant(const Params& p, int32_t k) { F::vacant(p.f, k); }
+  static __device__ __forceinline__ void fail(const Params& p, const Query<float, D>& q) {
+    const double z[D] = {};
+    F::fail(p.f, wide(q, z));
+  }
+  static __device__ __forceinline__ void init(Acc& a, const Params& p, const Query<float, D>& q) {
+    const float4 b = __ldg(reinterpret_cast<const float4*>(p.d.xb) + q.k);
+    const float4 c = __ldg(reinterpret_cast<const float4*>(p.d.xc) + q.k);
+    a.xb[0] = b.x; a.xb[1] = b.y; a.xb[2] = b.z;
+    a.xc[0] = c.x; a.xc[1] = c.y; a.xc[2] = c.z;
+    double x[D];
+    load_pos<double, D>(p.m.pos, q.k, x);
+    F::init_df(a.f, p.f, wide(q, x), p.d);
+  }
+  static __device__ __forceinline__ void row_begin(Acc& a, const Params& p,
+                                                   const Query<float, D>& q, int ri, int32_t b0,
+                                                   int32_t e0) {
+    if constexpr (kRowHook) {
+      const double z[D] = {};
+      F::row_begin(a.f, p.f, wide(q, z), ri, b0, e0);
+    }
+  }
+  static __device__ __forceinline__ void no_rows(Acc& a) {
+    if constexpr (kRowHook) F::no_rows(a.f);
+  }
+  static __device__ __forceinline__ void ovf_begin(Acc& a, int32_t ob0, int32_t oe0) {
+    if constexpr (kRowHook) F::ovf_begin(a.f, ob0, oe0);
+  }
+  // q.x: the query's Float32 part xa (the traversal's coordinates)
+  static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<float, D>& q,
+                                              int32_t js, const float*, float, float) {
+    const float4 ya = __ldg(reinterpret_cast<const float4*>(p.d.xa) + js);
+    const float4 yb = __ldg(reinterpret_cast<const float4*>(p.d.xb) + js);
+    const float4 yc = __ldg(reinterpret_cast<const float4*>(p.d.xc) + js);
+    df pd[3];
+    pd[0] = df_diff3(q.x[0], a.xb[0], a.xc[0], ya.x, yb.x, yc.x);
+    pd[1] = df_diff3(q.x[1], a.xb[1], a.xc[1], ya.y, yb.y, yc.y);
+    pd[2] = df_diff3(q.x[2], a.xb[2], a.xc[2], ya.z, yb.z, yc.z);
+    const df d2 = df_add(df_add(df_sqr(pd[0]), df_sqr(pd[1])), df_sqr(pd[2]));
+    bool accept;
+    if (df_lt(d2, p.d.k.r2_lo)) {
+      accept = true;
+    } else if (df_gt(d2, p.d.k.r2_hi)) {
+      accept = false;
+    } else {  // the band: the Float64 geometry decides
+      double xi[D], yj[D], pd64[D];
+      load_pos<double, D>(p.m.pos, q.k, xi);
+      load_pos<double, D>(p.m.pos, js, yj);
+      accept = pair_geom<double, D, false>(p.m.g, xi, yj, pd64) <= p.m.g.r2;
+    }
+    if (accept) F::pair_df(a.f, p.f, js, pd, d2, p.d);
+  }
+  static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<float, D>& q) {
+    double x[D];
+    load_pos<double, D>(p.m.pos, q.k, x);
+    F::finish_df(a.f, p.f, wide(q, x), p.d);
+  }
+};
+
+template <template <typename, int> class F>
+struct DF64Of {
+  template <typename T, int D>
+  using type = DF64<3, F<double, 3>>;
+};
+
+// The Float64 pair functions with double-float sums: the WCSPH density (with or without
+// recording the pair cache) and force.
+template <class F>
+struct df64_ok { static constexpr bool value = false; };
+template <>
+struct df64_ok<FDensity<double, 3>> { static constexpr bool value = true; };
+template <>
+struct df64_ok<FForce<double, 3>> { static constexpr bool value = true; };
+template <>
+struct df64_ok<WithMask<double, 3, FDensity<double, 3>>> { static constexpr bool value = true; };
+
 template <class F>
 struct is_exact64 { static constexpr bool value = false; };
 template <int D, class G>
@@ -1532,6 +1779,8 @@ template <class F>
 struct trav_blocks { static constexpr int value = 8; };
 template <int D, class G>
 struct trav_blocks<Exact64<D, G>> { static constexpr int value = 5; };
+template <int D, class G>
+struct trav_blocks<DF64<D, G>> { static constexpr int value = 5; };
 
 template <typename T, int D, bool PER, class F>
 __global__ void __launch_bounds__(TRAV_THREADS, trav_blocks<F>::value)
@@ -1546,7 +1795,7 @@ k_trav_sorted(const TravArgs<T> a, const typename F::Params p) {
 // hold (nb_len < 0), as a grid-stride loop over the slots on one wave of blocks: with the
 // pair cache's flag clear (no such query) every block returns at once.
 template <typename T, int D, bool PER, class F>
-__global__ void __launch_bounds__(TRAV_THREADS, 8)
+__global__ void __launch_bounds__(TRAV_THREADS, trav_blocks<F>::value)
 k_trav_fallback(const TravArgs<T> a, const typename F::Params p) {
   if (a.pc_any_fallback != nullptr && *a.pc_any_fallback == 0) return;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
@@ -1902,7 +2151,7 @@ __device__ __forceinline__ void walk_masks(const TravArgs<T>& a, const typename 
 // other instance returns at once then (each reads the same two words), so the common case
 // keeps the smaller walk and its registers.
 template <typename T, int D, bool PER, class F, bool OVF = false>
-__global__ void __launch_bounds__(TRAV_THREADS, 8)
+__global__ void __launch_bounds__(TRAV_THREADS, trav_blocks<F>::value)
 k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];

@@ -24,13 +24,23 @@ __global__ void __launch_bounds__(256)
 k_gather_state(const int32_t* __restrict__ perm, const TP* __restrict__ pos, int32_t n_slots_max,
                const int32_t* __restrict__ n_slots, const T* __restrict__ density,
                const T* __restrict__ pressure, const T* __restrict__ velocity,
-               T* __restrict__ pa, T* __restrict__ pb) {
+               T* __restrict__ pa, T* __restrict__ pb, float4* __restrict__ sdf = nullptr) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n_slots_max || k >= *n_slots) return;
   const int32_t i = perm[k];
   if (i < 0) {  // vacated by an incremental update: never a neighbour
     store4(pa, k, V4<T>{(T)NAN, (T)NAN, (T)NAN, (T)0});
     return;
+  }
+  if (sdf != nullptr) {  // the double-float copy (Float64 3D searches)
+    const double rho = (double)density[i];
+    const df P = df_from((double)pressure[i] / (rho * rho)), R = df_from(rho);
+    df v[3] = {df_make(0.0f), df_make(0.0f), df_make(0.0f)};
+#pragma unroll
+    for (int d = 0; d < D; ++d) v[d] = df_from((double)velocity[(int64_t)i * D + d]);
+    sdf[3 * k] = make_float4(P.hi, P.lo, R.hi, R.lo);
+    sdf[3 * k + 1] = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+    sdf[3 * k + 2] = make_float4(v[2].hi, v[2].lo, 0.0f, 0.0f);
   }
   TP x[D];
   load_pos<TP, D>(pos, k, x);
@@ -353,6 +363,83 @@ static MixedGeom mixed_geom(const pn_search* s, TravArgs<double>* a) {
 // coordinates, Mixed<D, F<float, D>> with the geometry m.
 // Float64 sorted queries without a pair cache to walk take the Float32 traversal `fast64`
 // with Exact64<F> when `g64` is given and F is one of exact64_ok's.
+// ------------------------------------------------------------------ double-float sums
+// A Float64 search's 3D WCSPH sweeps take the double-float sums (DF64) when the three-part
+// split of its coordinates is kept (3D, not hashed) and it has no periodic box.
+static bool df64_usable(const pn_search* s) {
+  return s->d_pos32lo2 != nullptr && s->d_sdf != nullptr && s->ndims == 3 && !s->periodic;
+}
+
+static DF64Geom df64_geom(const pn_search* s, const SphConst<double>& c, float* sdf) {
+  DF64Geom d{};
+  d.xa = s->d_pos32;
+  d.xb = s->d_pos32lo;
+  d.xc = s->d_pos32lo2;
+  d.sdf = reinterpret_cast<float4*>(sdf);
+  d.k.inv_h = df_from(c.inv_h);
+  d.k.h = df_from(c.h);
+  d.k.dw_coef = df_from(c.dw_coef);
+  d.k.eps_h2 = df_from(c.eps_h2);
+  d.k.m_alpha_c0 = df_from(-c.alpha * c.c0);
+  d.k.m_mass = df_from(-c.mass);
+  d.k.r_min2 = df_from(c.r_min2);
+  const double r2 = s->radius * s->radius;
+  d.k.r2_lo = df_from(r2 * (1.0 - 1e-12));
+  d.k.r2_hi = df_from(r2 * (1.0 + 1e-12));
+  return d;
+}
+// the WCSPH constants and the double-float state: written by a density sweep that keeps
+// the sorted state, read by the force
+static DF64Geom df64_geom_of(const pn_search* s, const DensityParams<double>& p) {
+  return df64_geom(s, p.c, p.pa != nullptr ? s->d_sdf : nullptr);
+}
+static DF64Geom df64_geom_of(const pn_search* s, const ForceParams<double>& p) {
+  return df64_geom(s, p.c, s->d_sdf);
+}
+template <class P>
+static DF64Geom df64_geom_of(const pn_search* s, const MaskPairParams<P>& p) {
+  return df64_geom_of(s, p.f);
+}
+
+// The double-float sweep: the pair cache's walk (and its stencil fallback) when the cache
+// is on, else the stencil traversal; the Float32 traversal arguments of the search.
+template <class G>
+static int launch_df64(const TravArgs<float>& a, const typename G::Params& p, int64_t n_launch,
+                       cudaStream_t st) {
+  const int blocks = div_up(n_launch, TRAV_THREADS);
+  if (blocks == 0) return PN_OK;
+  if (a.pc_mask != nullptr) {
+    launch_masks<float, 3, false, G>(a, p, blocks, st);
+    count_launch();
+    if (a.nb_fallback) {
+      TravArgs<float> g = a;
+      g.nb = nullptr;
+      g.pc_mask = nullptr;
+      g.pc_b0 = nullptr;
+      g.nb_fallback = 0;
+      k_trav_fallback<float, 3, false, G><<<std::min(blocks, 152 * 8), TRAV_THREADS, 0, st>>>(
+          g, p);
+      count_launch();
+    }
+  } else {
+    k_trav_sorted<float, 3, false, G><<<blocks, TRAV_THREADS, 0, st>>>(a, p);
+    count_launch();
+  }
+  return cuda_status(cudaGetLastError());
+}
+
+// the pair-cache fields of a search's traversal arguments, onto its Float32 traversal's
+static void copy_cache_args(TravArgs<float>& d, const TravArgs<double>& a) {
+  d.pc_b0 = a.pc_b0;
+  d.pc_mask = a.pc_mask;
+  d.pc_stride = a.pc_stride;
+  d.pc_ob0 = a.pc_ob0;
+  d.pc_omask = a.pc_omask;
+  d.nb_len = a.nb_len;
+  d.nb_fallback = a.nb_fallback;
+  d.pc_any_fallback = a.pc_any_fallback;
+}
+
 template <typename T, typename V, template <typename, int> class F>
 static int launch_pair(const pn_search* s, const TravArgs<T>& a, const typename F<V, 1>::Params& p,
                        const MixedGeom& m, bool sorted, int64_t n_launch, cudaStream_t st,
@@ -362,6 +449,14 @@ static int launch_pair(const pn_search* s, const TravArgs<T>& a, const typename 
   if constexpr (std::is_same<T, V>::value) {
     (void)m;
     (void)fast;
+    if constexpr (std::is_same<T, double>::value && df64_ok<F<double, 3>>::value) {
+      if (fast64 != nullptr && g64 != nullptr && sorted && df64_usable(s)) {
+        TravArgs<float> a32 = *fast64;
+        if (a.pc_mask != nullptr) copy_cache_args(a32, a);
+        const DF64Params<typename F<double, 1>::Params> dp{p, *g64, df64_geom_of(s, p)};
+        return launch_df64<DF64<3, F<double, 3>>>(a32, dp, n_launch, st);
+      }
+    }
     if constexpr (std::is_same<T, double>::value && exact64_ok<F<double, 3>>::value) {
       if (fast64 != nullptr && g64 != nullptr && a.pc_mask == nullptr && sorted &&
           s->ndims >= 2) {

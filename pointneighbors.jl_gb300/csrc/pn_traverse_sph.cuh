@@ -44,7 +44,12 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
           } else {
             bool via32 = false;  // Float64: the Float32 traversal, each candidate in Float64
             if constexpr (std::is_same<T, double>::value) {
-              if (c.fast64 && s->ndims >= 2) {
+              if (c.fast64 && df64_usable(s)) {  // sums in double-float
+                const DF64Params<MaskPairParams<DensityParams<V>>> dp{
+                    pp, c.g64, df64_geom(s, p.c, p.pa != nullptr ? s->d_sdf : nullptr)};
+                rc = launch_df64<DF64<3, FDensityMask<double, 3>>>(c.a32, dp, n_launch, st);
+                via32 = true;
+              } else if (c.fast64 && s->ndims >= 2) {
                 const Exact64Params<MaskPairParams<DensityParams<V>>> ep{pp, c.g64};
                 rc = launch_trav<float, Exact64Of<FDensityMask>::template type>(
                     s, c.a32, ep, sorted, n_launch, st);
@@ -83,7 +88,7 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
         switch (s->ndims) {
           case 1: k_gather_state<T, V, 1><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
           case 2: k_gather_state<T, V, 2><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
-          default: k_gather_state<T, V, 3><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb); count_launch(); break;
+          default: k_gather_state<T, V, 3><<<b, 256, 0, st>>>(s->d_perm, pos, ns, n_slots, dn, pr, ve, pa, pb, reinterpret_cast<float4*>(s->d_sdf)); count_launch(); break;
         }
       }
       ForceParams<V> pf{sph_const<V>(s, u), pa, pb, static_cast<V*>(u->accel)};
