@@ -75,21 +75,25 @@ __device__ __forceinline__ df df_sqr(df a) {
   p.lo = __fmaf_rn(__fmul_rn(2.0f, a.hi), a.lo, p.lo);
   return fast_two_sum(p.hi, p.lo);
 }
-// a / b: the Float32 quotient q1, the remainder a - q1 b in double-float, one correction
+// a / b (0 < |b| < 2^126): the Float32 quotient q1, the remainder a - q1 b in
+// double-float (exact for any q1), a second quotient and remainder, a last correction.  The
+// remainders are exact, so the Float32 quotients need not be correctly rounded: each
+// approximate quotient (a few ulp) only enlarges the next, smaller correction.
 __device__ __forceinline__ df df_div(df a, df b) {
-  const float q1 = __fdiv_rn(a.hi, b.hi);
+  const float q1 = __fdividef(a.hi, b.hi);
   const df r = df_sub(a, df_mul_f(b, q1));
-  const float q2 = __fdiv_rn(r.hi, b.hi);
+  const float q2 = __fdividef(r.hi, b.hi);
   df q = fast_two_sum(q1, q2);
   const df r2 = df_sub(r, df_mul_f(b, q2));
-  return df_add_f(q, __fdiv_rn(r2.hi, b.hi));
+  return df_add_f(q, __fdividef(r2.hi, b.hi));
 }
-// sqrt(a), a >= 0: s = sqrt(a.hi), then s + (a - s^2) / (2 s)
+// sqrt(a), a >= 0: s = sqrt(a.hi) correctly rounded, then s + (a - s^2) / (2 s) (one Newton
+// step; the correction is 2^-24 of s, so its own few-ulp quotient error is 2^-46 of s)
 __device__ __forceinline__ df df_sqrt(df a) {
   if (!(a.hi > 0.0f)) return df{0.0f, 0.0f};
   const float s = __fsqrt_rn(a.hi);
   const df e = df_sub(a, two_prod(s, s));
-  return fast_two_sum(s, __fdiv_rn(e.hi, __fmul_rn(2.0f, s)));
+  return fast_two_sum(s, __fdividef(e.hi, __fmul_rn(2.0f, s)));
 }
 __device__ __forceinline__ bool df_lt(df a, df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
 __device__ __forceinline__ bool df_gt(df a, df b) { return df_lt(b, a); }

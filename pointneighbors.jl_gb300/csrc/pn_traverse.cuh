@@ -379,7 +379,7 @@ struct MaskPairParams {
 // Double-float sums of the Float64 WCSPH sweeps (the DF64 wrapper): the constants, the
 // three-part Float32 split of the cell-sorted coordinates and the state the force reads.
 struct DFConst {
-  df inv_h, h, dw_coef, eps_h2, m_alpha_c0, m_mass, r_min2;
+  df inv_h, h, dw_coef, eps_h2, m_alpha_c0_h, m_mass, r_min2;
   df r2_lo, r2_hi;  // r^2 (1 -+ 1e-12): outside, the double-float d^2 decides
 };
 struct DF64Geom {
@@ -755,9 +755,11 @@ struct FForce {
     T vr = (T)0;
 #pragma unroll
     for (int k = 0; k < D; ++k) vr += (a.vi[k] - vj[k]) * pd[k];
-    // Monaghan: Pi = -alpha c0 mu / rho_mean for approaching pairs (v.x < 0), else 0
-    const T mu = fdiv(p.c.h * vr, d2 + p.c.eps_h2);
-    const T visc = vr < (T)0 ? fdiv(-p.c.alpha * p.c.c0 * mu, (T)0.5 * (a.rhoi + sb.w)) : (T)0;
+    // Monaghan: Pi = -alpha c0 mu / rho_mean, mu = h v.x / (d^2 + eps h^2), for approaching
+    // pairs (v.x < 0), else 0 -- one quotient: -alpha c0 h v.x / ((d^2 + eps h^2) rho_mean)
+    const T visc = vr < (T)0 ? fdiv(-p.c.alpha * p.c.c0 * p.c.h * vr,
+                                    (d2 + p.c.eps_h2) * ((T)0.5 * (a.rhoi + sb.w)))
+                             : (T)0;
     const T s = -p.c.mass * (a.Pi + Pj + visc) * gw;
 #pragma unroll
     for (int k = 0; k < D; ++k) a.a[k] += s * pd[k];
@@ -795,13 +797,14 @@ struct FForce {
     df vr = df_mul(df_sub(a.vi[0], vj[0]), pd[0]);
 #pragma unroll
     for (int k = 1; k < D; ++k) vr = df_add(vr, df_mul(df_sub(a.vi[k], vj[k]), pd[k]));
-    // Monaghan: Pi = -alpha c0 mu / rho_mean for approaching pairs (v.x < 0), else 0
-    const df mu = df_div(df_mul(d.k.h, vr), df_add(d2, d.k.eps_h2));
+    // Monaghan: Pi = -alpha c0 h v.x / ((d^2 + eps h^2) rho_mean) for approaching pairs
+    // (v.x < 0), else 0
     df sum = df_add(a.Pi, df_make(s0.x, s0.y));
     if (vr.hi < 0.0f) {
       const df rm = df_add(a.rhoi, df_make(s0.z, s0.w));
-      sum = df_add(sum, df_div(df_mul(d.k.m_alpha_c0, mu),
-                               df_make(__fmul_rn(0.5f, rm.hi), __fmul_rn(0.5f, rm.lo))));
+      const df den = df_mul(df_add(d2, d.k.eps_h2),
+                            df_make(__fmul_rn(0.5f, rm.hi), __fmul_rn(0.5f, rm.lo)));
+      sum = df_add(sum, df_div(df_mul(d.k.m_alpha_c0_h, vr), den));
     }
     const df sc = df_mul(df_mul(d.k.m_mass, sum), gw);
 #pragma unroll

@@ -380,7 +380,7 @@ static DF64Geom df64_geom(const pn_search* s, const SphConst<double>& c, float* 
   d.k.h = df_from(c.h);
   d.k.dw_coef = df_from(c.dw_coef);
   d.k.eps_h2 = df_from(c.eps_h2);
-  d.k.m_alpha_c0 = df_from(-c.alpha * c.c0);
+  d.k.m_alpha_c0_h = df_from(-c.alpha * c.c0 * c.h);
   d.k.m_mass = df_from(-c.mass);
   d.k.r_min2 = df_from(c.r_min2);
   const double r2 = s->radius * s->radius;
