@@ -381,6 +381,10 @@ struct MaskPairParams {
 struct DFConst {
   df inv_h, h, dw_coef, eps_h2, m_alpha_c0_h, m_mass, r_min2;
   df r2_lo, r2_hi;  // r^2 (1 -+ 1e-12): outside, the double-float d^2 decides
+  // below this Float32 d^2 of the traversal a candidate is certainly a neighbour: the
+  // traversal's distance is within rs - r of the exact one (rs: its widened radius), so
+  // d_32 < 2r - rs means d < r
+  float r_in2;
 };
 struct DF64Geom {
   const float* xa;  // x = xa + xb + xc exactly, cell-sorted, PS<D> floats per slot
@@ -906,7 +910,41 @@ struct FAdjointBackward {
 };
 
 // Pair functions that build the pair cache while they run.
+// No pair arithmetic: with WithMask, a sweep that only records the pair cache.  The Float64
+// WCSPH density in double-float (DF64) records its neighbours this way and then sums over
+// the cache, so that the double-float work runs in the cache walk's lanes.
+struct NoneParams { int32_t pad_; };
+template <typename T, int D>
+struct FNone {
+  static constexpr bool kCountOnly = false;
+  static constexpr bool kInline = false;
+  using Params = NoneParams;
+  struct Acc {};
+  struct AccDF {};
+  static __device__ __forceinline__ void vacant(const Params&, int32_t) {}
+  static __device__ __forceinline__ void fail(const Params&, const Query<T, D>&) {}
+  static __device__ __forceinline__ void init(Acc&, const Params&, const Query<T, D>&) {}
+  static __device__ __forceinline__ void pair(Acc&, const Params&, const Query<T, D>&, int32_t,
+                                              const T*, T, T) {}
+  static __device__ __forceinline__ void finish(Acc&, const Params&, const Query<T, D>&) {}
+  static __device__ __forceinline__ void init_df(AccDF&, const Params&, const Query<T, D>&,
+                                                 const DF64Geom&) {}
+  static __device__ __forceinline__ void pair_df(AccDF&, const Params&, int32_t, const df*, df,
+                                                 const DF64Geom&) {}
+  static __device__ __forceinline__ void finish_df(AccDF&, const Params&, const Query<T, D>&,
+                                                   const DF64Geom&) {}
+};
+// Pair functions whose accepted pairs need no pos_diff or d^2 (DF64 decides them from the
+// Float32 d^2 where that is certain)
+template <class F>
+struct df_no_geometry { static constexpr bool value = false; };
+template <typename T, int D>
+struct df_no_geometry<FNone<T, D>> { static constexpr bool value = true; };
+template <typename T, int D, class G>
+struct df_no_geometry<WithMask<T, D, G>> { static constexpr bool value = df_no_geometry<G>::value; };
+
 template <typename T, int D> using FDensityMask = WithMask<T, D, FDensity<T, D>>;
+template <typename T, int D> using FNoneMask = WithMask<T, D, FNone<T, D>>;
 template <typename T, int D> using FAdjointForwardMask = WithMask<T, D, FAdjointForward<T, D>>;
 
 // ================================================================== traversal kernel
@@ -1320,9 +1358,16 @@ struct DF64 {
   static __device__ __forceinline__ void ovf_begin(Acc& a, int32_t ob0, int32_t oe0) {
     if constexpr (kRowHook) F::ovf_begin(a.f, ob0, oe0);
   }
-  // q.x: the query's Float32 part xa (the traversal's coordinates)
+  // q.x: the query's Float32 part xa (the traversal's coordinates); d2_32: the traversal's
+  // Float32 d^2
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<float, D>& q,
-                                              int32_t js, const float*, float, float) {
+                                              int32_t js, const float*, float d2_32, float) {
+    if constexpr (df_no_geometry<F>::value) {  // only the decision is wanted
+      if (d2_32 < p.d.k.r_in2) {
+        F::pair_df(a.f, p.f, js, nullptr, df_make(0.0f), p.d);
+        return;
+      }
+    }
     const float4 ya = __ldg(reinterpret_cast<const float4*>(p.d.xa) + js);
     const float4 yb = __ldg(reinterpret_cast<const float4*>(p.d.xb) + js);
     const float4 yc = __ldg(reinterpret_cast<const float4*>(p.d.xc) + js);

@@ -370,7 +370,8 @@ static bool df64_usable(const pn_search* s) {
   return s->d_pos32lo2 != nullptr && s->d_sdf != nullptr && s->ndims == 3 && !s->periodic;
 }
 
-static DF64Geom df64_geom(const pn_search* s, const SphConst<double>& c, float* sdf) {
+static DF64Geom df64_geom(const pn_search* s, const SphConst<double>& c, float* sdf,
+                          double rs = 0.0) {
   DF64Geom d{};
   d.xa = s->d_pos32;
   d.xb = s->d_pos32lo;
@@ -386,6 +387,8 @@ static DF64Geom df64_geom(const pn_search* s, const SphConst<double>& c, float* 
   const double r2 = s->radius * s->radius;
   d.k.r2_lo = df_from(r2 * (1.0 - 1e-12));
   d.k.r2_hi = df_from(r2 * (1.0 + 1e-12));
+  const double r_in = 2.0 * s->radius - rs;  // rs = 0: no Float32 decision
+  d.k.r_in2 = rs > 0.0 && r_in > 0.0 ? (float)(r_in * r_in * (1.0 - 1e-6)) : 0.0f;
   return d;
 }
 // the WCSPH constants and the double-float state: written by a density sweep that keeps

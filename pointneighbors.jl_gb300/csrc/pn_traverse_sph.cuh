@@ -33,6 +33,22 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
       }
       int rc = PN_OK;
       bool done = false;
+      if constexpr (std::is_same<T, double>::value && !kMixed) {
+        if (cache_on && !s->pc_valid && c.fast64 && df64_usable(s)) {
+          // double-float sums: record the neighbours (decisions only), then sum over the
+          // cache below
+          MaskPairParams<NoneParams> pm{NoneParams{}, {}};
+          rc = pc_prepare(s, n_sorted, &pm.m, st);
+          if (rc == PN_OK) {
+            const DF64Params<MaskPairParams<NoneParams>> dp{
+                pm, c.g64, df64_geom(s, p.c, nullptr, (double)c.a32.g.r)};
+            rc = launch_df64<DF64<3, FNoneMask<double, 3>>>(c.a32, dp, n_launch, st);
+          }
+          if (rc != PN_OK) return rc;
+          s->pc_valid = true;
+          use_cache();
+        }
+      }
       if (cache_on && !s->pc_valid) {
         MaskPairParams<DensityParams<V>> pp{p, {}};
         rc = pc_prepare(s, n_sorted, &pp.m, st);
@@ -44,12 +60,7 @@ int foreach_sph(pn_search* s, int32_t functor, int64_t n_x, const void* params,
           } else {
             bool via32 = false;  // Float64: the Float32 traversal, each candidate in Float64
             if constexpr (std::is_same<T, double>::value) {
-              if (c.fast64 && df64_usable(s)) {  // sums in double-float
-                const DF64Params<MaskPairParams<DensityParams<V>>> dp{
-                    pp, c.g64, df64_geom(s, p.c, p.pa != nullptr ? s->d_sdf : nullptr)};
-                rc = launch_df64<DF64<3, FDensityMask<double, 3>>>(c.a32, dp, n_launch, st);
-                via32 = true;
-              } else if (c.fast64 && s->ndims >= 2) {
+              if (c.fast64 && s->ndims >= 2) {
                 const Exact64Params<MaskPairParams<DensityParams<V>>> ep{pp, c.g64};
                 rc = launch_trav<float, Exact64Of<FDensityMask>::template type>(
                     s, c.a32, ep, sorted, n_launch, st);
