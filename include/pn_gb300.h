@@ -21,6 +21,12 @@
  *  - The pair function is a compile-time functor picked by `functor` (pn_functor); an
  *    arbitrary Julia closure cannot be compiled into the library, and there is no CPU
  *    fallback: unknown functors return PN_ERR_UNSUPPORTED_FUNCTOR.
+ *  - Float64 searches decide every neighbour by the reference's Float64 test.  For the 3D
+ *    WCSPH density and force of a Float64 search without a periodic box, the pair
+ *    arithmetic itself runs in double-float (pairs of Float32 numbers, about 48 significant
+ *    bits; GB300's Float64 units are slow): the sums agree with Float64 sums to about 1e-14
+ *    of the sum of their terms' magnitudes.  The other Float64 pair functions and periodic
+ *    or 2D searches compute in Float64.
  */
 #ifndef PN_GB300_H
 #define PN_GB300_H
