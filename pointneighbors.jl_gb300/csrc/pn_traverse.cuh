@@ -2195,17 +2195,36 @@ __device__ __forceinline__ void walk_masks(const TravArgs<T>& a, const typename 
 // Cell-sorted queries over the pair cache's hit masks: for every stencil row, the accepted
 // candidates of the row's clipped run, in slot order; queries marked for the fallback are
 // left to the stencil launch after this one.
+template <typename T, int D, bool PER, class F, bool OVF>
+__device__ __forceinline__ void mask_query(const TravArgs<T>& a, const typename F::Params& p,
+                                           int64_t k, int32_t n_slots);
+
 // OVF: the instance for a cache with overflow masks while overflow lists hold points; the
 // other instance returns at once then (each reads the same two words), so the common case
-// keeps the smaller walk and its registers.
-template <typename T, int D, bool PER, class F, bool OVF = false>
+// keeps the smaller walk and its registers.  STRIDE: grid-stride over the queries (launched
+// on one wave of blocks, so that it costs little when it returns at once; the host takes it
+// when the last update it knows of kept no point in an overflow list).
+template <typename T, int D, bool PER, class F, bool OVF = false, bool STRIDE = false>
 __global__ void __launch_bounds__(TRAV_THREADS, trav_blocks<F>::value)
 k_masks_sorted(const TravArgs<T> a, const typename F::Params p) {
-  const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t n_slots = a.ovf_start ? a.ovf_start[a.g.n_total] : a.start[a.g.n_total];
-  if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
   const bool ovf_walk = a.pc_ob0 != nullptr && n_slots > __ldg(&a.start[a.g.n_total]);
   if (ovf_walk != OVF) return;
+  if constexpr (STRIDE) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n_slots; k += stride)
+      mask_query<T, D, PER, F, OVF>(a, p, k, n_slots);
+  } else {
+    const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if ((int64_t)blockIdx.x * blockDim.x >= n_slots) return;  // whole block idle
+    mask_query<T, D, PER, F, OVF>(a, p, k, n_slots);
+  }
+}
+
+// One cell-sorted query of the pair cache's walk.
+template <typename T, int D, bool PER, class F, bool OVF>
+__device__ __forceinline__ void mask_query(const TravArgs<T>& a, const typename F::Params& p,
+                                           int64_t k, int32_t n_slots) {
   Query<T, D> q;
   bool valid = k < n_slots;
   q.i = valid ? a.perm[PN_IDX(a.err, BC_QUERY_SLOT, k, a.bc_slots)] : -1;

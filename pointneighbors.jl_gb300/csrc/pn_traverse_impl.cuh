@@ -168,13 +168,20 @@ template <int D, class G>
 struct never_cached<Mixed<D, G>> { static constexpr bool value = true; };
 
 // The pair cache's walk: with overflow masks, also the instance that walks them (each
-// instance returns at once unless the device state is its case).
+// instance returns at once unless the device state is its case).  ovf_likely: the last
+// update known to the host kept points in overflow lists; the overflow instance then gets
+// the full grid, else one wave of blocks (grid-stride), which costs little when it returns
+// at once.  Either grid covers every query.
 template <typename T, int D, bool PER, class F>
 static void launch_masks(const TravArgs<T>& a, const typename F::Params& p, int blocks,
-                         cudaStream_t st) {
+                         cudaStream_t st, bool ovf_likely = false) {
   k_masks_sorted<T, D, PER, F, false><<<blocks, TRAV_THREADS, 0, st>>>(a, p);
   if (a.pc_ob0 != nullptr) {
-    k_masks_sorted<T, D, PER, F, true><<<blocks, TRAV_THREADS, 0, st>>>(a, p);
+    if (ovf_likely)
+      k_masks_sorted<T, D, PER, F, true, false><<<blocks, TRAV_THREADS, 0, st>>>(a, p);
+    else
+      k_masks_sorted<T, D, PER, F, true, true>
+          <<<std::min(blocks, 152 * trav_blocks<F>::value), TRAV_THREADS, 0, st>>>(a, p);
     count_launch();
   }
 }
@@ -196,13 +203,13 @@ static int launch_trav(const pn_search* s, const TravArgs<T>& a, const typename 
       }                                                                                 \
     } else if constexpr (sorted_only<F<T, DD>>::value) {                                \
       if (a.pc_mask != nullptr)                                                         \
-        launch_masks<T, DD, PP, F<T, DD>>(a, p, blocks, st);                            \
+        launch_masks<T, DD, PP, F<T, DD>>(a, p, blocks, st, s->n_ovf > 0);              \
       else                                                                              \
         k_trav_sorted<T, DD, PP, F<T, DD>><<<blocks, TRAV_THREADS, 0, st>>>(a, p);      \
       count_launch();                                                                   \
     } else if (a.pc_mask != nullptr && sorted) {                                        \
       if constexpr (!never_cached<F<T, DD>>::value) {                                   \
-        launch_masks<T, DD, PP, F<T, DD>>(a, p, blocks, st);                            \
+        launch_masks<T, DD, PP, F<T, DD>>(a, p, blocks, st, s->n_ovf > 0);              \
         count_launch();                                                                 \
       }                                                                                 \
     } else if (a.nb != nullptr) {                                                       \
