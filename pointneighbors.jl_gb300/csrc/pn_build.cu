@@ -380,7 +380,9 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
               int32_t* __restrict__ ovf_counts, int32_t* __restrict__ ovf_n,
               int32_t* __restrict__ ovf_list, int32_t* __restrict__ ovf_cell,
               int32_t* __restrict__ ovf_slot, int32_t* __restrict__ outside,
-              int32_t* __restrict__ err, const float* __restrict__ xkey) {
+              int32_t* __restrict__ err, const float* __restrict__ xkey,
+              int32_t* __restrict__ cell_of, int32_t* __restrict__ slot_of,
+              int32_t* __restrict__ counts) {
   const int lane = threadIdx.x & 31;
   const int32_t nm = *n_main;
   int32_t ovf_max = 0;  // the largest overflow list this thread has seen grow
@@ -391,6 +393,7 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
     int32_t cell = -1;
     bool moved = false;
     int32_t i = -1;
+    int32_t hcell = -1;  // the point's current cell, for the rebuild's histogram
     if (k < nm) {
       i = main_perm[k];
       T p[D];
@@ -406,6 +409,7 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
         stride *= g.n[d];
       }
       if (PER && out && *(volatile int32_t*)outside == 0) atomicExch(outside, 1);
+      if (ok) hcell = lin;
       if (!ok) {
         set_error(err, PN_ERR_OUT_OF_DOMAIN);
       } else if (lin == cell_of_slot[k]) {
@@ -426,6 +430,20 @@ k_mark_movers(const GridDev<T> g, const int32_t* __restrict__ main_perm,
         store_pos<T, D>(pos, k, nan_p);
       }
     }
+    // The rebuild's histogram, as k_bin would make it (cell and rank per point index): the
+    // rebuild path then needs no bin of its own.  `base` is uniform over the block, so
+    // every lane of the warp reaches the ballots.
+    const unsigned hv = __ballot_sync(0xffffffffu, hcell >= 0);
+    if (hcell >= 0) {
+      const unsigned peers = __match_any_sync(hv, hcell);
+      const int leader = __ffs(peers) - 1;
+      int32_t hb = 0;
+      if (lane == leader)
+        hb = atomicAdd(&counts[PN_IDX(err, BC_CELL, hcell, g.n_total)], __popc(peers));
+      hb = __shfl_sync(peers, hb, leader);
+      slot_of[i] = hb + __popc(peers & lanemask_lt());
+    }
+    if (k < nm) cell_of[i] = hcell;
     // Movers: one list entry each (warp-aggregated), plus their rank in the new cell.
     const unsigned mv = __ballot_sync(0xffffffffu, moved);
     if (mv) {
@@ -510,14 +528,6 @@ __global__ void k_decide_update(const int32_t* __restrict__ ovf_n,
     gate[0] = m;
     gate[1] = m == GATE_OVERFLOW ? 1 : 0;
   }
-}
-
-__global__ void __launch_bounds__(256)
-k_zero_if_rebuild(int32_t* __restrict__ a, int32_t n, const int32_t* __restrict__ gate) {
-  if (*gate != GATE_REBUILD) return;
-  for (int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x)
-    a[c] = 0;
 }
 
 // After a rebuild the new structure is the main one: empty overflow lists, main_perm = perm.
@@ -1109,7 +1119,8 @@ static void launch_mark(pn_search* s, const T* y, cudaStream_t st) {
   k_mark_movers<T, D, PER><<<blocks, 256, 0, st>>>(
       make_grid<T>(s), s->d_main_perm, s->d_cell_of_slot, s->d_start + s->n_total, y,
       s->d_perm, static_cast<T*>(s->d_pos), s->d_ovf_counts, s->d_ovf_n, s->d_ovf_list,
-      s->d_ovf_cell, s->d_ovf_slot, s->d_err + 1, s->d_err, s->d_xkey); count_launch();
+      s->d_ovf_cell, s->d_ovf_slot, s->d_err + 1, s->d_err, s->d_xkey, s->d_cell_of,
+      s->d_slot_of, s->d_counts); count_launch();
 }
 
 template <typename T, int D>
@@ -1139,6 +1150,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   cudaMemsetAsync(build_stats(s), 0, 2 * sizeof(int32_t), st);
   cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
   cudaMemsetAsync(s->d_err + ERR_DELTA, 0, sizeof(int32_t), st);
+  cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * s->n_total, st);  // the mark's histogram
   const bool per = s->periodic != 0;
   switch (s->ndims * 2 + (per ? 1 : 0)) {
     case 2: launch_mark<T, 1, false>(s, y, st); break;
@@ -1159,11 +1171,9 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
     case 2: launch_movers<T, 2>(s, y, st); break;
     default: launch_movers<T, 3>(s, y, st); break;
   }
-  // rebuild path (every point is binned: the incremental strategy has no eachindex_y)
+  // rebuild path (every point is binned: the incremental strategy has no eachindex_y); the
+  // histogram is the mark kernel's
   const int32_t m = (int32_t)s->n_binned;
-  k_zero_if_rebuild<<<std::max(1, std::min(div_up(s->n_total, 256), 152 * 4)), 256, 0, st>>>(
-      s->d_counts, s->n_total, gate); count_launch();
-  dispatch_bin<T>(s, y, n_y, nullptr, m, st, gate);
   scan_cells(s, s->d_counts, s->d_start, st, nullptr, s->cfg.max_points_per_cell, gate,
              GATE_REBUILD);
   k_scatter<<<div_up(m, 256), 256, 0, st>>>(s->d_cell_of, s->d_slot_of, nullptr, m, s->d_start,
