@@ -49,8 +49,9 @@ struct TravArgs {
   // stencil row's three cells are one x-sorted run and a query only scans the part of it
   // within x +- sqrt(r^2 - dy^2 - dz^2) (dy, dz: distance to the row's band).  `unsorted`
   // (device flag, or null = sorted) is set while an incremental update keeps overflow lists
-  // (positions refreshed in place); `clip_m` is a per-dimension margin that covers the
-  // rounding of the cell edges, so the clipped run is always a superset of the neighbours.
+  // (positions refreshed in place): then the rows are clipped by `xkey` below, or not at all
+  // where there is none; `clip_m` is a per-dimension margin that covers the rounding of the
+  // cell edges, so the clipped run is always a superset of the neighbours.
   const int32_t* unsorted;
   T clip_m[3];
   // Float32 incremental searches with overflow lists (or null): the rows are clipped by the

@@ -7,7 +7,8 @@ step sequence on the 200^3 = 8,000,000-point FP32 lattice and compares a sample 
 query points with the oracle, which bins all 8M points: neighbour counts bit-exact (counted
 over the same pair cache), density and acceleration within 1e-5 of the sum of |terms|.
 With rebuild_fraction 0.01 every update! rebuilds (about 8 % of the points change cell per
-step); with 1.0 it keeps overflow lists, whose queries leave the cache for the stencil.
+step); with 1.0 it keeps overflow lists: the rows are clipped by the sort keys widened by
+the largest in-place move, and the cache also holds each row's overflow run.
 """
 import numpy as np
 import pytest
