@@ -279,6 +279,11 @@ static int create(const pn_config* cfg, int64_t list_size, pn_search** out,
          cudaMalloc(&s->d_ovf_start, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
          cudaMalloc(&s->d_ovf_n, sizeof(int32_t) * 4) == cudaSuccess &&
          cudaMalloc(&s->d_scan_state, sizeof(unsigned long long) * (s->scan_tiles + 1)) == cudaSuccess;
+    if (ok && !s->hashed && !s->mixed && s->dtype == PN_FLOAT32 &&
+        s->cfg.update_strategy == PN_PARALLEL_INCREMENTAL_UPDATE) {
+      ok = cudaMalloc(&s->d_cell_delta, sizeof(float) * nt) == cudaSuccess &&
+           cudaMemset(s->d_cell_delta, 0, sizeof(float) * nt) == cudaSuccess;
+    }
     if (ok && s->hashed)
       ok = cudaMalloc(&s->d_hbucket, sizeof(int32_t) * (nt + 1)) == cudaSuccess &&
            cudaMalloc(&s->d_hbbox, sizeof(int32_t) * 6) == cudaSuccess &&
@@ -396,6 +401,7 @@ int pn_destroy(pn_search* s) {
   if (!s) return PN_OK;
   free_points(s);
   void* ptrs[] = {s->d_err,       s->d_counts,     s->d_start,     s->d_scan_state,
+                  s->d_cell_delta,
                   s->d_ovf_counts, s->d_ovf_start,  s->d_ovf_n,     s->d_qcount,
                   s->d_part,       s->d_sort_tmp,   s->d_sum_part,  s->d_pc_b0,
                   s->d_pc_mask,    s->d_pc_ob0,     s->d_pc_omask,  s->d_hkey_t,

@@ -530,6 +530,39 @@ __global__ void k_decide_update(const int32_t* __restrict__ ovf_n,
   }
 }
 
+// Overflow path only: per cell the largest |x - xkey| of its main slots moved in place (the
+// rows' clipping margins, cell_delta zeroed by the caller).  Slots are cell-sorted, so a
+// warp's lanes mostly share a cell: one atomic per cell and warp; the distances are >= 0,
+// so their bits order like the values.
+template <int S>
+__global__ void __launch_bounds__(256)
+k_cell_delta(const float* __restrict__ pos, const float* __restrict__ xkey,
+             const int32_t* __restrict__ perm, const int32_t* __restrict__ cell_of_slot,
+             const int32_t* __restrict__ n_main, int32_t n_total, float* __restrict__ cell_delta,
+             const int32_t* __restrict__ gate, int32_t* __restrict__ err) {
+  if (*gate != GATE_OVERFLOW) return;
+  const int32_t nm = *n_main;
+  const int lane = threadIdx.x & 31;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x; base < nm;
+       base += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = base + threadIdx.x;
+    int32_t cell = -1;
+    float d = 0.0f;
+    if (k < nm && perm[k] >= 0) {
+      cell = cell_of_slot[k];
+      d = fabsf(__fsub_rn(pos[k * S], xkey[k]));
+    }
+    const unsigned act = __ballot_sync(0xffffffffu, cell >= 0);
+    if (cell >= 0) {
+      const unsigned peers = __match_any_sync(act, cell);
+      const int32_t mb = __reduce_max_sync(peers, __float_as_int(d));
+      if (lane == __ffs(peers) - 1 && mb > 0)
+        atomicMax(reinterpret_cast<int32_t*>(cell_delta) + PN_IDX(err, BC_CELL, cell, n_total),
+                  mb);
+    }
+  }
+}
+
 // After a rebuild the new structure is the main one: empty overflow lists, main_perm = perm.
 __global__ void __launch_bounds__(256)
 k_reset_overflow(const int32_t* __restrict__ start, int32_t n_total,
@@ -643,6 +676,7 @@ int build(pn_search* s, const T* y, int64_t n_y, const int32_t* idx, int64_t n_i
     launch_finalize<T>(s, y, (int32_t)m, st);
   }
   cudaMemsetAsync(s->d_err + ERR_DELTA, 0, sizeof(int32_t), st);
+  if (s->d_cell_delta) cudaMemsetAsync(s->d_cell_delta, 0, sizeof(float) * s->n_total, st);
   s->n_binned = m;
   s->pc_valid = false;
   s->ovf_active = false;
@@ -1151,6 +1185,7 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   cudaMemsetAsync(s->d_err + 1, 0, sizeof(int32_t), st);  // points outside the periodic box
   cudaMemsetAsync(s->d_err + ERR_DELTA, 0, sizeof(int32_t), st);
   cudaMemsetAsync(s->d_counts, 0, sizeof(int32_t) * s->n_total, st);  // the mark's histogram
+  if (s->d_cell_delta) cudaMemsetAsync(s->d_cell_delta, 0, sizeof(float) * s->n_total, st);
   const bool per = s->periodic != 0;
   switch (s->ndims * 2 + (per ? 1 : 0)) {
     case 2: launch_mark<T, 1, false>(s, y, st); break;
@@ -1164,6 +1199,17 @@ int update_incremental(pn_search* s, const T* y, int64_t n_y, cudaStream_t st) {
   k_decide_update<<<1, 32, 0, st>>>(s->d_ovf_n, s->d_start + s->n_total, s->rebuild_fraction,
                                     gate); count_launch();
   // overflow path
+  if (s->d_cell_delta != nullptr) {
+    const int b = std::max(1, std::min(div_up(s->n_binned, 256), 152 * 8));
+    const float* pos = static_cast<const float*>(s->d_pos);
+    const int32_t* nmain = s->d_start + s->n_total;
+    switch (s->ndims) {
+      case 1: k_cell_delta<1><<<b, 256, 0, st>>>(pos, s->d_xkey, s->d_perm, s->d_cell_of_slot, nmain, s->n_total, s->d_cell_delta, gate, s->d_err); break;
+      case 2: k_cell_delta<2><<<b, 256, 0, st>>>(pos, s->d_xkey, s->d_perm, s->d_cell_of_slot, nmain, s->n_total, s->d_cell_delta, gate, s->d_err); break;
+      default: k_cell_delta<4><<<b, 256, 0, st>>>(pos, s->d_xkey, s->d_perm, s->d_cell_of_slot, nmain, s->n_total, s->d_cell_delta, gate, s->d_err); break;
+    }
+    count_launch();
+  }
   scan_cells(s, s->d_ovf_counts, s->d_ovf_start, st, s->d_start + s->n_total, 0, gate,
              GATE_OVERFLOW, false);
   switch (s->ndims) {

@@ -83,6 +83,7 @@ struct pn_search {
   // rows are clipped by while the positions of the main slots move in place; the largest
   // distance of a main slot's x from its key is err word ERR_DELTA
   float* d_xkey = nullptr;             // [slots]
+  float* d_cell_delta = nullptr;       // [n_total] the largest |x - xkey| per cell
   // Float64 searches (not hashed): the third part of the coordinates' Float32 split
   // (x = pos32 + pos32lo + pos32lo2 exactly) and the double-float WCSPH state, for the
   // double-float sums of the 3D WCSPH sweeps

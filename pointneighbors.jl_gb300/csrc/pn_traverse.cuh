@@ -61,6 +61,7 @@ struct TravArgs {
   // clipped by their keys (their x: they are re-sorted at every update).
   const float* xkey;
   const float* delta;
+  const float* cell_delta;  // per cell the largest |x - xkey| of its main slots
   // Precomputed neighbour lists (or null: the grid traversal).  Groups of 32 rows are stored
   // transposed in quads: row r's entries 4k..4k+3 are the int4 at
   // nb[nb_grp[r / 32] + 128 k + 4 (r % 32)], so a warp reads its rows' k-th quads in one
@@ -1757,7 +1758,12 @@ __device__ __forceinline__ void traverse_query(const TravArgs<T>& a, const typen
         int32_t b0 = __ldg(&a.start[l0]), e0 = __ldg(&a.start[l0 + 3]);
         PN_RUN(a.err, b0, e0, a.bc_slots);
         if (clip) {
-          clip_row<T, D>(a, q, below, above, oy, oz, b0, e0, margin, keyed);
+          // the row's margin: the largest move in its three cells
+          T rm = margin;
+          if (keyed && a.cell_delta != nullptr)
+            rm = (T)fmaxf(fmaxf(__ldg(&a.cell_delta[l0]), __ldg(&a.cell_delta[l0 + 1])),
+                          __ldg(&a.cell_delta[l0 + 2]));
+          clip_row<T, D>(a, q, below, above, oy, oz, b0, e0, rm, keyed);
           if constexpr (has_row_hook<F>::value)
             F::row_begin(acc, p, q, (oz + OZ) * (2 * OY + 1) + (oy + OY), b0, e0);
         }

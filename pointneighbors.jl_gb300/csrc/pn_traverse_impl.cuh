@@ -316,6 +316,7 @@ static TravArgs<T> trav_args(const pn_search* s, const T* x, int64_t n_x, const 
   a.outside = s->d_err + 1;
   a.unsorted = s->d_err + 3;
   a.xkey = s->ovf_active ? s->d_xkey : nullptr;
+  a.cell_delta = s->ovf_active ? s->d_cell_delta : nullptr;
   a.delta = reinterpret_cast<const float*>(s->d_err + ERR_DELTA);
   if (s->hashed && !s->hash_dense) {  // the hash lists' traversal
     a.hash_list = s->d_hbucket;
