@@ -117,3 +117,57 @@ def test_pair_cache_adjoint(P):
     assert abs(float(out[0][1]) - float(out[1][1])) <= 1e-6 * abs(float(out[0][1]))
     g0, g1 = out[0][2], out[1][2]
     assert float((g0 - g1).abs().max() / g0.abs().max()) < 1e-4
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_keyed_clipping_with_overflow_lists(P, O, d):
+    """Float32 searches that keep overflow lists (rebuild_fraction 1) over a random walk
+    with large steps: the main slots move in place and the rows are clipped by the sort keys
+    widened by their cells' largest move; the pair cache records each row's main and overflow
+    runs.  After every update!: neighbour lists equal a fresh ParallelUpdate build, the
+    counts over the pair cache equal the oracle's, and the density equals the same search's
+    density without the cache bit for bit."""
+    side = 26 if d == 2 else 16
+    x0 = P.workloads.perturbed_lattice((side,) * d, 0.25, seed=7 + d, dtype=np.float32)
+    n = len(x0)
+    r = np.float32(3.0)
+    lo, hi = np.full(d, -4.0, np.float32), np.full(d, side + 4.0, np.float32)
+
+    def search(strategy, cache):
+        cl = P.FullGridCellList(min_corner=lo, max_corner=hi, search_radius=r,
+                                max_points_per_cell=0)
+        return P.GridNeighborhoodSearch(d, search_radius=r, n_points=n, cell_list=cl,
+                                        update_strategy=strategy, pair_cache=cache)
+
+    inc = search(P.ParallelIncrementalUpdate(1.0), 1)
+    inc_nc = search(P.ParallelIncrementalUpdate(1.0), 0)
+    fresh = search(P.ParallelUpdate(), 0)
+    xd = dcoords(x0)
+    P.initialize(inc, xd, xd)
+    P.initialize(inc_nc, xd, xd)
+    rng = np.random.default_rng(20 + d)
+    xs = x0.astype(np.float64)
+    W = P.workloads
+    consts = dict(W.WCSPH)
+    for _ in range(4):
+        xs = np.clip(xs + rng.normal(0.0, 0.4, xs.shape), 0.0, side)
+        x = xs.astype(np.float32)
+        xd = dcoords(x)
+        P.update(inc, xd, xd)
+        P.update(inc_nc, xd, xd)
+        P.initialize(fresh, xd, xd)
+        rho = [torch.zeros(n, device="cuda") for _ in range(2)]
+        prs = [torch.zeros(n, device="cuda") for _ in range(2)]
+        for k, nhs in enumerate((inc, inc_nc)):
+            P.foreach_point_neighbor(P.WCSPHDensity(density=rho[k], pressure=prs[k], **consts),
+                                     xd, xd, nhs)
+        assert torch.equal(rho[0], rho[1])
+        cnt = torch.zeros(n, dtype=torch.int32, device="cuda")
+        P.foreach_point_neighbor(P.CountNeighbors(cnt), xd, xd, inc)  # walks the cache
+        g = O.grid_create(d, r, lo, hi, dtype=np.float32)
+        ocnt = O.foreach(g, O.build(g, x), x, x, O.F_COUNT)
+        assert np.array_equal(cnt.cpu().numpy(), ocnt)
+        oi, ni = P.neighbor_lists(xd, xd, inc)
+        of, nf = P.neighbor_lists(xd, xd, fresh)
+        assert torch.equal(oi, of) and torch.equal(ni, nf)
+    assert inc.grid_info()["n_overflow"] > 0  # the overflow lists were in use
