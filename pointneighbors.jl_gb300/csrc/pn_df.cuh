@@ -108,14 +108,19 @@ __device__ __forceinline__ double df_to(df a) { return (double)a.hi + (double)a.
 
 // The exact difference (xa + xb + xc) - (ya + yb + yc) of two Float64 values given as their
 // three-part Float32 splits (x = xa + xb + xc exactly, each part the Float32 rounding of
-// what the previous parts leave), to double-float precision: the parts' differences are
-// taken exactly (two_sum) and added from the largest.
+// what the previous parts leave), to double-float precision: the two leading parts'
+// differences are taken exactly (two_sum) and summed exactly into hi + e; the remaining
+// terms (the two sums' errors, the third parts' difference and e) are each below an ulp of
+// the leading parts and are added in Float32, then renormalised -- within 2^-46 of the
+// difference (tests/test_df_arith.py checks this against exact rationals).
 __device__ __forceinline__ df df_diff3(float xa, float xb, float xc, float ya, float yb,
                                        float yc) {
   const df a = two_sum(xa, -ya);
   const df b = two_sum(xb, -yb);
-  const float c = __fsub_rn(xc, yc);
-  return df_add_f(df_add(a, b), c);
+  const df s = two_sum(a.hi, b.hi);
+  const float low =
+      __fadd_rn(__fadd_rn(__fadd_rn(a.lo, b.lo), __fsub_rn(xc, yc)), s.lo);
+  return fast_two_sum(s.hi, low);
 }
 
 }  // namespace pn

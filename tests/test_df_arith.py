@@ -85,19 +85,20 @@ def split3(x):
 def df_diff3(x, y):
     xa, xb, xc = split3(x)
     ya, yb, yc = split3(y)
-    a = two_sum(xa, f32(-ya))
-    b = two_sum(xb, f32(-yb))
-    c = f32(xc - yc)
-    return df_add_f(df_add(a, b), c)
+    s1, e1 = two_sum(xa, f32(-ya))
+    s2, e2 = two_sum(xb, f32(-yb))
+    s, e = two_sum(s1, s2)
+    low = f32(f32(f32(e1 + e2) + f32(xc - yc)) + e)
+    return fast_two_sum(s, low)
 
 
 def val(d):
     return Fraction(float(d[0])) + Fraction(float(d[1]))
 
 
-def _points(rng, n, scale):
+def _points(rng, n, scale, reach=3.0):
     x = rng.uniform(-scale, scale, size=(n, 3))
-    y = x + rng.uniform(-3.0, 3.0, size=(n, 3))
+    y = x + rng.uniform(-reach, reach, size=(n, 3))
     return x, y
 
 
@@ -113,8 +114,10 @@ def test_split3_is_exact():
 
 def test_diff3_and_d2_accuracy():
     rng = np.random.default_rng(2)
-    for scale in (200.0, 1e6):
-        x, y = _points(rng, 400, scale)
+    # lattice-sized coordinates, large offsets, coordinates on both sides of zero, and
+    # nearly coincident points far from the origin (the difference a few ulp of x)
+    for scale, reach in ((200.0, 3.0), (1e6, 3.0), (1.0, 3.0), (1e6, 1e-9)):
+        x, y = _points(rng, 400, scale, reach)
         for xi, yi in zip(x, y):
             pd = [df_diff3(xi[k], yi[k]) for k in range(3)]
             for k in range(3):
