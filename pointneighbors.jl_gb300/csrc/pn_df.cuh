@@ -54,6 +54,13 @@ __device__ __forceinline__ df df_add(df a, df b) {
   return fast_two_sum(s.hi, s.lo);
 }
 __device__ __forceinline__ df df_sub(df a, df b) { return df_add(a, df_neg(b)); }
+// a + b for a, b >= 0 (d^2, the density sum): nothing cancels, so the low parts need no
+// error term of their own
+__device__ __forceinline__ df df_add_pos(df a, df b) {
+  df s = two_sum(a.hi, b.hi);
+  s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+  return fast_two_sum(s.hi, s.lo);
+}
 __device__ __forceinline__ df df_add_f(df a, float b) {
   df s = two_sum(a.hi, b);
   s.lo = __fadd_rn(s.lo, a.lo);

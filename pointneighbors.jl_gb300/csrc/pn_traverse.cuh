@@ -707,7 +707,7 @@ struct FDensity {
     if (!(t.hi > 0.0f)) return;  // beyond the support 2h: the Float64 form adds a zero
     const df t2 = df_sqr(t);
     const df u = df_add_f(df_make(__fmul_rn(2.0f, q.hi), __fmul_rn(2.0f, q.lo)), 1.0f);
-    a.w = df_add(a.w, df_mul(df_sqr(t2), u));
+    a.w = df_add_pos(a.w, df_mul(df_sqr(t2), u));
   }
   static __device__ __forceinline__ void finish_df(AccDF& a, const Params& p, const Query<T, D>& q,
                                                    const DF64Geom& d) {
@@ -1377,7 +1377,7 @@ struct DF64 {
     pd[0] = df_diff3(q.x[0], a.xb[0], a.xc[0], ya.x, yb.x, yc.x);
     pd[1] = df_diff3(q.x[1], a.xb[1], a.xc[1], ya.y, yb.y, yc.y);
     pd[2] = df_diff3(q.x[2], a.xb[2], a.xc[2], ya.z, yb.z, yc.z);
-    const df d2 = df_add(df_add(df_sqr(pd[0]), df_sqr(pd[1])), df_sqr(pd[2]));
+    const df d2 = df_add_pos(df_add_pos(df_sqr(pd[0]), df_sqr(pd[1])), df_sqr(pd[2]));
     bool accept;
     if (df_lt(d2, p.d.k.r2_lo)) {
       accept = true;

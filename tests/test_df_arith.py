@@ -9,7 +9,8 @@ is restated here as Dekker's exact product (the same p + e = a b).  Checked:
 * d^2 formed from those differences is within 1e-13 of the exact d^2 -- far inside the
   1e-12 band outside which the double-float d^2 decides the neighbour test, so that the
   decision always equals the Float64 one;
-* df_mul / df_add / df_sqr keep 2^-44 relative accuracy on WCSPH-sized operands.
+* df_mul / df_add / df_add_pos (non-negative operands) / df_sqr keep 2^-44 relative
+  accuracy on WCSPH-sized operands.
 """
 from fractions import Fraction
 
@@ -52,6 +53,13 @@ def df_add(a, b):
     s, se = fast_two_sum(s, se)
     se = f32(se + te)
     return fast_two_sum(s, se)
+
+
+def df_add_pos(a, b):
+    """the sum of two non-negative values (d^2, the density): no cancellation"""
+    s, e = two_sum(a[0], b[0])
+    e = f32(e + f32(a[1] + b[1]))
+    return fast_two_sum(s, e)
 
 
 def df_add_f(a, b):
@@ -124,7 +132,7 @@ def test_diff3_and_d2_accuracy():
                 exact = Fraction(float(xi[k])) - Fraction(float(yi[k]))
                 if exact != 0:
                     assert abs(val(pd[k]) - exact) <= abs(exact) * Fraction(1, 2**46)
-            d2 = df_add(df_add(df_sqr(pd[0]), df_sqr(pd[1])), df_sqr(pd[2]))
+            d2 = df_add_pos(df_add_pos(df_sqr(pd[0]), df_sqr(pd[1])), df_sqr(pd[2]))
             exact = sum((Fraction(float(xi[k])) - Fraction(float(yi[k])))**2 for k in range(3))
             # the Float64 d^2 is within ~4 ulp (1e-15) of the exact one; the band is 1e-12
             assert abs(val(d2) - exact) <= exact * Fraction(1, 10**13)
@@ -138,5 +146,5 @@ def test_mul_add_accuracy():
         b = (f32(v), f32(v - float(f32(v))))
         exact_a, exact_b = val(a), val(b)
         for got, exact in ((df_mul(a, b), exact_a * exact_b), (df_add(a, b), exact_a + exact_b),
-                           (df_sqr(a), exact_a * exact_a)):
+                           (df_add_pos(a, b), exact_a + exact_b), (df_sqr(a), exact_a * exact_a)):
             assert abs(val(got) - exact) <= abs(exact) * Fraction(1, 2**44)
