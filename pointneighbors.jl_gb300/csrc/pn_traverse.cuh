@@ -1836,6 +1836,12 @@ template <int D, class G>
 struct trav_blocks<Exact64<D, G>> { static constexpr int value = 5; };
 template <int D, class G>
 struct trav_blocks<DF64<D, G>> { static constexpr int value = 5; };
+// the recording sweep of the double-float density: mostly the Float32 traversal (its
+// double-float work only for the rare band candidates), so it keeps 8 blocks per SM
+template <>
+struct trav_blocks<DF64<3, WithMask<double, 3, FNone<double, 3>>>> {
+  static constexpr int value = 8;
+};
 
 template <typename T, int D, bool PER, class F>
 __global__ void __launch_bounds__(TRAV_THREADS, trav_blocks<F>::value)
