@@ -449,10 +449,9 @@ int pn_batch_sync(pn_batch* b);
  *  - Limit: 4 bytes per cell of the padded grid + 12 bytes per point + 20 bytes must fit
  *    PN_NOALLOC_SCRATCH_BYTES, else PN_ERR_SCRATCH_LIMIT (nothing is launched).
  *  - The first call on a device (the current one) looks up the scratch's address there,
- *    which can load the library's module: make that first call before any stream capture.
- *    The address is kept per device for the life of the process; after cudaDeviceReset
- *    the module is loaded anew (possibly elsewhere), so do not call this entry point
- *    again in a process that reset the device.
+ *    which can load the library's module: make that first call before any stream capture
+ *    (and again after a cudaDeviceReset).  Every call looks the address up anew, so a
+ *    module loaded elsewhere after a reset is found.
  *  - Every call shares the scratch, which keeps the last call's contents (each call clears
  *    what must start at zero); calls that overlap on the GPU race, so serialise calls made
  *    from several host threads or streams.

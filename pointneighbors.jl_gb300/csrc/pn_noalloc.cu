@@ -24,8 +24,8 @@
 //
 // Set-up.  The first call on a device (the device current on the calling thread) looks up
 // the array's device address with cudaGetSymbolAddress, which can load the module; that
-// first call should therefore come before any stream capture on that device.  The address
-// is cached per device.
+// first call should therefore come before any stream capture on that device.  Later calls
+// look the address up again, which allocates nothing.
 //
 // Sharing.  Every call on a device uses the same array and the array keeps the contents of
 // the last call; the kernel clears what must start at zero (the error word and the per-cell
@@ -36,7 +36,6 @@
 // barriers between its phases and no block waits on another).  It is meant for the point
 // sets that fit the scratch (up to about 340,000 points), not as the fast path: the
 // pn_search traversal is.
-#include <mutex>
 
 #include "pn_traverse.cuh"
 
@@ -178,26 +177,17 @@ k_count_noalloc(GridDev<T> g, const T* __restrict__ x, int32_t n, int32_t max_pp
   }
 }
 
-std::mutex g_setup_mutex;
-constexpr int NA_MAX_DEVICES = 64;
-void* g_scratch_ptr[NA_MAX_DEVICES] = {};
-
-// The scratch array's address on the current device, looked up on the first call there.
+// The scratch array's address on the current device.  It is looked up on every call (after
+// the module is loaded the lookup allocates nothing), so that it stays right when the device
+// was reset and the module loaded anew elsewhere.
 int scratch_on_current_device(int32_t** out) {
-  int dev = -1;
-  if (cudaGetDevice(&dev) != cudaSuccess) return PN_ERR_CUDA;
-  if (dev < 0 || dev >= NA_MAX_DEVICES) return PN_ERR_INVALID_ARG;
-  std::lock_guard<std::mutex> lock(g_setup_mutex);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, pn_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      cudaGetLastError();
-      return PN_ERR_CUDA;
-    }
-    g_scratch_ptr[dev] = p;
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, pn_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) {
+    cudaGetLastError();
+    return PN_ERR_CUDA;
   }
-  *out = (int32_t*)g_scratch_ptr[dev];
+  *out = (int32_t*)p;
   return PN_OK;
 }
 
