@@ -748,12 +748,14 @@ struct FForce {
     }
   }
   // In 3D the traversal reads the candidates from the state (x, y, z, p/rho^2), and `aux`
-  // is the candidate's p/rho^2; otherwise it is loaded here.
+  // is the candidate's p/rho^2; otherwise it is loaded here.  The neighbour's (v, rho) is
+  // loaded before the r_min test, so that its gather is in flight together with the
+  // coordinates' instead of after them.
   static __device__ __forceinline__ void pair(Acc& a, const Params& p, const Query<T, D>&, int32_t js,
                                               const T* pd, T d2, T aux) {
+    const V4<T> sb = load4(p.pb, js);
     if (d2 < p.c.r_min2) return;
     const T Pj = D == 3 ? aux : load4(p.pa, js).w;
-    const V4<T> sb = load4(p.pb, js);
     const T vj[3] = {sb.x, sb.y, sb.z};
     const T q = fsqrt(d2) * p.c.inv_h;
     const T t = fmax((T)1 - (T)0.5 * q, (T)0);  // zero beyond the support 2h
