@@ -415,10 +415,16 @@ struct WithMask {
   // lo, hi: the row's main run from b0; om: its overflow run from ob0 (ovf: the row's
   // candidates now come from the overflow run); ovf_any: the overflow masks are written.
   // FA: F's accumulator (F::Acc, or F::AccDF for the double-float sums of DF64).
+  // kShift: F can take the main runs in groups (the Float32 3D density).  For a row that
+  // comes in groups, (hi, lo) is a 128-bit shift register: each group's hit bits enter at
+  // the top, and the row's flush shifts the register down by `sh` = 128 - GROUP x (the
+  // row's groups), which puts candidate b0 + t at bit t as record() does (sh = 0 for a row
+  // recorded one candidate at a time).
+  static constexpr bool kShift = has_group<F>::value && D == 3 && sizeof(T) == 4;
   template <class FA>
   struct AccT {
     FA f;
-    int32_t ri, b0, ob0;
+    int32_t ri, b0, ob0, sh;
     uint64_t lo, hi, om;
     bool fb, ovf, ovf_any;
   };
@@ -429,7 +435,7 @@ struct WithMask {
   template <class A>
   static __device__ __forceinline__ void init_mask(A& a, const Params& p) {
     a.ri = -1;
-    a.b0 = a.ob0 = 0;
+    a.b0 = a.ob0 = a.sh = 0;
     a.lo = a.hi = a.om = 0;
     a.fb = a.ovf = false;
     a.ovf_any = p.m.ob0 != nullptr && __ldg(p.m.ovf_end) > __ldg(p.m.main_end);
@@ -441,6 +447,18 @@ struct WithMask {
   template <class A>
   static __device__ __forceinline__ void flush(A& a, const Params& p, const Query<T, D>& q) {
     if (a.ri < 0) return;
+    if constexpr (kShift) {
+      // align the shift register (sh < 0: more than 128 slots, the query is marked for
+      // the fallback and its masks are not read)
+      const int sh = a.sh;
+      if (sh >= 64) {
+        a.lo = sh >= 128 ? 0ull : a.hi >> (sh - 64);
+        a.hi = 0ull;
+      } else if (sh > 0) {
+        a.lo = (a.lo >> sh) | (a.hi << (64 - sh));
+        a.hi >>= sh;
+      }
+    }
     const int64_t o =
         (int64_t)a.ri * p.m.stride + PN_IDX(p.m.err, BC_PAIR_CACHE, q.k, p.m.stride);
     p.m.b0[o] = a.b0;
@@ -450,15 +468,19 @@ struct WithMask {
       if (a.om != 0) p.m.omask[o] = a.om;
     }
   }
+  // grouped: the run comes in groups (the traversal calls F directly); a wrapper that
+  // decides the candidates itself (mixed precision, Float64) records them one by one
   template <class A>
   static __device__ __forceinline__ void row_begin(A& a, const Params& p, const Query<T, D>& q,
-                                                   int ri, int32_t b0, int32_t e0) {
+                                                   int ri, int32_t b0, int32_t e0,
+                                                   bool grouped = kShift) {
     flush(a, p, q);
     a.ri = ri;
     a.b0 = b0;
     a.lo = a.hi = a.om = 0;
     a.ovf = false;
     if (e0 - b0 > 128) a.fb = true;
+    if constexpr (kShift) a.sh = grouped ? 128 - GROUP * ((max(e0 - b0, 0) + GROUP - 1) / GROUP) : 0;
   }
   // the row's overflow run [ob0, oe0) follows its main run
   template <class A>
@@ -511,9 +533,11 @@ struct WithMask {
     uint32_t hits = 0u;
 #pragma unroll
     for (int u = 0; u < GROUP; ++u) hits |= d2[u] <= r2 ? 1u << u : 0u;
-    const uint32_t off = (uint32_t)(js0 - a.b0);  // main runs only (overflow runs: pair())
-    if (off < 64) a.lo |= (uint64_t)hits << off;
-    else if (off < 128) a.hi |= (uint64_t)hits << (off - 64);
+    // main runs only (overflow runs: pair()), group by group from b0: into the top of the
+    // shift register
+    static_assert(kShift, "groups are taken only by the Float32 3D density");
+    a.lo = (a.lo >> GROUP) | (a.hi << (64 - GROUP));
+    a.hi = (a.hi >> GROUP) | ((uint64_t)hits << (64 - GROUP));
   }
   static __device__ __forceinline__ void finish(Acc& a, const Params& p, const Query<T, D>& q) {
     F::finish(a.f, p.f, q);
@@ -1148,7 +1172,7 @@ struct MixedFast {
   static __device__ __forceinline__ void row_begin(Acc& a, const Params& p,
                                                    const Query<float, D>& q, int ri, int32_t b0,
                                                    int32_t e0) {
-    if constexpr (kRowHook) F::row_begin(a.f, p.f, q, ri, b0, e0);
+    if constexpr (kRowHook) F::row_begin(a.f, p.f, q, ri, b0, e0, false);
   }
   static __device__ __forceinline__ void no_rows(Acc& a) {
     if constexpr (kRowHook) F::no_rows(a.f);
@@ -1272,7 +1296,7 @@ struct Exact64 {
   static __device__ __forceinline__ void row_begin(Acc& a, const Params& p,
                                                    const Query<float, D>& q, int ri, int32_t b0,
                                                    int32_t e0) {
-    if constexpr (kRowHook) F::row_begin(a.f, p.f, wide(q, a.x), ri, b0, e0);
+    if constexpr (kRowHook) F::row_begin(a.f, p.f, wide(q, a.x), ri, b0, e0, false);
   }
   static __device__ __forceinline__ void no_rows(Acc& a) {
     if constexpr (kRowHook) F::no_rows(a.f);
@@ -1353,7 +1377,7 @@ struct DF64 {
                                                    int32_t e0) {
     if constexpr (kRowHook) {
       const double z[D] = {};
-      F::row_begin(a.f, p.f, wide(q, z), ri, b0, e0);
+      F::row_begin(a.f, p.f, wide(q, z), ri, b0, e0, false);
     }
   }
   static __device__ __forceinline__ void no_rows(Acc& a) {
