@@ -477,7 +477,9 @@ def run_gpu(args, rank, world, local):
                             else "hash lists") if hashing else "full grid"),
                 "algorithmic_bytes_per_launch": alg,
                 "note": ("force over the pair cache's hit masks and density + masks: "
-                         "issue-bound (ncu issue slots 76 % / 87 %, DRAM 5 %)"
+                         "issue- and latency-bound (ncu at 4.1M points: issue slots 79 % / "
+                         "88 %, L1 wavefronts 68 % / 71 %, DRAM < 5 % of peak; the force "
+                         "walk waits on its neighbours' gathers)"
                          if args.pair_cache > 0 else
                          "issue-bound, not HBM-bound: ncu issue slots active 83 % (force), "
                          "93 % (density), DRAM < 2 % of peak")}
